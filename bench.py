@@ -1,0 +1,354 @@
+#!/usr/bin/env python3
+"""PDLP throughput on one GB300 (libcoolpdlp_cuda).
+
+Workload: the large single LP -- m = 2,000,000 rows, n = 4,000,000 columns,
+~24M nonzeros with power-law row lengths (tail 1.5, capped at 20,000), row
+factors log-uniform in [1e-3, 1e3], seed 1 -- solved by PDLP with FP32
+iterates and FP64 KKT reductions.  Seeded synthetic input (the reference
+publishes no benchmark data).
+
+A "step" is one block of solve!: check_every = 100 PDLP iterations plus one
+termination/restart check (four-iterate KKT pass).  `value` = iterations/s
+with the LP resident in HBM, timed with CUDA events on the library's stream;
+`e2e` = iterations/s through cpdlp_solve with the LP in pinned host memory
+(upload, scaling, power method, 1,000 iterations, download all inside the
+timed region).  The working set (~0.6 GB per iteration) is larger than L2,
+so no flush is needed between steps.
+
+--impl reference times the CPU restatement of the reference algorithm
+(oracle/, Float64, all host threads) on the same LP.
+Under torchrun with N ranks every rank solves its own copy (one LP does not
+shard): value = all ranks' iterations / the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "coolpdlp.jl_gb300"))
+
+METRIC = "PDHG iters/s (HBM GB/s) and LPs/s to 1e-4 rel KKT; p50/p99 solve latency"
+UNIT = "iters/s"
+CHECK_EVERY = 100
+E2E_ITERS = 1000
+
+
+def parse_args():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="shrink the workload (testing only; 1.0 = the named workload)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    return ap.parse_args()
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def workload(scale: float):
+    from coolpdlp import generators as G
+    m = int(2_000_000 * scale)
+    n = 2 * m
+    nnz = int(24_000_000 * scale)
+    return G.powerlaw_lp(m, n, nnz, seed=1, cap=min(20000, n))
+
+
+def workload_config(lp, scale):
+    return {
+        "workload": (f"power-law single LP m={lp.m:,} n={lp.n:,} nnz={lp.nnz:,} "
+                     "(row lengths tail 1.5 capped at 20,000; row factors log-U[1e-3,1e3]; seed 1)"),
+        "algorithm": "PDLP", "iterates": "FP32", "kkt_reductions": "FP64",
+        "step": f"{CHECK_EVERY} PDLP iterations + one termination/restart check",
+        "l2": "inputs larger than L2 (~0.6 GB moved per iteration), no flush",
+        "scale": scale,
+    }
+
+
+def load_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.device)], stdout=self.out, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.out.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    mx.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(lp, budget_s: float = 20.0) -> dict:
+    """The oracle (CPU restatement, FP64, all host threads) on the same LP:
+    preprocessing untimed, then whole 100-iteration blocks until ~budget_s."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    prm = O.params(termination_reltol=0.0, max_kkt_passes=1 << 60, time_limit=1e30)
+    t0 = time.perf_counter()
+    S = O.OracleState(lp, prm)
+    t_setup = time.perf_counter() - t0
+    iters, t = 0, 0.0
+    while t < budget_s and iters < 100 * 50:
+        a = time.perf_counter()
+        S.step(10)
+        t += time.perf_counter() - a
+        iters += 10
+    S.close()
+    return {"value": iters / t, "unit": UNIT, "cores": int(O.lib().orc_num_threads()),
+            "kind": "port",
+            "sample": (f"{iters} PDLP iterations (FP64) of the same LP after "
+                       f"{t_setup:.1f} s of untimed preprocessing"), "seconds": t}
+
+
+def run_reference(args):
+    ws, rank, local = dist_info()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    lp = workload(args.scale)
+    prm = O.params(termination_reltol=0.0, max_kkt_passes=1 << 60, time_limit=1e30)
+    S = O.OracleState(lp, prm)
+    per_step = 10  # a bounded sample of the 100-iteration block
+    for _ in range(args.warmup):
+        S.step(per_step)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        S.step(per_step)
+    dt = time.perf_counter() - t0
+    S.close()
+    v = args.steps * per_step / dt
+    cores = int(O.lib().orc_num_threads())
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": workload_config(lp, args.scale),
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{per_step} PDLP iterations per step (FP64, step! only)"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    ws, rank, local = dist_info()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group(backend="nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    from coolpdlp import build as B
+    B.build_library()
+    from coolpdlp import _abi as A
+    from coolpdlp import native
+
+    lp = workload(args.scale)
+    h = native.Handle(local)
+    prm = A.default_params_py(A.ALGO_PDLP)
+    prm.float_type = A.VAL_F32
+    prm.termination_reltol = 0.0
+    prm.max_kkt_passes = 1 << 60
+    prm.time_limit = 1e30
+    L = native.LPStruct(lp.m, lp.n, lp.colptr, lp.rowval, lp.nzval, lp.c, lp.lv, lp.uv, lp.lc,
+                        lp.uc)
+    t0 = time.perf_counter()
+    P = native.Problem(h, L, prm)
+    S = native.State(P, prm)
+    setup_s = time.perf_counter() - t0
+    ext = torch.cuda.ExternalStream(h.stream, device=torch.device("cuda", local))
+
+    for _ in range(args.warmup):
+        S.solve_blocks(1)
+    launches0 = S.stats().kernel_launches
+    clk = ClockSampler(local)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    h.synchronize()
+    clk.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    w0 = time.perf_counter()
+    for _ in range(args.steps):
+        S.solve_blocks(1)
+    e1.record(ext)
+    h.synchronize()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - w0
+    clocks = clk.stop()
+    ms = e0.elapsed_time(e1)
+    launches = S.stats().kernel_launches - launches0
+    ms_max = ms
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_max = float(t.item())
+        torch.distributed.barrier()
+    iters = args.steps * CHECK_EVERY
+    value = ws * iters / (ms_max * 1e-3)
+
+    # roofline of the dominant kernel: live CUDA-event timing per kernel
+    prof = S.profile(20)
+    kb = S.kernel_bytes()
+    names = ["primal_step", "dual_step", "kkt4"]
+    per_step_ms = [prof[0] * CHECK_EVERY, prof[1] * CHECK_EVERY, prof[2]]
+    dom = int(np.argmax(per_step_ms))
+    peak, peak_kind = load_peak()
+    kernels = {}
+    for i, nm in enumerate(names):
+        gbs = kb[i] / (prof[i] * 1e-3) / 1e9
+        kernels[nm] = {"ms": prof[i], "bytes": kb[i], "gbs": gbs, "frac": gbs / peak,
+                       "share_of_step": per_step_ms[i] / sum(per_step_ms)}
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic_powerlaw_fp32.json")
+    if os.path.exists(tp) and args.scale == 1.0:
+        try:
+            with open(tp) as f:
+                traffic = json.load(f).get(names[dom])
+        except Exception:
+            traffic = None
+    ach = kernels[names[dom]]["gbs"]
+    roofline = {"bound": "hbm", "kernel": names[dom], "achieved": ach, "peak": peak,
+                "peak_source": peak_kind, "unit": "GB/s", "frac": ach / peak, "traffic": traffic}
+    step_bytes = kb[0] * CHECK_EVERY + kb[1] * CHECK_EVERY + kb[2]
+    hbm_gbs_whole = step_bytes * args.steps / (ms * 1e-3) / 1e9
+
+    # e2e through cpdlp_solve with pinned host buffers
+    def pinned(a, dt):
+        t = torch.empty(a.shape, dtype=dt, pin_memory=True)
+        t.numpy()[...] = a
+        return t
+    pins = [pinned(lp.colptr, torch.int64), pinned(lp.rowval, torch.int64),
+            pinned(lp.nzval, torch.float64), pinned(lp.c, torch.float64),
+            pinned(lp.lv, torch.float64), pinned(lp.uv, torch.float64),
+            pinned(lp.lc, torch.float64), pinned(lp.uc, torch.float64)]
+    Lp = native.LPStruct(lp.m, lp.n, *[p.numpy() for p in pins])
+    xo = torch.empty(lp.n, dtype=torch.float64, pin_memory=True)
+    yo = torch.empty(lp.m, dtype=torch.float64, pin_memory=True)
+    prm_e = A.ParamsC.from_buffer_copy(prm)
+    prm_e.max_kkt_passes = E2E_ITERS
+    import ctypes
+    def e2e_once():
+        st = A.StatsC()
+        h.check(h.lib.cpdlp_solve(h.h, ctypes.byref(Lp.s), ctypes.byref(prm_e), None, None,
+                                  native._pd(xo.numpy()), native._pd(yo.numpy()),
+                                  ctypes.byref(st)), "cpdlp_solve")
+        return st
+    e2e_val = None
+    if args.e2e_steps > 0:
+        del S, P
+        e2e_once()  # warm-up
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(args.e2e_steps):
+            a = time.perf_counter()
+            st = e2e_once()
+            ts.append(time.perf_counter() - a)
+        t_e2e = statistics.mean(ts)
+        if ws > 1:
+            t = torch.tensor([t_e2e], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            t_e2e = float(t.item())
+        e2e_val = ws * st.kkt_passes / t_e2e
+    h2d = (lp.n + 1) * 8 + lp.nnz * 16 + (3 * lp.n + 2 * lp.m) * 8
+    d2h = (lp.n + lp.m) * 8 + ctypes.sizeof(A.StatsC)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": workload_config(lp, args.scale),
+            "hbm_gbs": hbm_gbs_whole,
+            "roofline": roofline, "kernels": kernels,
+            "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h,
+                    "what": f"cpdlp_solve of the LP from pinned host buffers, {E2E_ITERS} iterations"},
+            "gpu_launches": int(launches),
+            "clocks": clocks,
+            "wall_s_timed": wall, "setup_s": setup_s,
+        }
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(lp)
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

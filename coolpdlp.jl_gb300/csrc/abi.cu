@@ -1,0 +1,335 @@
+// abi.cu -- the extern "C" entry points of libcoolpdlp_cuda (include/coolpdlp_cuda.h).
+// Each converts cpdlp::Error / std::exception into a status code and stores
+// the message in the handle.
+#include <memory>
+#include <new>
+
+#include "batch.cuh"
+#include "matrix.cuh"
+#include "solver.cuh"
+
+using namespace cpdlp;
+
+struct cpdlp_handle : Handle {};
+
+namespace {
+
+inline Handle* H(cpdlp_handle* h) { return static_cast<Handle*>(h); }
+
+template <class F>
+int guarded(cpdlp_handle* h, F&& f) {
+    try {
+        if (h) CK(cudaSetDevice(h->device));
+        f();
+        if (h) h->last_error.clear();
+        return CPDLP_OK;
+    } catch (const Error& e) {
+        if (h) h->last_error = e.what();
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        if (h) h->last_error = "host allocation failed";
+        return CPDLP_ERR_OUT_OF_MEMORY;
+    } catch (const std::exception& e) {
+        if (h) h->last_error = e.what();
+        return CPDLP_ERR_CUDA;
+    }
+}
+
+#define NEED(h) \
+    if (!(h)) return CPDLP_ERR_ARGUMENT
+
+}  // namespace
+
+extern "C" {
+
+int cpdlp_abi_version(void) { return CPDLP_ABI_VERSION; }
+
+void cpdlp_params_default(cpdlp_params* p, int32_t algorithm) {
+    if (!p) return;
+    memset(p, 0, sizeof(*p));
+    const bool pdhg = algorithm == CPDLP_ALGO_PDHG;
+    p->algorithm = pdhg ? CPDLP_ALGO_PDHG : CPDLP_ALGO_PDLP;
+    p->float_type = CPDLP_VAL_F64;
+    p->chambolle_pock_alpha = 1.0;
+    p->ruiz_iter = pdhg ? 0 : 10;
+    p->invnorm_scaling = 0.9;
+    p->primal_weight_damping = pdhg ? NAN : 0.5;
+    p->zero_tol = 1e-8;
+    p->sufficient_decay = pdhg ? NAN : 0.2;
+    p->necessary_decay = pdhg ? NAN : 0.8;
+    p->artificial_decay = pdhg ? NAN : 0.36;
+    p->show_progress = 0;
+    p->check_every = 100;
+    p->record_error_history = 1;
+    p->termination_reltol = 1e-4;
+    p->max_kkt_passes = 100000;
+    p->time_limit = 100.0;
+    p->power_tol_override = 0.0;
+    p->power_maxiter_override = 0;
+    p->power_seed = 0;
+    p->refine_reltol = 0.0;
+    p->tile_nnz = 0;
+}
+
+int cpdlp_create(int32_t device, cpdlp_handle** out) {
+    if (!out) return CPDLP_ERR_ARGUMENT;
+    *out = nullptr;
+    cpdlp_handle* h = new (std::nothrow) cpdlp_handle();
+    if (!h) return CPDLP_ERR_OUT_OF_MEMORY;
+    h->device = device;
+    int rc = guarded(h, [&] {
+        int count = 0;
+        CK(cudaGetDeviceCount(&count));
+        if (device < 0 || device >= count) fail(CPDLP_ERR_ARGUMENT, "no such CUDA device");
+        CK(cudaSetDevice(device));
+        CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+        CK(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, device));
+    });
+    if (rc != CPDLP_OK) {
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return CPDLP_OK;
+}
+
+int cpdlp_destroy(cpdlp_handle* h) {
+    NEED(h);
+    cudaSetDevice(h->device);
+    if (h->stream) {
+        cudaStreamSynchronize(h->stream);
+        cudaStreamDestroy(h->stream);
+    }
+    if (h->pinned) cudaFreeHost(h->pinned);
+    delete h;
+    return CPDLP_OK;
+}
+
+const char* cpdlp_last_error(const cpdlp_handle* h) {
+    if (!h) return "null handle";
+    return h->last_error.c_str();
+}
+
+int cpdlp_synchronize(cpdlp_handle* h) {
+    NEED(h);
+    return guarded(h, [&] { CK(cudaStreamSynchronize(h->stream)); });
+}
+
+void* cpdlp_stream(cpdlp_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+// ---- matrices ----
+int cpdlp_matrix_from_csc(cpdlp_handle* h, int64_t m, int64_t n, int64_t nnz,
+                          const int64_t* colptr, const int64_t* rowval, const double* nzval,
+                          int32_t format, int32_t value_type, cpdlp_matrix** out) {
+    NEED(h);
+    if (!out) return CPDLP_ERR_ARGUMENT;
+    *out = nullptr;
+    return guarded(h, [&] {
+        Matrix* M = matrix_from_csc(*H(h), m, n, nnz, colptr, rowval, nzval, format, value_type);
+        *out = reinterpret_cast<cpdlp_matrix*>(M);
+    });
+}
+
+int cpdlp_matrix_destroy(cpdlp_matrix* A) {
+    if (!A) return CPDLP_ERR_ARGUMENT;
+    Matrix* M = reinterpret_cast<Matrix*>(A);
+    cudaSetDevice(M->h->device);
+    cudaStreamSynchronize(M->h->stream);
+    delete M;
+    return CPDLP_OK;
+}
+
+int cpdlp_matrix_shape(const cpdlp_matrix* A, int64_t* m, int64_t* n, int64_t* nnz,
+                       int64_t* width) {
+    if (!A) return CPDLP_ERR_ARGUMENT;
+    const Matrix* M = reinterpret_cast<const Matrix*>(A);
+    if (m) *m = M->m;
+    if (n) *n = M->n;
+    if (nnz) *nnz = M->nnz;
+    if (width) *width = M->width;
+    return CPDLP_OK;
+}
+
+int cpdlp_matrix_export(cpdlp_handle* h, const cpdlp_matrix* A, int64_t* ptr, int64_t* idx,
+                        double* val) {
+    NEED(h);
+    if (!A) return CPDLP_ERR_ARGUMENT;
+    return guarded(h, [&] { matrix_export(*H(h), *reinterpret_cast<const Matrix*>(A), ptr, idx, val); });
+}
+
+int cpdlp_spmv(cpdlp_handle* h, const cpdlp_matrix* A, const void* b, void* c, double alpha,
+               double beta) {
+    NEED(h);
+    if (!A) return CPDLP_ERR_ARGUMENT;
+    return guarded(h, [&] {
+        matrix_spmv(*H(h), *reinterpret_cast<const Matrix*>(A), b, c, alpha, beta);
+        CK(cudaStreamSynchronize(h->stream));
+    });
+}
+
+// ---- solve path ----
+int cpdlp_problem_create(cpdlp_handle* h, const cpdlp_lp* lp, const cpdlp_params* params,
+                         cpdlp_problem** out) {
+    NEED(h);
+    if (!out) return CPDLP_ERR_ARGUMENT;
+    *out = nullptr;
+    return guarded(h, [&] {
+        *out = reinterpret_cast<cpdlp_problem*>(problem_create(*H(h), lp, params));
+    });
+}
+
+int cpdlp_problem_destroy(cpdlp_problem* p) {
+    if (!p) return CPDLP_ERR_ARGUMENT;
+    ProblemBase* P = reinterpret_cast<ProblemBase*>(p);
+    cudaSetDevice(P->h->device);
+    cudaStreamSynchronize(P->h->stream);
+    delete P;
+    return CPDLP_OK;
+}
+
+int cpdlp_problem_scaling(cpdlp_handle* h, const cpdlp_problem* p, double* d1, double* d2) {
+    NEED(h);
+    if (!p) return CPDLP_ERR_ARGUMENT;
+    return guarded(h, [&] {
+        problem_scaling(*H(h), const_cast<ProblemBase*>(reinterpret_cast<const ProblemBase*>(p)), d1, d2);
+    });
+}
+
+int cpdlp_problem_spectral_norm(cpdlp_handle* h, cpdlp_problem* p, const cpdlp_params* params,
+                                double* norm, int64_t* iterations) {
+    NEED(h);
+    if (!p || !params) return CPDLP_ERR_ARGUMENT;
+    return guarded(h, [&] {
+        double v = problem_spectral_norm(*H(h), reinterpret_cast<ProblemBase*>(p), params, iterations);
+        if (norm) *norm = v;
+    });
+}
+
+int cpdlp_state_create(cpdlp_handle* h, cpdlp_problem* p, const cpdlp_params* params,
+                       const double* x0, const double* y0, cpdlp_state** out) {
+    NEED(h);
+    if (!out) return CPDLP_ERR_ARGUMENT;
+    *out = nullptr;
+    return guarded(h, [&] {
+        *out = reinterpret_cast<cpdlp_state*>(
+            state_create(*H(h), reinterpret_cast<ProblemBase*>(p), params, x0, y0));
+    });
+}
+
+int cpdlp_state_destroy(cpdlp_state* s) {
+    if (!s) return CPDLP_ERR_ARGUMENT;
+    StateBase* S = reinterpret_cast<StateBase*>(s);
+    cudaSetDevice(S->P->h->device);
+    cudaStreamSynchronize(S->P->h->stream);
+    delete S;
+    return CPDLP_OK;
+}
+
+int cpdlp_state_solve(cpdlp_handle* h, cpdlp_state* s, cpdlp_stats* stats) {
+    NEED(h);
+    if (!s) return CPDLP_ERR_ARGUMENT;
+    return guarded(h, [&] {
+        StateBase* S = reinterpret_cast<StateBase*>(s);
+        S->solve();
+        if (stats) S->stats(stats);
+    });
+}
+
+int cpdlp_state_solve_blocks(cpdlp_handle* h, cpdlp_state* s, int64_t max_blocks,
+                             cpdlp_stats* stats) {
+    NEED(h);
+    if (!s || max_blocks < 0) return CPDLP_ERR_ARGUMENT;
+    return guarded(h, [&] {
+        StateBase* S = reinterpret_cast<StateBase*>(s);
+        S->solve_blocks(max_blocks);
+        if (stats) S->stats(stats);
+    });
+}
+
+int cpdlp_state_profile(cpdlp_handle* h, cpdlp_state* s, int32_t reps, double* ms) {
+    NEED(h);
+    if (!s || !ms || reps <= 0) return CPDLP_ERR_ARGUMENT;
+    return guarded(h, [&] { reinterpret_cast<StateBase*>(s)->profile(reps, ms); });
+}
+
+int cpdlp_state_kernel_bytes(const cpdlp_state* s, double* bytes) {
+    if (!s || !bytes) return CPDLP_ERR_ARGUMENT;
+    reinterpret_cast<const StateBase*>(s)->kernel_bytes(bytes);
+    return CPDLP_OK;
+}
+
+int cpdlp_state_step(cpdlp_handle* h, cpdlp_state* s, int64_t count) {
+    NEED(h);
+    if (!s || count < 0) return CPDLP_ERR_ARGUMENT;
+    return guarded(h, [&] { reinterpret_cast<StateBase*>(s)->step(count); });
+}
+
+int cpdlp_state_kkt(cpdlp_handle* h, cpdlp_state* s, int32_t which, cpdlp_kkt_errors* err) {
+    NEED(h);
+    if (!s || !err || which < 0 || which > CPDLP_VEC_SOL_RESTART) return CPDLP_ERR_ARGUMENT;
+    return guarded(h, [&] { reinterpret_cast<StateBase*>(s)->kkt(which, err); });
+}
+
+int cpdlp_state_vectors(cpdlp_handle* h, const cpdlp_state* s, int32_t which, double* x,
+                        double* y) {
+    NEED(h);
+    if (!s || which < 0 || which > CPDLP_VEC_SOL_RESTART) return CPDLP_ERR_ARGUMENT;
+    return guarded(h, [&] {
+        const_cast<StateBase*>(reinterpret_cast<const StateBase*>(s))->vectors(which, x, y);
+    });
+}
+
+int cpdlp_state_solution(cpdlp_handle* h, const cpdlp_state* s, double* x, double* y) {
+    NEED(h);
+    if (!s) return CPDLP_ERR_ARGUMENT;
+    return guarded(h, [&] {
+        const_cast<StateBase*>(reinterpret_cast<const StateBase*>(s))->solution(x, y);
+    });
+}
+
+int cpdlp_state_stats(cpdlp_handle* h, const cpdlp_state* s, cpdlp_stats* stats) {
+    NEED(h);
+    if (!s || !stats) return CPDLP_ERR_ARGUMENT;
+    reinterpret_cast<const StateBase*>(s)->stats(stats);
+    return CPDLP_OK;
+}
+
+int cpdlp_state_history(const cpdlp_state* s, int64_t* kkt_passes, cpdlp_kkt_errors* errs,
+                        int64_t capacity, int64_t* count) {
+    if (!s) return CPDLP_ERR_ARGUMENT;
+    const StateBase* S = reinterpret_cast<const StateBase*>(s);
+    const int64_t len = (int64_t)S->hist_passes.size();
+    const int64_t k = capacity < len ? capacity : len;
+    for (int64_t t = 0; t < k; t++) {
+        if (kkt_passes) kkt_passes[t] = S->hist_passes[(size_t)t];
+        if (errs) errs[t] = S->hist_err[(size_t)t];
+    }
+    if (count) *count = len;
+    return CPDLP_OK;
+}
+
+int cpdlp_solve(cpdlp_handle* h, const cpdlp_lp* lp, const cpdlp_params* params,
+                const double* x0, const double* y0, double* x_out, double* y_out,
+                cpdlp_stats* stats) {
+    NEED(h);
+    return guarded(h, [&] {
+        double t0 = now_seconds();
+        std::unique_ptr<ProblemBase> P(problem_create(*H(h), lp, params));
+        std::unique_ptr<StateBase> S(state_create(*H(h), P.get(), params, x0, y0));
+        S->starting_time = t0;
+        if (P->m == 0 && P->zero_cost) S->early_exit_zero_problem();  // common.jl:194-198
+        else S->solve();
+        S->solution(x_out, y_out);
+        if (stats) S->stats(stats);
+    });
+}
+
+int cpdlp_batch_solve(cpdlp_handle* h, int64_t count, const cpdlp_lp* lps,
+                      const cpdlp_params* params, double* const* x_out, double* const* y_out,
+                      cpdlp_stats* stats) {
+    NEED(h);
+    if (count < 0 || (count > 0 && (!lps || !params))) return CPDLP_ERR_ARGUMENT;
+    return guarded(h, [&] { batch_solve(*H(h), count, lps, params, x_out, y_out, stats); });
+}
+
+}  // extern "C"

@@ -1,0 +1,153 @@
+// cpdlp_common.cuh -- shared infrastructure of libcoolpdlp_cuda (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/coolpdlp_cuda.h"
+
+namespace cpdlp {
+
+// ---------------------------------------------------------------------------
+// errors: every internal failure is a cpdlp::Error carrying a CPDLP_ERR_* code;
+// the C-ABI layer turns it into a status and cpdlp_last_error().
+// ---------------------------------------------------------------------------
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+[[noreturn]] inline void fail(int code, const std::string& msg) { throw Error(code, msg); }
+
+inline void cuda_check(cudaError_t e, const char* what, const char* file, int line) {
+    if (e != cudaSuccess) {
+        char buf[512];
+        snprintf(buf, sizeof(buf), "%s failed at %s:%d: %s", what, file, line,
+                 cudaGetErrorString(e));
+        if (e == cudaErrorMemoryAllocation) fail(CPDLP_ERR_OUT_OF_MEMORY, buf);
+        fail(CPDLP_ERR_CUDA, buf);
+    }
+}
+#define CK(x) ::cpdlp::cuda_check((x), #x, __FILE__, __LINE__)
+#define CK_LAUNCH() ::cpdlp::cuda_check(cudaGetLastError(), "kernel launch", __FILE__, __LINE__)
+
+// ---------------------------------------------------------------------------
+// device buffer (owning, move-only)
+// ---------------------------------------------------------------------------
+template <class T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DBuf() = default;
+    explicit DBuf(size_t count) { alloc(count); }
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    DBuf(DBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+    DBuf& operator=(DBuf&& o) noexcept {
+        if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+        return *this;
+    }
+    ~DBuf() { release(); }
+    void alloc(size_t count) {
+        release();
+        n = count;
+        if (count) CK(cudaMalloc((void**)&p, sizeof(T) * count));
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    size_t bytes() const { return sizeof(T) * n; }
+    T* get() const { return p; }
+};
+
+// ---------------------------------------------------------------------------
+// scalar semantics shared by host and device (src/utils/linalg.jl:1-53)
+// Base.max/min on floats: NaN propagates and -0.0 < +0.0.
+// ---------------------------------------------------------------------------
+template <class T>
+__host__ __device__ __forceinline__ T jl_max(T x, T y) {
+    bool sx = signbit(x), sy = signbit(y);
+    if ((y > x) || (sy < sx)) return (x != x) ? x : y;
+    return (y != y) ? y : x;
+}
+template <class T>
+__host__ __device__ __forceinline__ T jl_min(T x, T y) {
+    bool sx = signbit(x), sy = signbit(y);
+    if ((y < x) || (sy > sx)) return (x != x) ? x : y;
+    return (y != y) ? y : x;
+}
+template <class T>
+__host__ __device__ __forceinline__ T proj_box(T x, T l, T u) { return jl_min(u, jl_max(l, x)); }
+template <class T>
+__host__ __device__ __forceinline__ T pos_part(T a) { return jl_max(a, T(0)); }
+template <class T>
+__host__ __device__ __forceinline__ T neg_part(T a) { return -jl_min(a, T(0)); }
+template <class T>
+__host__ __device__ __forceinline__ T safeprod_left(T l, T r) { return isinf(l) ? r : l * r; }
+template <class T>
+__host__ __device__ __forceinline__ T proj_multiplier(T lam, T l, T u) {
+    bool lmin = (l == -INFINITY), umax = (u == INFINITY);
+    if (lmin) return umax ? T(0) : -neg_part(lam);
+    return umax ? pos_part(lam) : lam;
+}
+template <class T>
+__host__ __device__ __forceinline__ T combine(T l, T u) {
+    T ls = isfinite(l) ? fabs(l) : T(0);
+    T us = isfinite(u) ? fabs(u) : T(0);
+    return jl_max(jl_max(T(0), ls), us);
+}
+
+// Exact IEEE products/sums without contraction into FMA, so that sequential
+// sums match the Float64 reference operation by operation.
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+
+// ---------------------------------------------------------------------------
+// handle
+// ---------------------------------------------------------------------------
+struct Handle {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string last_error;
+    int num_sms = 0;
+    // reusable small host-pinned area for reductions read back each check
+    double* pinned = nullptr;
+    size_t pinned_bytes = 0;
+    double* pinned_area(size_t bytes) {
+        if (bytes > pinned_bytes) {
+            if (pinned) cudaFreeHost(pinned);
+            pinned = nullptr;
+            pinned_bytes = 0;
+            CK(cudaMallocHost((void**)&pinned, bytes));
+            pinned_bytes = bytes;
+        }
+        return pinned;
+    }
+};
+
+inline unsigned grid_for(int64_t items, int threads, int64_t cap = 1 << 30) {
+    int64_t g = (items + threads - 1) / threads;
+    if (g < 1) g = 1;
+    if (g > cap) g = cap;
+    return (unsigned)g;
+}
+
+// wall clock (seconds)
+double now_seconds();
+
+}  // namespace cpdlp

@@ -1,0 +1,1134 @@
+// solver.cu -- single-LP PDLP / PDHG on one GB300.
+//
+// Per PDHG step two fused kernels run (pdlp.jl:96-124):
+//   primal: s = (A' y)_j (warp tiles over the rows of A')  ->
+//           x+ = proj_box(x - tau*(c - s), lv, uv), xbar = 2x+ - x,
+//           avg_x = a*x+ + b*avg_x_last                      (pdlp.jl:110-113, :126-136)
+//   dual:   s = (A xbar)_i (warp tiles over the rows of A)  ->
+//           y+ = y - sigma*s - sigma*proj_box(y/sigma - s, -uc, -lc),
+//           avg_y = a*y+ + b*avg_y_last                      (pdlp.jl:115-117)
+// Iterates ping-pong between two buffers (the reference swaps sol/sol_last,
+// pdlp.jl:101, and copies avg into avg_last, :129; here the average ping-pongs
+// too).  check_every steps are captured once as a CUDA graph per buffer parity.
+// Every check evaluates the KKT errors of sol, avg, sol_last and avg_last in
+// ONE pass over both matrices (four gathered vectors per nonzero), with FP64
+// accumulation, a deterministic block-then-tree reduction and one small
+// device->host read; restart and termination decisions run on the host in
+// FP64 exactly as restart.jl:40-57, termination.jl:89-101 state them.
+#include <algorithm>
+#include <chrono>
+#include <memory>
+#include <type_traits>
+
+#include "solver.cuh"
+
+namespace cpdlp {
+
+double now_seconds() {
+    using namespace std::chrono;
+    return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+namespace {
+
+constexpr int RED_THREADS = TILE_WARPS * 32;
+
+// ---------------------------------------------------------------------------
+// preconditioning kernels (FP64, preconditioning.jl:37-155)
+// ---------------------------------------------------------------------------
+enum NormKind { NK_INF = 0, NK_ONE = 1, NK_TWO = 2, NK_ZERO = 3, NK_P = 4 };
+
+// d[r] = 1/sqrt(norm(row r)), 1 when the norm is zero (preconditioning.jl:102-111).
+// Sequential in storage order, like the reference's column_norm (linalg.jl:98-99).
+__global__ void k_row_norm_scale(const int32_t* __restrict__ ptr, const double* __restrict__ v,
+                                 int64_t rows, int kind, double p, double* __restrict__ d) {
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    const int a = ptr[r], b = ptr[r + 1];
+    double s = 0.0;
+    if (kind == NK_INF) {
+        for (int k = a; k < b; k++) s = jl_max(s, fabs(v[k]));
+    } else if (kind == NK_ONE) {
+        for (int k = a; k < b; k++) s = __dadd_rn(s, fabs(v[k]));
+    } else if (kind == NK_TWO) {
+        for (int k = a; k < b; k++) s = __dadd_rn(s, __dmul_rn(v[k], v[k]));
+        s = sqrt(s);
+    } else if (kind == NK_ZERO) {
+        for (int k = a; k < b; k++) s += (v[k] != 0.0) ? 1.0 : 0.0;
+    } else {
+        for (int k = a; k < b; k++) s = __dadd_rn(s, pow(fabs(v[k]), p));
+        if (b > a) s = pow(s, 1.0 / p);
+    }
+    d[r] = (s == 0.0) ? 1.0 : 1.0 / sqrt(s);
+}
+
+// A_p = D1*A*D2 on A's CSC values (S1 order): (d1_i * a_ij) * d2_j
+__global__ void k_scale_S1(const int32_t* __restrict__ idx1, const int32_t* __restrict__ col1,
+                           const double* __restrict__ vin, const double* __restrict__ d1,
+                           const double* __restrict__ d2, double* __restrict__ vout, int64_t nnz) {
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nnz) vout[k] = __dmul_rn(__dmul_rn(d1[idx1[k]], vin[k]), d2[col1[k]]);
+}
+// At_p = D2*At*D1 on At's CSC values (S2 order): (d2_j * a_ij) * d1_i
+__global__ void k_scale_S2(const int32_t* __restrict__ idx2, const int32_t* __restrict__ row2,
+                           const double* __restrict__ vin, const double* __restrict__ d1,
+                           const double* __restrict__ d2, double* __restrict__ vout, int64_t nnz) {
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nnz) vout[k] = __dmul_rn(__dmul_rn(d2[idx2[k]], vin[k]), d1[row2[k]]);
+}
+// r[i] = d[i] * r[i]  (products of diagonal preconditioners commute exactly)
+__global__ void k_mul_into(double* __restrict__ r, const double* __restrict__ d, int64_t len) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < len) r[i] = __dmul_rn(d[i], r[i]);
+}
+__global__ void k_fill(double* __restrict__ r, double v, int64_t len) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < len) r[i] = v;
+}
+__global__ void k_invert_perm(const int32_t* __restrict__ p21, int32_t* __restrict__ p12, int64_t nnz) {
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nnz) p12[p21[k]] = (int32_t)k;
+}
+// precondition(milp, prec) on the vectors (preconditioning.jl:61-91)
+template <class T>
+__global__ void k_scale_vec_n(const double* __restrict__ c, const double* __restrict__ lv,
+                              const double* __restrict__ uv, const double* __restrict__ D2,
+                              T* __restrict__ co, T* __restrict__ lvo, T* __restrict__ uvo,
+                              double* __restrict__ invD2, int64_t n) {
+    int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const double d = D2[j];
+    co[j] = (T)__dmul_rn(d, c[j]);
+    lvo[j] = (T)__ddiv_rn(lv[j], d);
+    uvo[j] = (T)__ddiv_rn(uv[j], d);
+    invD2[j] = __drcp_rn(d);
+}
+template <class T>
+__global__ void k_scale_vec_m(const double* __restrict__ lc, const double* __restrict__ uc,
+                              const double* __restrict__ D1, T* __restrict__ lco, T* __restrict__ uco,
+                              double* __restrict__ invD1, int64_t m) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    const double d = D1[i];
+    lco[i] = (T)__dmul_rn(d, lc[i]);
+    uco[i] = (T)__dmul_rn(d, uc[i]);
+    invD1[i] = __drcp_rn(d);
+}
+// constant parts of the KKT errors and of primal_weight_init:
+// q0 = sum (invD1*combine(lc,uc))^2, q1 = sum combine(lc,uc)^2 (m side)
+// q2 = sum (invD2*c)^2, q3 = sum c^2 (n side)
+template <class T>
+__global__ void k_scales(const T* __restrict__ lc, const T* __restrict__ uc,
+                         const double* __restrict__ invD1, int64_t m, const T* __restrict__ c,
+                         const double* __restrict__ invD2, int64_t n, double* __restrict__ part) {
+    double acc[4] = {0, 0, 0, 0};
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += stride) {
+        double cb = combine((double)lc[i], (double)uc[i]);
+        double s = invD1[i] * cb;
+        acc[0] += s * s;
+        acc[1] += cb * cb;
+    }
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
+        double cj = (double)c[j];
+        double s = invD2[j] * cj;
+        acc[2] += s * s;
+        acc[3] += cj * cj;
+    }
+    block_reduce_store<4>(acc, part);
+}
+
+// ---------------------------------------------------------------------------
+// epilogues of the tile engine
+// ---------------------------------------------------------------------------
+struct NoAcc {};
+
+template <class T>
+struct StoreEpi {  // out = s (mul! with alpha = true, beta = false)
+    T* out;
+    using Acc = NoAcc;
+    __device__ void init(Acc&) {}
+    __device__ void row(int, int r, T s, Acc&) { out[r] = s; }
+    __device__ void row_long(int, int r, T s, int, Acc&) { out[r] = s; }
+    __device__ void finish(Acc&) {}
+};
+
+template <class T>
+struct PrimalEpi {
+    const T* __restrict__ x;
+    const T* __restrict__ c;
+    const T* __restrict__ lv;
+    const T* __restrict__ uv;
+    T* __restrict__ xn;
+    T* __restrict__ xbar;
+    const T* __restrict__ xa_old;
+    T* __restrict__ xa_new;
+    const StepCoef<T>* __restrict__ coef;
+    int avg;
+    using Acc = NoAcc;
+    __device__ void init(Acc&) {}
+    __device__ __forceinline__ void row(int, int j, T s, Acc&) {
+        const T tau = coef->tau;
+        const T xj = x[j];
+        const T xp = proj_box(sub_rn(xj, mul_rn(tau, sub_rn(c[j], s))), lv[j], uv[j]);
+        xn[j] = xp;
+        xbar[j] = sub_rn(mul_rn(T(2), xp), xj);
+        if (avg) xa_new[j] = add_rn(mul_rn(xp, coef->a), mul_rn(xa_old[j], coef->b));
+    }
+    __device__ void row_long(int p, int j, T s, int, Acc& a) { row(p, j, s, a); }
+    __device__ void finish(Acc&) {}
+};
+
+template <class T>
+struct DualEpi {
+    const T* __restrict__ y;
+    const T* __restrict__ lc;
+    const T* __restrict__ uc;
+    T* __restrict__ yn;
+    const T* __restrict__ ya_old;
+    T* __restrict__ ya_new;
+    const StepCoef<T>* __restrict__ coef;
+    int avg;
+    using Acc = NoAcc;
+    __device__ void init(Acc&) {}
+    __device__ __forceinline__ void row(int, int i, T s, Acc&) {
+        const T sigma = coef->sigma;
+        const T yi = y[i];
+        const T t2 = sub_rn(yi, mul_rn(sigma, s));
+        const T t4 = sub_rn(mul_rn(coef->inv_sigma, yi), s);
+        const T pr = proj_box(t4, -uc[i], -lc[i]);
+        const T yp = sub_rn(t2, mul_rn(sigma, pr));
+        yn[i] = yp;
+        if (avg) ya_new[i] = add_rn(mul_rn(yp, coef->a), mul_rn(ya_old[i], coef->b));
+    }
+    __device__ void row_long(int p, int i, T s, int, Acc& a) { row(p, i, s, a); }
+    __device__ void finish(Acc&) {}
+};
+
+// KKT row side (errors.jl:73-80, 87-89): s = (A x_p)_i
+template <class T, int NV>
+struct KktRowEpi {
+    const T* __restrict__ lc;
+    const T* __restrict__ uc;
+    const double* __restrict__ invD1;
+    const T* y[NV];
+    double* block_out;
+    double* long_out;
+    struct Acc { double v[2 * NV]; };
+    __device__ void init(Acc& a) {
+#pragma unroll
+        for (int q = 0; q < 2 * NV; q++) a.v[q] = 0.0;
+    }
+    __device__ __forceinline__ void terms(int p, int i, T s, double& pr2, double& pc) const {
+        const double sd = (double)s, l = (double)lc[i], u = (double)uc[i];
+        const double d = __dmul_rn(invD1[i], __dsub_rn(sd, proj_box(sd, l, u)));
+        pr2 = __dmul_rn(d, d);
+        const double yy = (double)y[p][i];
+        pc = __dsub_rn(safeprod_left(u, pos_part(-yy)), safeprod_left(l, neg_part(-yy)));
+    }
+    __device__ __forceinline__ void row(int p, int i, T s, Acc& a) {
+        double pr2, pc;
+        terms(p, i, s, pr2, pc);
+        a.v[2 * p] += pr2;
+        a.v[2 * p + 1] += pc;
+    }
+    __device__ void row_long(int p, int i, T s, int lid, Acc&) {
+        double pr2, pc;
+        terms(p, i, s, pr2, pc);
+        long_out[(size_t)lid * 2 * NV + 2 * p] = pr2;
+        long_out[(size_t)lid * 2 * NV + 2 * p + 1] = pc;
+    }
+    __device__ void finish(Acc& a) { block_reduce_store<2 * NV>(a.v, block_out); }
+};
+
+// KKT column side (errors.jl:74-75, 82-95): s = (A' y_p)_j
+template <class T, int NV>
+struct KktColEpi {
+    const T* __restrict__ c;
+    const T* __restrict__ lv;
+    const T* __restrict__ uv;
+    const double* __restrict__ invD2;
+    const T* x[NV];
+    double* block_out;
+    double* long_out;
+    struct Acc { double v[3 * NV]; };
+    __device__ void init(Acc& a) {
+#pragma unroll
+        for (int q = 0; q < 3 * NV; q++) a.v[q] = 0.0;
+    }
+    __device__ __forceinline__ void terms(int p, int j, T s, double& du2, double& pv,
+                                          double& cx) const {
+        const double cj = (double)c[j], l = (double)lv[j], u = (double)uv[j];
+        const double g = __dsub_rn(cj, (double)s);
+        const double r = proj_multiplier(g, l, u);
+        const double d = __dmul_rn(invD2[j], __dsub_rn(g, r));
+        du2 = __dmul_rn(d, d);
+        pv = __dsub_rn(safeprod_left(u, pos_part(-r)), safeprod_left(l, neg_part(-r)));
+        cx = __dmul_rn(cj, (double)x[p][j]);
+    }
+    __device__ __forceinline__ void row(int p, int j, T s, Acc& a) {
+        double du2, pv, cx;
+        terms(p, j, s, du2, pv, cx);
+        a.v[3 * p] += du2;
+        a.v[3 * p + 1] += pv;
+        a.v[3 * p + 2] += cx;
+    }
+    __device__ void row_long(int p, int j, T s, int lid, Acc&) {
+        double du2, pv, cx;
+        terms(p, j, s, du2, pv, cx);
+        double* o = long_out + (size_t)lid * 3 * NV + 3 * p;
+        o[0] = du2;
+        o[1] = pv;
+        o[2] = cx;
+    }
+    __device__ void finish(Acc& a) { block_reduce_store<3 * NV>(a.v, block_out); }
+};
+
+// power method, second product: Ax_j = (A' s)_j; accumulates x.Ax and Ax.Ax
+template <class T>
+struct PowerEpi {
+    const T* __restrict__ x;
+    T* __restrict__ out;
+    double* block_out;
+    double* long_out;
+    struct Acc { double v[2]; };
+    __device__ void init(Acc& a) { a.v[0] = a.v[1] = 0.0; }
+    __device__ __forceinline__ void row(int, int j, T s, Acc& a) {
+        out[j] = s;
+        a.v[0] += (double)x[j] * (double)s;
+        a.v[1] += (double)s * (double)s;
+    }
+    __device__ void row_long(int, int j, T s, int lid, Acc&) {
+        out[j] = s;
+        long_out[(size_t)lid * 2] = (double)x[j] * (double)s;
+        long_out[(size_t)lid * 2 + 1] = (double)s * (double)s;
+    }
+    __device__ void finish(Acc& a) { block_reduce_store<2>(a.v, block_out); }
+};
+
+// powm! residual and normalisation: r = Ax - theta*x, x = Ax * (1/||Ax||)
+template <class T>
+__global__ void __launch_bounds__(RED_THREADS)
+    k_power_residual(T* __restrict__ x, const T* __restrict__ Ax, T theta, T inv, int64_t n,
+                     double* __restrict__ part) {
+    double acc[1] = {0.0};
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
+        const T r = add_rn(mul_rn(-theta, x[j]), Ax[j]);
+        acc[0] += (double)r * (double)r;
+        x[j] = mul_rn(Ax[j], inv);
+    }
+    block_reduce_store<1>(acc, part);
+}
+
+// ||a - b||^2 over x (n) and y (m): primal_weight_update! (step_size.jl:58-75)
+template <class T>
+__global__ void __launch_bounds__(RED_THREADS)
+    k_diff_norms(const T* __restrict__ ax, const T* __restrict__ bx, int64_t n,
+                 const T* __restrict__ ay, const T* __restrict__ by, int64_t m,
+                 double* __restrict__ part) {
+    double acc[2] = {0.0, 0.0};
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
+        double d = (double)ax[j] - (double)bx[j];
+        acc[0] += d * d;
+    }
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += stride) {
+        double d = (double)ay[i] - (double)by[i];
+        acc[1] += d * d;
+    }
+    block_reduce_store<2>(acc, part);
+}
+
+template <class T>
+__global__ void k_unscale(const T* __restrict__ v, const double* __restrict__ D, double* __restrict__ out,
+                          int64_t len) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < len) out[i] = __dmul_rn(D[i], (double)v[i]);
+}
+template <class T>
+__global__ void k_prescale(const double* __restrict__ v, const double* __restrict__ D, T* __restrict__ out,
+                           int64_t len) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < len) out[i] = (T)__ddiv_rn(v[i], D[i]);
+}
+template <class T>
+__global__ void k_widen(const T* __restrict__ v, double* __restrict__ out, int64_t len) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < len) out[i] = (double)v[i];
+}
+template <class T>
+__global__ void k_proj_zero(T* __restrict__ x, const T* __restrict__ lv, const T* __restrict__ uv, int64_t n) {
+    int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) x[j] = proj_box(T(0), lv[j], uv[j]);
+}
+
+inline unsigned red_grid(Handle& h, int64_t items) {
+    int64_t g = (items + RED_THREADS - 1) / RED_THREADS;
+    int64_t cap = (int64_t)(h.num_sms > 0 ? h.num_sms : 152) * 4;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (unsigned)g;
+}
+
+template <class T>
+CsrView<T, T> view_A(ProblemT<T>& P) {
+    return CsrView<T, T>{P.a_ptr.p, P.a_idx.p, P.a_val.p, P.planA.tasks.p, P.planA.ntasks,
+                         P.planA.counters.p, P.partA.p};
+}
+template <class T>
+CsrView<T, T> view_At(ProblemT<T>& P) {
+    return CsrView<T, T>{P.at_ptr.p, P.at_idx.p, P.at_val.p, P.planAt.tasks.p, P.planAt.ntasks,
+                         P.planAt.counters.p, P.partAt.p};
+}
+
+// device reduction of (rows x q) partials into host doubles
+void fetch_reduced(Handle& h, const double* part, int64_t rows, int q, double* dev_out,
+                   double* host_out) {
+    reduce_partials(part, rows, q, dev_out, h.stream);
+    double* pin = h.pinned_area(sizeof(double) * 64);
+    CK(cudaMemcpyAsync(pin, dev_out, sizeof(double) * q, cudaMemcpyDeviceToHost, h.stream));
+    CK(cudaStreamSynchronize(h.stream));
+    memcpy(host_out, pin, sizeof(double) * q);
+}
+
+// ---------------------------------------------------------------------------
+// problem creation: preprocess (common.jl:154-169) on the device
+// ---------------------------------------------------------------------------
+template <class T>
+ProblemBase* make_problem(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm) {
+    double t0 = now_seconds();
+    cudaStream_t s = h.stream;
+    auto* P = new ProblemT<T>();
+    std::unique_ptr<ProblemT<T>> guard(P);
+    P->h = &h;
+    P->vt = std::is_same<T, float>::value ? CPDLP_VAL_F32 : CPDLP_VAL_F64;
+    P->prm = *prm;
+    const int64_t m = lp->m, n = lp->n;
+    for (const double* v : {lp->c, lp->lv, lp->uv})
+        if (n > 0 && !v) fail(CPDLP_ERR_ARGUMENT, "null variable vector (c, lv or uv)");
+    for (const double* v : {lp->lc, lp->uc})
+        if (m > 0 && !v) fail(CPDLP_ERR_ARGUMENT, "null constraint vector (lc or uc)");
+    CscPair S;
+    build_csc_pair(h, m, n, lp->nnz, lp->colptr, lp->rowval, lp->nzval, S);
+    const int64_t nnz = S.nnz;
+    P->m = m; P->n = n; P->nnz = nnz;
+    const size_t zn = (size_t)(nnz > 0 ? nnz : 1), mz = (size_t)(m > 0 ? m : 1),
+                 nzv = (size_t)(n > 0 ? n : 1);
+    // vA: A's values in S1 order, vAt: At's values in S2 order
+    DBuf<double> vA(std::move(S.val1)), vAt(zn), wA(zn), wAt(zn), tA(zn), tAt(zn);
+    gather_values<double, double>(vA.p, S.p21.p, vAt.p, nnz, s);
+    DBuf<double> d1(mz), d2(nzv), r1(mz), r2(nzv), D1(mz), D2(nzv);
+    const unsigned gm = grid_for(m, 256), gn = grid_for(n, 256), gz = grid_for(nnz, 256);
+    k_fill<<<gm, 256, 0, s>>>(r1.p, 1.0, m);
+    k_fill<<<gn, 256, 0, s>>>(r2.p, 1.0, n);
+    CK_LAUNCH();
+    // Ruiz (preconditioning.jl:117-125)
+    if (prm->ruiz_iter > 0 && nnz > 0) {
+        CK(cudaMemcpyAsync(wA.p, vA.p, sizeof(double) * nnz, cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemcpyAsync(wAt.p, vAt.p, sizeof(double) * nnz, cudaMemcpyDeviceToDevice, s));
+    }
+    for (int it = 0; it < prm->ruiz_iter; it++) {
+        k_row_norm_scale<<<gn, 256, 0, s>>>(S.ptr1.p, wA.p, n, NK_INF, 0.0, d2.p);
+        k_row_norm_scale<<<gm, 256, 0, s>>>(S.ptr2.p, wAt.p, m, NK_INF, 0.0, d1.p);
+        if (nnz > 0) {
+            k_scale_S1<<<gz, 256, 0, s>>>(S.idx1.p, S.col1.p, wA.p, d1.p, d2.p, tA.p, nnz);
+            k_scale_S2<<<gz, 256, 0, s>>>(S.idx2.p, S.row2.p, wAt.p, d1.p, d2.p, tAt.p, nnz);
+            std::swap(wA, tA);
+            std::swap(wAt, tAt);
+        }
+        k_mul_into<<<gm, 256, 0, s>>>(r1.p, d1.p, m);
+        k_mul_into<<<gn, 256, 0, s>>>(r2.p, d2.p, n);
+        CK_LAUNCH();
+    }
+    // Pock-Chambolle on the Ruiz-scaled ORIGINAL matrix (preconditioning.jl:146-155)
+    if (nnz > 0) {
+        k_scale_S1<<<gz, 256, 0, s>>>(S.idx1.p, S.col1.p, vA.p, r1.p, r2.p, tA.p, nnz);
+        k_scale_S2<<<gz, 256, 0, s>>>(S.idx2.p, S.row2.p, vAt.p, r1.p, r2.p, tAt.p, nnz);
+        CK_LAUNCH();
+    }
+    auto kind_of = [](double p, int& kind) {
+        if (std::isinf(p) && p > 0) kind = NK_INF;
+        else if (p == 1.0) kind = NK_ONE;
+        else if (p == 2.0) kind = NK_TWO;
+        else if (p == 0.0) kind = NK_ZERO;
+        else kind = NK_P;
+    };
+    const double alpha = prm->chambolle_pock_alpha;
+    int kc, kr;
+    kind_of(alpha, kc);
+    kind_of(2.0 - alpha, kr);
+    k_row_norm_scale<<<gn, 256, 0, s>>>(S.ptr1.p, tA.p, n, kc, alpha, d2.p);
+    k_row_norm_scale<<<gm, 256, 0, s>>>(S.ptr2.p, tAt.p, m, kr, 2.0 - alpha, d1.p);
+    CK_LAUNCH();
+    // prec = prec_r * prec_cp: D1 = r1 .* d1_cp, D2 = d2_cp .* r2
+    CK(cudaMemcpyAsync(D1.p, d1.p, sizeof(double) * m, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(D2.p, d2.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    k_mul_into<<<gm, 256, 0, s>>>(D1.p, r1.p, m);
+    k_mul_into<<<gn, 256, 0, s>>>(D2.p, r2.p, n);
+    CK_LAUNCH();
+    // precondition(milp, prec): final values from the original ones
+    if (nnz > 0) {
+        k_scale_S1<<<gz, 256, 0, s>>>(S.idx1.p, S.col1.p, vA.p, D1.p, D2.p, tA.p, nnz);
+        k_scale_S2<<<gz, 256, 0, s>>>(S.idx2.p, S.row2.p, vAt.p, D1.p, D2.p, tAt.p, nnz);
+        CK_LAUNCH();
+    }
+    // solver matrices: A rows = S2 structure with A's values; A' rows = S1 with A''s values
+    DBuf<int32_t> p12(zn);
+    if (nnz > 0) {
+        k_invert_perm<<<gz, 256, 0, s>>>(S.p21.p, p12.p, nnz);
+        CK_LAUNCH();
+    }
+    P->a_val.alloc(zn);
+    P->at_val.alloc(zn);
+    gather_values<T, double>(tA.p, S.p21.p, P->a_val.p, nnz, s);
+    gather_values<T, double>(tAt.p, p12.p, P->at_val.p, nnz, s);
+    P->a_ptr = std::move(S.ptr2);
+    P->a_idx = std::move(S.idx2);
+    P->at_ptr = std::move(S.ptr1);
+    P->at_idx = std::move(S.idx1);
+    // vectors
+    DBuf<double> hc(nzv), hlv(nzv), huv(nzv), hlc(mz), huc(mz);
+    if (n > 0) {
+        CK(cudaMemcpyAsync(hc.p, lp->c, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(hlv.p, lp->lv, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(huv.p, lp->uv, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    }
+    if (m > 0) {
+        CK(cudaMemcpyAsync(hlc.p, lp->lc, sizeof(double) * m, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(huc.p, lp->uc, sizeof(double) * m, cudaMemcpyHostToDevice, s));
+    }
+    P->c.alloc(nzv); P->lv.alloc(nzv); P->uv.alloc(nzv); P->lc.alloc(mz); P->uc.alloc(mz);
+    P->invD1.alloc(mz); P->invD2.alloc(nzv);
+    k_scale_vec_n<T><<<gn, 256, 0, s>>>(hc.p, hlv.p, huv.p, D2.p, P->c.p, P->lv.p, P->uv.p,
+                                        P->invD2.p, n);
+    k_scale_vec_m<T><<<gm, 256, 0, s>>>(hlc.p, huc.p, D1.p, P->lc.p, P->uc.p, P->invD1.p, m);
+    CK_LAUNCH();
+    P->D1 = std::move(D1);
+    P->D2 = std::move(D2);
+    // tile plans from the row pointers
+    std::vector<int32_t> hp2((size_t)m + 1), hp1((size_t)n + 1);
+    CK(cudaMemcpyAsync(hp2.data(), P->a_ptr.p, sizeof(int32_t) * (m + 1), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(hp1.data(), P->at_ptr.p, sizeof(int32_t) * (n + 1), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    build_tile_plan(hp2, (int32_t)m, choose_items(nnz, m, prm->tile_nnz), P->planA, s);
+    build_tile_plan(hp1, (int32_t)n, choose_items(nnz, n, prm->tile_nnz), P->planAt, s);
+    P->partA.alloc((size_t)(P->planA.npieces > 0 ? P->planA.npieces : 1) * 4);
+    P->partAt.alloc((size_t)(P->planAt.npieces > 0 ? P->planAt.npieces : 1) * 4);
+    P->rows_A_partials = (int64_t)tiles_grid(P->planA) + P->planA.nlong;
+    P->rows_At_partials = (int64_t)tiles_grid(P->planAt) + P->planAt.nlong;
+    int64_t rows_max = std::max<int64_t>(std::max(P->rows_A_partials, P->rows_At_partials),
+                                         (int64_t)h.num_sms * 4 + 8);
+    P->red_rows.alloc((size_t)rows_max * 12);
+    P->red_cols.alloc((size_t)rows_max * 12);
+    P->red_out.alloc(64);
+    // constant scales (errors.jl:79-85)
+    {
+        unsigned g = red_grid(h, std::max(m, n));
+        k_scales<T><<<g, RED_THREADS, 0, s>>>(P->lc.p, P->uc.p, P->invD1.p, m, P->c.p, P->invD2.p,
+                                              n, P->red_rows.p);
+        CK_LAUNCH();
+        double q[4];
+        fetch_reduced(h, P->red_rows.p, g, 4, P->red_out.p, q);
+        P->primal_scale = 1.0 + sqrt(q[0]);
+        P->dual_scale = 1.0 + sqrt(q[2]);
+    }
+    bool zc = true;
+    for (int64_t j = 0; j < n; j++)
+        if (lp->c[j] != 0.0) { zc = false; break; }
+    P->zero_cost = zc;
+    CK(cudaStreamSynchronize(s));
+    P->setup_seconds = now_seconds() - t0;
+    guard.release();
+    return P;
+}
+
+// ---------------------------------------------------------------------------
+// spectral norm: IterativeSolvers.powm! on Symmetrized(A, A') (linalg.jl:60-96)
+// ---------------------------------------------------------------------------
+uint64_t splitmix64_at(uint64_t seed, uint64_t counter) {
+    uint64_t z = seed + (counter + 1) * 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+// Gaussian start vector: SplitMix64 + Box-Muller, element i from counters 2i, 2i+1
+void gaussian_vector(uint64_t seed, int64_t len, std::vector<double>& out) {
+    out.resize((size_t)len);
+    for (int64_t i = 0; i < len; i++) {
+        double u1 = (double)((splitmix64_at(seed, 2 * (uint64_t)i) >> 11) + 1) * (1.0 / 9007199254740992.0);
+        double u2 = (double)((splitmix64_at(seed, 2 * (uint64_t)i + 1) >> 11) + 1) * (1.0 / 9007199254740992.0);
+        out[(size_t)i] = std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
+    }
+}
+
+double powm_default_tol(int64_t n, bool f32) {
+    uint64_t un = (uint64_t)n;
+    int64_t n3 = (int64_t)(un * un * un);  // Julia Int64 arithmetic wraps modulo 2^64
+    double eps = f32 ? 1.1920928955078125e-07 : 2.220446049250313e-16;
+    return eps * (double)n3;
+}
+
+template <class T>
+double spectral_norm_T(Handle& h, ProblemT<T>& P, const cpdlp_params* prm, int64_t* iters_out) {
+    cudaStream_t s = h.stream;
+    const int64_t m = P.m, n = P.n;
+    const bool f32 = std::is_same<T, float>::value;
+    double tol = prm->power_tol_override > 0 ? prm->power_tol_override : powm_default_tol(n, f32);
+    int64_t maxiter = prm->power_maxiter_override > 0 ? prm->power_maxiter_override : n;
+    std::vector<double> x0;
+    gaussian_vector(prm->power_seed, n, x0);
+    std::vector<T> x0t(x0.begin(), x0.end());
+    DBuf<T> x((size_t)(n > 0 ? n : 1)), Ax((size_t)(n > 0 ? n : 1)), sv((size_t)(m > 0 ? m : 1));
+    if (n > 0) CK(cudaMemcpyAsync(x.p, x0t.data(), sizeof(T) * n, cudaMemcpyHostToDevice, s));
+    CsrView<T, T> A = view_A(P), At = view_At(P);
+    double theta_d = 0.0, residual = INFINITY;
+    int64_t it = 0;
+    const unsigned gr = red_grid(h, n);
+    while (!(it > maxiter || residual <= tol)) {
+        launch_tiles<1>(P.planA, A, VecSet<T, 1>{{x.p}}, StoreEpi<T>{sv.p}, s);
+        PowerEpi<T> pe{x.p, Ax.p, P.red_cols.p, P.red_cols.p + (size_t)tiles_grid(P.planAt) * 2};
+        launch_tiles<1>(P.planAt, At, VecSet<T, 1>{{sv.p}}, pe, s);
+        double q[2];
+        fetch_reduced(h, P.red_cols.p, P.rows_At_partials, 2, P.red_out.p, q);
+        const T theta = (T)q[0];
+        const T nrm = (T)std::sqrt(q[1]);
+        const T inv = T(1) / nrm;
+        k_power_residual<T><<<gr, RED_THREADS, 0, s>>>(x.p, Ax.p, theta, inv, n, P.red_rows.p);
+        CK_LAUNCH();
+        double r2;
+        fetch_reduced(h, P.red_rows.p, gr, 1, P.red_out.p, &r2);
+        residual = std::sqrt(r2);
+        theta_d = (double)theta;
+        it++;
+    }
+    if (iters_out) *iters_out = it;
+    return std::sqrt(theta_d);
+}
+
+// ---------------------------------------------------------------------------
+// solver state
+// ---------------------------------------------------------------------------
+template <class T>
+struct StateT : StateBase {
+    ProblemT<T>* PT = nullptr;
+    Handle* h = nullptr;
+    DBuf<T> x[2], y[2], xa[2], ya[2], xr, yr, xbar;
+    int cur = 0;  // sol = (x[cur], y[cur]); sol_last = (x[cur^1], y[cur^1]); same for averages
+    DBuf<StepCoef<T>> coef, coef1;
+    std::vector<StepCoef<T>> coef_host;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    int graph_len = 0;
+
+    ~StateT() override {
+        for (auto& g : graph)
+            if (g) cudaGraphExecDestroy(g);
+    }
+
+    bool pdlp() const { return prm.algorithm == CPDLP_ALGO_PDLP; }
+
+    StepCoef<T> coef_for(double eta_sum_k) const {
+        StepCoef<T> k;
+        const double tau = eta / omega, sigma = eta * omega;
+        k.tau = (T)tau;
+        k.sigma = (T)sigma;
+        k.inv_sigma = (T)(1.0 / sigma);
+        k.a = (T)(eta / (eta + eta_sum_k));
+        k.b = (T)(eta_sum_k / (eta + eta_sum_k));
+        return k;
+    }
+
+    // One step!: kernels only.  `c` points at this step's coefficients.
+    void enqueue_step(int parity_in, const StepCoef<T>* c, cudaStream_t s) {
+        ProblemT<T>& P = *PT;
+        const int o = parity_in, nw = parity_in ^ 1;  // read old, write new
+        PrimalEpi<T> pe{x[o].p, P.c.p, P.lv.p, P.uv.p, x[nw].p, xbar.p, xa[o].p, xa[nw].p, c,
+                        pdlp() ? 1 : 0};
+        launch_tiles<1>(P.planAt, view_At(P), VecSet<T, 1>{{y[o].p}}, pe, s);
+        DualEpi<T> de{y[o].p, P.lc.p, P.uc.p, y[nw].p, ya[o].p, ya[nw].p, c, pdlp() ? 1 : 0};
+        launch_tiles<1>(P.planA, view_A(P), VecSet<T, 1>{{xbar.p}}, de, s);
+    }
+
+    void advance_counters(int64_t k) {
+        kkt_passes += k;
+        if (pdlp()) {
+            inner += k;
+            total += k;
+        }
+    }
+
+    void build_graph(int parity, int len) {
+        cudaStream_t s = h->stream;
+        cudaGraph_t g;
+        CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        int par = parity;
+        for (int k = 0; k < len; k++) {
+            enqueue_step(par, coef.p + k, s);
+            par ^= 1;
+        }
+        CK(cudaStreamEndCapture(s, &g));
+        if (graph[parity]) cudaGraphExecDestroy(graph[parity]);
+        CK(cudaGraphInstantiate(&graph[parity], g, 0));
+        cudaGraphDestroy(g);
+    }
+
+    // `len` steps as one graph launch (len == check_every).
+    void run_block(int len) {
+        cudaStream_t s = h->stream;
+        if (len != graph_len) {
+            for (auto& g : graph)
+                if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+            graph_len = len;
+            coef.alloc((size_t)len);
+            coef_host.resize((size_t)len);
+        }
+        if (!graph[cur]) build_graph(cur, len);
+        double es = eta_sum;
+        for (int k = 0; k < len; k++) {
+            coef_host[(size_t)k] = coef_for(es);
+            if (pdlp()) es += eta;
+        }
+        // pageable source: the bytes are staged before the call returns
+        CK(cudaMemcpyAsync(coef.p, coef_host.data(), sizeof(StepCoef<T>) * len,
+                           cudaMemcpyHostToDevice, s));
+        CK(cudaGraphLaunch(graph[cur], s));
+        launches += 2 * (int64_t)len;
+        eta_sum = es;
+        if (len & 1) cur ^= 1;
+        advance_counters(len);
+    }
+
+    void run_single() {
+        cudaStream_t s = h->stream;
+        if (!coef1.p) coef1.alloc(1);
+        StepCoef<T> k = coef_for(eta_sum);
+        CK(cudaMemcpyAsync(coef1.p, &k, sizeof(k), cudaMemcpyHostToDevice, s));
+        CK(cudaStreamSynchronize(s));
+        enqueue_step(cur, coef1.p, s);
+        launches += 2;
+        cur ^= 1;
+        if (pdlp()) eta_sum += eta;
+        advance_counters(1);
+    }
+
+    void step(int64_t count) override {
+        const int ce = prm.check_every > 0 ? prm.check_every : 100;
+        while (count >= ce) {
+            run_block(ce);
+            count -= ce;
+        }
+        while (count-- > 0) run_single();
+        CK(cudaStreamSynchronize(h->stream));
+    }
+
+    // KKT errors of NV (x, y) pairs in one pass (errors.jl:65-109)
+    template <int NV>
+    void kkt_multi(const T* const (&xs)[NV], const T* const (&ys)[NV], cpdlp_kkt_errors* out) {
+        ProblemT<T>& P = *PT;
+        cudaStream_t s = h->stream;
+        const unsigned gA = tiles_grid(P.planA), gAt = tiles_grid(P.planAt);
+        KktRowEpi<T, NV> re;
+        re.lc = P.lc.p; re.uc = P.uc.p; re.invD1 = P.invD1.p;
+        for (int p = 0; p < NV; p++) re.y[p] = ys[p];
+        re.block_out = P.red_rows.p;
+        re.long_out = P.red_rows.p + (size_t)gA * 2 * NV;
+        VecSet<T, NV> vx;
+        for (int p = 0; p < NV; p++) vx.v[p] = xs[p];
+        launch_tiles<NV>(P.planA, view_A(P), vx, re, s);
+        KktColEpi<T, NV> ce;
+        ce.c = P.c.p; ce.lv = P.lv.p; ce.uv = P.uv.p; ce.invD2 = P.invD2.p;
+        for (int p = 0; p < NV; p++) ce.x[p] = xs[p];
+        ce.block_out = P.red_cols.p;
+        ce.long_out = P.red_cols.p + (size_t)gAt * 3 * NV;
+        VecSet<T, NV> vy;
+        for (int p = 0; p < NV; p++) vy.v[p] = ys[p];
+        launch_tiles<NV>(P.planAt, view_At(P), vy, ce, s);
+        reduce_partials(P.red_rows.p, P.rows_A_partials, 2 * NV, P.red_out.p, s);
+        reduce_partials(P.red_cols.p, P.rows_At_partials, 3 * NV, P.red_out.p + 2 * NV, s);
+        launches += 4;
+        double* pin = h->pinned_area(sizeof(double) * 64);
+        CK(cudaMemcpyAsync(pin, P.red_out.p, sizeof(double) * 5 * NV, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        for (int p = 0; p < NV; p++) {
+            const double pr2 = pin[2 * p], pc = pin[2 * p + 1];
+            const double du2 = pin[2 * NV + 3 * p], pv = pin[2 * NV + 3 * p + 1],
+                         cx = pin[2 * NV + 3 * p + 2];
+            cpdlp_kkt_errors& e = out[p];
+            e.primal = std::sqrt(pr2);
+            e.primal_scale = P.primal_scale;
+            e.dual = std::sqrt(du2);
+            e.dual_scale = P.dual_scale;
+            e.gap = std::fabs((cx + pc) + pv);
+            e.gap_scale = (1.0 + std::fabs(pc + pv)) + std::fabs(cx);
+        }
+    }
+
+    void vec_of(int which, const T*& vx, const T*& vy) {
+        switch (which) {
+            case CPDLP_VEC_SOL_LAST: vx = x[cur ^ 1].p; vy = y[cur ^ 1].p; break;
+            case CPDLP_VEC_SOL_AVG: vx = xa[cur].p; vy = ya[cur].p; break;
+            case CPDLP_VEC_SOL_AVG_LAST: vx = xa[cur ^ 1].p; vy = ya[cur ^ 1].p; break;
+            case CPDLP_VEC_SOL_RESTART: vx = xr.p; vy = yr.p; break;
+            default: vx = x[cur].p; vy = y[cur].p; break;
+        }
+    }
+
+    void kkt(int which, cpdlp_kkt_errors* e) override {
+        const T *vx, *vy;
+        vec_of(which, vx, vy);
+        const T* const xs[1] = {vx};
+        const T* const ys[1] = {vy};
+        kkt_multi<1>(xs, ys, e);
+    }
+
+    void push_history() {
+        if (!prm.record_error_history) return;
+        hist_passes.push_back(kkt_passes);
+        hist_err.push_back(err);
+    }
+
+    static double relative(const cpdlp_kkt_errors& e) {
+        return jl_max(jl_max(e.primal / e.primal_scale, e.dual / e.dual_scale), e.gap / e.gap_scale);
+    }
+    static double absolute(const cpdlp_kkt_errors& e, double w) {
+        return std::sqrt((w * w) * (e.primal * e.primal) + (1.0 / (w * w)) * (e.dual * e.dual) +
+                         e.gap * e.gap);
+    }
+
+    int32_t termination_status_now() const {
+        if (relative(err) <= prm.termination_reltol) return CPDLP_OPTIMAL;
+        if (time_elapsed >= prm.time_limit) return CPDLP_TIME_LIMIT;
+        if (kkt_passes >= prm.max_kkt_passes) return CPDLP_ITERATION_LIMIT;
+        return CPDLP_STILL_RUNNING;
+    }
+
+    // termination_check! (common.jl:218-231), given err of sol
+    bool termination_check_with(const cpdlp_kkt_errors& e_sol) {
+        time_elapsed = now_seconds() - starting_time;
+        err = e_sol;
+        push_history();
+        status = termination_status_now();
+        return status != CPDLP_STILL_RUNNING;
+    }
+
+    // restart_check! (pdlp.jl:138-170) with the four errors already evaluated
+    bool restart_check(const cpdlp_kkt_errors (&e4)[4]) {
+        const double w = omega;
+        const cpdlp_kkt_errors &e = e4[0], &ea = e4[1], &el = e4[2], &eal = e4[3];
+        if (absolute(e, w) < absolute(ea, w)) {
+            restart_from_avg = 0;
+            err_cand = e;
+        } else {
+            restart_from_avg = 1;
+            err_cand = ea;
+        }
+        err_cand_last = (absolute(el, w) < absolute(eal, w)) ? el : eal;
+        if (!err_restart_valid) {
+            kkt(CPDLP_VEC_SOL_RESTART, &err_restart);
+            err_restart_valid = true;
+        }
+        const double ac = absolute(err_cand, w), ar = absolute(err_restart, w),
+                     acl = absolute(err_cand_last, w);
+        const bool sufficient = ac <= prm.sufficient_decay * ar;
+        const bool necessary = ac <= prm.necessary_decay * ar;
+        const bool no_local_progress = ac > acl;
+        const bool long_inner_loop = (double)inner >= prm.artificial_decay * (double)total;
+        return sufficient || (necessary && no_local_progress) || long_inner_loop;
+    }
+
+    // restart! (pdlp.jl:172-196) + primal_weight_update! (step_size.jl:58-75)
+    void restart() {
+        ProblemT<T>& P = *PT;
+        cudaStream_t s = h->stream;
+        const T* cx = restart_from_avg ? xa[cur].p : x[cur].p;
+        const T* cy = restart_from_avg ? ya[cur].p : y[cur].p;
+        eta_sum = 0.0;
+        const unsigned g = red_grid(*h, std::max(P.m, P.n));
+        k_diff_norms<T><<<g, RED_THREADS, 0, s>>>(cx, xr.p, P.n, cy, yr.p, P.m, P.red_rows.p);
+        CK_LAUNCH();
+        launches += 2;
+        double q[2];
+        fetch_reduced(*h, P.red_rows.p, g, 2, P.red_out.p, q);
+        const double dx = std::sqrt(q[0]), dy = std::sqrt(q[1]);
+        const double th = prm.primal_weight_damping;
+        if (dx > prm.zero_tol && dy > prm.zero_tol)
+            omega = std::exp(th * std::log(dy / dx) + (1.0 - th) * std::log(omega));
+        if (restart_from_avg) {
+            CK(cudaMemcpyAsync(x[cur].p, xa[cur].p, sizeof(T) * P.n, cudaMemcpyDeviceToDevice, s));
+            CK(cudaMemcpyAsync(y[cur].p, ya[cur].p, sizeof(T) * P.m, cudaMemcpyDeviceToDevice, s));
+        }
+        CK(cudaMemsetAsync(xa[cur].p, 0, sizeof(T) * P.n, s));
+        CK(cudaMemsetAsync(ya[cur].p, 0, sizeof(T) * P.m, s));
+        CK(cudaMemcpyAsync(xr.p, x[cur].p, sizeof(T) * P.n, cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemcpyAsync(yr.p, y[cur].p, sizeof(T) * P.m, cudaMemcpyDeviceToDevice, s));
+        // the restart point now equals the candidate, whose errors are known
+        err_restart = err_cand;
+        err_restart_valid = true;
+        outer += 1;
+        inner = 0;
+    }
+
+
+    int32_t solve_blocks(int64_t max_blocks) override {
+        const int ce = prm.check_every > 0 ? prm.check_every : 100;
+        int64_t blocks = 0;
+        if (!pdlp()) {
+            for (;;) {
+                if (blocks >= max_blocks) return status;
+                run_block(ce);
+                blocks++;
+                cpdlp_kkt_errors e;
+                kkt(CPDLP_VEC_SOL, &e);
+                if (termination_check_with(e)) break;
+            }
+            return status;
+        }
+        // The reference's nested loops (pdlp.jl:75-91) reduce to: block, check,
+        // restart check; on termination the outer loop checks once more.
+        for (;;) {
+            if (blocks >= max_blocks) return status;
+            run_block(ce);
+            blocks++;
+            cpdlp_kkt_errors e4[4];
+            const T* const xs[4] = {x[cur].p, xa[cur].p, x[cur ^ 1].p, xa[cur ^ 1].p};
+            const T* const ys[4] = {y[cur].p, ya[cur].p, y[cur ^ 1].p, ya[cur ^ 1].p};
+            kkt_multi<4>(xs, ys, e4);
+            if (termination_check_with(e4[0])) {
+                // the outer loop's second termination_check! (pdlp.jl:88) re-evaluates sol
+                termination_check_with(e4[0]);
+                break;
+            }
+            if (restart_check(e4)) restart();
+        }
+        return status;
+    }
+
+    void profile(int reps, double* ms) override {
+        ProblemT<T>& P = *PT;
+        cudaStream_t s = h->stream;
+        const size_t nz = (size_t)std::max<int64_t>(P.n, 1), mz = (size_t)std::max<int64_t>(P.m, 1);
+        DBuf<T> tx(nz), tb(nz), txa(nz), ty(mz), tya(mz);
+        if (!coef1.p) coef1.alloc(1);
+        StepCoef<T> k = coef_for(eta_sum);
+        CK(cudaMemcpyAsync(coef1.p, &k, sizeof(k), cudaMemcpyHostToDevice, s));
+        const int o = cur;
+        cudaEvent_t e0, e1;
+        CK(cudaEventCreate(&e0));
+        CK(cudaEventCreate(&e1));
+        auto timed = [&](auto&& launch) {
+            launch();  // warm-up
+            CK(cudaEventRecord(e0, s));
+            for (int r = 0; r < reps; r++) launch();
+            CK(cudaEventRecord(e1, s));
+            CK(cudaEventSynchronize(e1));
+            float t = 0;
+            CK(cudaEventElapsedTime(&t, e0, e1));
+            return (double)t / reps;
+        };
+        ms[0] = timed([&] {
+            PrimalEpi<T> pe{x[o].p, P.c.p, P.lv.p, P.uv.p, tx.p, tb.p, xa[o].p, txa.p, coef1.p,
+                            pdlp() ? 1 : 0};
+            launch_tiles<1>(P.planAt, view_At(P), VecSet<T, 1>{{y[o].p}}, pe, s);
+        });
+        ms[1] = timed([&] {
+            DualEpi<T> de{y[o].p, P.lc.p, P.uc.p, ty.p, ya[o].p, tya.p, coef1.p, pdlp() ? 1 : 0};
+            launch_tiles<1>(P.planA, view_A(P), VecSet<T, 1>{{xbar.p}}, de, s);
+        });
+        ms[2] = timed([&] {
+            const unsigned gA = tiles_grid(P.planA), gAt = tiles_grid(P.planAt);
+            KktRowEpi<T, 4> re;
+            re.lc = P.lc.p; re.uc = P.uc.p; re.invD1 = P.invD1.p;
+            re.y[0] = y[cur].p; re.y[1] = ya[cur].p; re.y[2] = y[cur ^ 1].p; re.y[3] = ya[cur ^ 1].p;
+            re.block_out = P.red_rows.p;
+            re.long_out = P.red_rows.p + (size_t)gA * 8;
+            VecSet<T, 4> vx{{x[cur].p, xa[cur].p, x[cur ^ 1].p, xa[cur ^ 1].p}};
+            launch_tiles<4>(P.planA, view_A(P), vx, re, s);
+            KktColEpi<T, 4> ce;
+            ce.c = P.c.p; ce.lv = P.lv.p; ce.uv = P.uv.p; ce.invD2 = P.invD2.p;
+            ce.x[0] = x[cur].p; ce.x[1] = xa[cur].p; ce.x[2] = x[cur ^ 1].p; ce.x[3] = xa[cur ^ 1].p;
+            ce.block_out = P.red_cols.p;
+            ce.long_out = P.red_cols.p + (size_t)gAt * 12;
+            VecSet<T, 4> vy{{y[cur].p, ya[cur].p, y[cur ^ 1].p, ya[cur ^ 1].p}};
+            launch_tiles<4>(P.planAt, view_At(P), vy, ce, s);
+        });
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+
+    void kernel_bytes(double* bytes) const override {
+        const ProblemT<T>& P = *PT;
+        const double nnz = (double)P.nnz, m = (double)P.m, n = (double)P.n;
+        const double sv = sizeof(T), si = sizeof(int32_t), sf = sizeof(T);
+        const bool avg = prm.algorithm == CPDLP_ALGO_PDLP;
+        // primal: A' values+indices, row pointer, gather y (m), read x c lv uv,
+        // write x+ xbar (+ avg read/write)
+        bytes[0] = nnz * (sv + si) + (n + 1) * si + sf * (m + (avg ? 8 : 6) * n);
+        // dual: A values+indices, row pointer, gather xbar (n), read y lc uc,
+        // write y+ (+ avg read/write)
+        bytes[1] = nnz * (sv + si) + (m + 1) * si + sf * (n + (avg ? 6 : 4) * m);
+        // KKT of 4 pairs: both matrices once, 4 gathered vectors per side,
+        // bounds, the 4 epilogue vectors per side, D1/D2 inverses (FP64)
+        bytes[2] = 2 * nnz * (sv + si) + (m + n + 2) * si + sf * (4 * n + 4 * m) +
+                   sf * (2 * m + 4 * m) + sf * (3 * n + 4 * n) + 8.0 * (m + n);
+    }
+
+    void early_exit_zero_problem() override {
+        ProblemT<T>& P = *PT;
+        k_proj_zero<T><<<grid_for(P.n, 256), 256, 0, h->stream>>>(x[cur].p, P.lv.p, P.uv.p, P.n);
+        CK_LAUNCH();
+        status = CPDLP_OPTIMAL;
+        CK(cudaStreamSynchronize(h->stream));
+    }
+
+    void vectors(int which, double* hx, double* hy) override {
+        ProblemT<T>& P = *PT;
+        const T *vx, *vy;
+        vec_of(which, vx, vy);
+        DBuf<double> tmp((size_t)std::max<int64_t>(std::max(P.m, P.n), 1));
+        cudaStream_t s = h->stream;
+        if (hx && P.n > 0) {
+            k_widen<T><<<grid_for(P.n, 256), 256, 0, s>>>(vx, tmp.p, P.n);
+            CK_LAUNCH();
+            CK(cudaMemcpyAsync(hx, tmp.p, sizeof(double) * P.n, cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+        }
+        if (hy && P.m > 0) {
+            k_widen<T><<<grid_for(P.m, 256), 256, 0, s>>>(vy, tmp.p, P.m);
+            CK_LAUNCH();
+            CK(cudaMemcpyAsync(hy, tmp.p, sizeof(double) * P.m, cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+        }
+    }
+
+    // get_solution (common.jl:233-235): unprecondition (preconditioning.jl:53-59)
+    void solution(double* hx, double* hy) override {
+        ProblemT<T>& P = *PT;
+        DBuf<double> tx((size_t)std::max<int64_t>(P.n, 1)), ty((size_t)std::max<int64_t>(P.m, 1));
+        cudaStream_t s = h->stream;
+        if (P.n > 0) k_unscale<T><<<grid_for(P.n, 256), 256, 0, s>>>(x[cur].p, P.D2.p, tx.p, P.n);
+        if (P.m > 0) k_unscale<T><<<grid_for(P.m, 256), 256, 0, s>>>(y[cur].p, P.D1.p, ty.p, P.m);
+        CK_LAUNCH();
+        if (hx && P.n > 0) CK(cudaMemcpyAsync(hx, tx.p, sizeof(double) * P.n, cudaMemcpyDeviceToHost, s));
+        if (hy && P.m > 0) CK(cudaMemcpyAsync(hy, ty.p, sizeof(double) * P.m, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+    }
+};
+
+template <class T>
+StateBase* make_state(Handle& h, ProblemT<T>* P, const cpdlp_params* prm, const double* x0,
+                      const double* y0) {
+    double t0 = now_seconds();
+    auto* S = new StateT<T>();
+    std::unique_ptr<StateT<T>> guard(S);
+    S->P = P;
+    S->PT = P;
+    S->h = &h;
+    S->prm = *prm;
+    S->starting_time = t0;
+    cudaStream_t s = h.stream;
+    const int64_t m = P->m, n = P->n;
+    const size_t nz = (size_t)(n > 0 ? n : 1), mz = (size_t)(m > 0 ? m : 1);
+    for (int b = 0; b < 2; b++) {
+        S->x[b].alloc(nz); S->y[b].alloc(mz); S->xa[b].alloc(nz); S->ya[b].alloc(mz);
+    }
+    S->xr.alloc(nz); S->yr.alloc(mz); S->xbar.alloc(nz);
+    // sol = precondition(sol_init): x ./ D2, y ./ D1 (preconditioning.jl:45-51)
+    DBuf<double> tx(nz), ty(mz);
+    if (x0 && n > 0) CK(cudaMemcpyAsync(tx.p, x0, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    else CK(cudaMemsetAsync(tx.p, 0, sizeof(double) * nz, s));
+    if (y0 && m > 0) CK(cudaMemcpyAsync(ty.p, y0, sizeof(double) * m, cudaMemcpyHostToDevice, s));
+    else CK(cudaMemsetAsync(ty.p, 0, sizeof(double) * mz, s));
+    if (n > 0) k_prescale<T><<<grid_for(n, 256), 256, 0, s>>>(tx.p, P->D2.p, S->x[0].p, n);
+    if (m > 0) k_prescale<T><<<grid_for(m, 256), 256, 0, s>>>(ty.p, P->D1.p, S->y[0].p, m);
+    CK_LAUNCH();
+    // sol_last = zero(sol), sol_avg = copy(sol), sol_avg_last = zero(sol), sol_restart = copy(sol)
+    CK(cudaMemsetAsync(S->x[1].p, 0, sizeof(T) * nz, s));
+    CK(cudaMemsetAsync(S->y[1].p, 0, sizeof(T) * mz, s));
+    CK(cudaMemcpyAsync(S->xa[0].p, S->x[0].p, sizeof(T) * nz, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(S->ya[0].p, S->y[0].p, sizeof(T) * mz, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemsetAsync(S->xa[1].p, 0, sizeof(T) * nz, s));
+    CK(cudaMemsetAsync(S->ya[1].p, 0, sizeof(T) * mz, s));
+    CK(cudaMemcpyAsync(S->xr.p, S->x[0].p, sizeof(T) * nz, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(S->yr.p, S->y[0].p, sizeof(T) * mz, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemsetAsync(S->xbar.p, 0, sizeof(T) * nz, s));
+    S->cur = 0;
+    // fixed_stepsize (step_size.jl:22-27)
+    double sn = spectral_norm_T(h, *P, prm, &S->power_iterations);
+    S->eta = prm->invnorm_scaling * (1.0 / sn);
+    // primal_weight_init (step_size.jl:29-40); PDHG: omega = 1 (pdhg.jl:48)
+    if (prm->algorithm == CPDLP_ALGO_PDHG) {
+        S->omega = 1.0;
+    } else {
+        unsigned g = red_grid(h, std::max(m, n));
+        k_scales<T><<<g, RED_THREADS, 0, s>>>(P->lc.p, P->uc.p, P->invD1.p, m, P->c.p,
+                                              P->invD2.p, n, P->red_rows.p);
+        CK_LAUNCH();
+        double q[4];
+        fetch_reduced(h, P->red_rows.p, g, 4, P->red_out.p, q);
+        const double c_norm = std::sqrt(q[3]), cb_norm = std::sqrt(q[1]);
+        S->omega = (c_norm > prm->zero_tol && cb_norm > prm->zero_tol) ? c_norm / cb_norm : 1.0;
+    }
+    S->eta_sum = 0.0;
+    for (auto* e : {&S->err, &S->err_cand, &S->err_cand_last, &S->err_restart})
+        e->primal = e->primal_scale = e->dual = e->dual_scale = e->gap = e->gap_scale = NAN;
+    CK(cudaStreamSynchronize(s));
+    S->setup_seconds = P->setup_seconds + (now_seconds() - t0);
+    guard.release();
+    return S;
+}
+
+}  // namespace
+
+void StateBase::stats(cpdlp_stats* st) const {
+    memset(st, 0, sizeof(*st));
+    st->err = err;
+    st->time_elapsed = time_elapsed;
+    st->kkt_passes = kkt_passes;
+    st->termination_status = status;
+    st->restart_from_avg = restart_from_avg;
+    st->outer = outer;
+    st->inner = inner;
+    st->total = total;
+    st->eta = eta;
+    st->eta_sum = eta_sum;
+    st->omega = omega;
+    st->history_length = (int64_t)hist_passes.size();
+    st->power_iterations = power_iterations;
+    st->refine_kkt_passes = refine_passes;
+    st->setup_seconds = setup_seconds;
+    st->kernel_launches = launches;
+}
+
+ProblemBase* problem_create(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm) {
+    if (!lp || !prm) fail(CPDLP_ERR_ARGUMENT, "null lp or params");
+    if (lp->m < 0 || lp->n < 0) fail(CPDLP_ERR_DIMENSION, "negative problem size");
+    if (prm->float_type == CPDLP_VAL_F32) return make_problem<float>(h, lp, prm);
+    if (prm->float_type == CPDLP_VAL_F64) return make_problem<double>(h, lp, prm);
+    fail(CPDLP_ERR_ARGUMENT, "float_type must be CPDLP_VAL_F64 or CPDLP_VAL_F32");
+}
+
+StateBase* state_create(Handle& h, ProblemBase* P, const cpdlp_params* prm, const double* x0,
+                        const double* y0) {
+    if (!P || !prm) fail(CPDLP_ERR_ARGUMENT, "null problem or params");
+    if (prm->check_every <= 0) fail(CPDLP_ERR_ARGUMENT, "check_every must be positive");
+    if (P->vt == CPDLP_VAL_F32)
+        return make_state<float>(h, static_cast<ProblemT<float>*>(P), prm, x0, y0);
+    return make_state<double>(h, static_cast<ProblemT<double>*>(P), prm, x0, y0);
+}
+
+double problem_spectral_norm(Handle& h, ProblemBase* P, const cpdlp_params* prm, int64_t* iters) {
+    if (P->vt == CPDLP_VAL_F32)
+        return spectral_norm_T<float>(h, *static_cast<ProblemT<float>*>(P), prm, iters);
+    return spectral_norm_T<double>(h, *static_cast<ProblemT<double>*>(P), prm, iters);
+}
+
+void problem_scaling(Handle& h, ProblemBase* P, double* d1, double* d2) {
+    if (d1 && P->m > 0)
+        CK(cudaMemcpyAsync(d1, P->D1.p, sizeof(double) * P->m, cudaMemcpyDeviceToHost, h.stream));
+    if (d2 && P->n > 0)
+        CK(cudaMemcpyAsync(d2, P->D2.p, sizeof(double) * P->n, cudaMemcpyDeviceToHost, h.stream));
+    CK(cudaStreamSynchronize(h.stream));
+}
+
+}  // namespace cpdlp

@@ -1,0 +1,82 @@
+// solver.cuh -- single-LP PDLP / PDHG on the device.
+#pragma once
+
+#include "cpdlp_common.cuh"
+#include "sparse_build.cuh"
+#include "tiles.cuh"
+
+namespace cpdlp {
+
+// Scalars of one step, in the iterate type T (pdlp.jl:108, :126-136).
+template <class T>
+struct StepCoef {
+    T tau, sigma, inv_sigma, a, b;
+};
+
+// A preprocessed LP resident on the device (the MILP after preprocess,
+// common.jl:154-169).  The CSR of A (rows of A) and of A' (rows of A') hold
+// A's and A''s scaled values respectively, as the reference scales its two
+// CSC copies separately (preconditioning.jl:37-43).
+struct ProblemBase {
+    virtual ~ProblemBase() = default;
+    Handle* h = nullptr;
+    int32_t vt = CPDLP_VAL_F64;   // iterate / matrix value type
+    int64_t m = 0, n = 0, nnz = 0;
+    DBuf<int32_t> a_ptr, a_idx, at_ptr, at_idx;
+    TilePlan planA, planAt;
+    DBuf<double> D1, D2, invD1, invD2;
+    double primal_scale = 0, dual_scale = 0;
+    bool zero_cost = false;
+    cpdlp_params prm{};
+    double setup_seconds = 0;
+    // reduction scratch (FP64 block partials) sized for NVEC = 4
+    DBuf<double> red_rows, red_cols, red_out;
+    int64_t rows_A_partials = 0, rows_At_partials = 0;
+};
+
+template <class T>
+struct ProblemT : ProblemBase {
+    DBuf<T> a_val, at_val;
+    DBuf<T> c, lv, uv, lc, uc;
+    DBuf<T> partA, partAt;   // long-row piece partials, NVEC = 4
+};
+
+struct StateBase {
+    virtual ~StateBase() = default;
+    ProblemBase* P = nullptr;
+    cpdlp_params prm{};
+    double eta = 0, eta_sum = 0, omega = 1;
+    int64_t outer = 0, inner = 0, total = 0, kkt_passes = 0;
+    int32_t status = CPDLP_STILL_RUNNING;
+    int32_t restart_from_avg = 0;
+    cpdlp_kkt_errors err{}, err_cand{}, err_cand_last{}, err_restart{};
+    bool err_restart_valid = false;
+    double starting_time = 0, time_elapsed = 0, setup_seconds = 0;
+    int64_t power_iterations = 0;
+    int64_t refine_passes = 0;
+    int64_t launches = 0;  // kernels of this library launched by the state
+    std::vector<int64_t> hist_passes;
+    std::vector<cpdlp_kkt_errors> hist_err;
+    virtual void step(int64_t count) = 0;
+    // solve! (pdlp.jl:69-94) with at most `max_blocks` rounds of check_every
+    // steps + checks; returns STILL_RUNNING when the budget runs out.
+    virtual int32_t solve_blocks(int64_t max_blocks) = 0;
+    int32_t solve() { return solve_blocks(INT64_MAX); }
+    // mean ms per launch of the primal step, dual step and 4-vector KKT kernels
+    virtual void profile(int reps, double* ms) = 0;
+    // algorithmic bytes per launch of the same three kernels
+    virtual void kernel_bytes(double* bytes) const = 0;
+    virtual void kkt(int which, cpdlp_kkt_errors* e) = 0;
+    virtual void vectors(int which, double* x, double* y) = 0;
+    virtual void solution(double* x, double* y) = 0;
+    virtual void early_exit_zero_problem() = 0;
+    void stats(cpdlp_stats* st) const;
+};
+
+ProblemBase* problem_create(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm);
+StateBase* state_create(Handle& h, ProblemBase* P, const cpdlp_params* prm, const double* x0,
+                        const double* y0);
+double problem_spectral_norm(Handle& h, ProblemBase* P, const cpdlp_params* prm, int64_t* iters);
+void problem_scaling(Handle& h, ProblemBase* P, double* d1, double* d2);
+
+}  // namespace cpdlp

@@ -1,0 +1,42 @@
+// sparse_build.cuh -- device construction of the sparse formats.
+#pragma once
+
+#include "cpdlp_common.cuh"
+
+namespace cpdlp {
+
+// Exclusive prefix sum of `n` int32 counts into `out` (n+1 entries, out[n] =
+// total), on `stream`.  Deterministic.
+void exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, cudaStream_t stream);
+
+// Stable LSD radix sort (8-bit digits) of `n` (key, payload) pairs by key,
+// keys < 2^key_bits.  Inputs are consumed (used as ping-pong space); the
+// sorted pairs end in *keys/*vals (pointers may be swapped).
+void radix_sort_pairs(uint32_t*& keys, uint32_t*& vals, uint32_t*& keys_tmp, uint32_t*& vals_tmp,
+                      int64_t n, int key_bits, cudaStream_t stream);
+
+// A CSC matrix uploaded to the device, validated, with its transpose.
+//   S1 = CSC(A) = CSR(A'): ptr1 (n+1), idx1 (row of A), col1 (column of each entry)
+//   S2 = CSR(A) = CSC(A'): ptr2 (m+1), idx2 (column of A), row2 (row of each entry)
+//   p21[k2] = S1 position of S2 entry k2 (the permutation of sparse(transpose(A)))
+//   val1: input values in S1 order (double)
+struct CscPair {
+    int64_t m = 0, n = 0, nnz = 0;
+    DBuf<int32_t> ptr1, idx1, col1, ptr2, idx2, row2, p21;
+    DBuf<double> val1;
+};
+
+// Uploads 1-based CSC host arrays, validates them on the device (monotone
+// colptr, rows in range and strictly ascending inside each column) and builds
+// the transpose.  Throws Error(CPDLP_ERR_ARGUMENT/DIMENSION/UNSUPPORTED).
+void build_csc_pair(Handle& h, int64_t m, int64_t n, int64_t nnz, const int64_t* colptr1,
+                    const int64_t* rowval1, const double* nzval, CscPair& out);
+
+// Expands a row-pointer array into the row index of every entry.
+void expand_rows(const int32_t* ptr, int64_t rows, int32_t* row_of, int64_t nnz, cudaStream_t s);
+
+// Gathers `out[k] = in[perm[k]]`, converting the value type.
+template <class TO, class TI>
+void gather_values(const TI* in, const int32_t* perm, TO* out, int64_t nnz, cudaStream_t s);
+
+}  // namespace cpdlp

@@ -1,0 +1,96 @@
+// tiles.cu -- host side of the warp-tile partition and the partial reduction.
+#include "tiles.cuh"
+
+namespace cpdlp {
+
+int choose_items(int64_t nnz, int64_t rows, int requested_tile_nnz) {
+    if (requested_tile_nnz > 0) {
+        if (requested_tile_nnz <= 128) return 4;
+        if (requested_tile_nnz <= 256) return 8;
+        return 16;
+    }
+    // Autotuner default: the tile should hold many short rows (so that row
+    // sums are sequential and the lanes stay busy) while a warp issues enough
+    // independent loads; 512 nonzeros per warp for typical LPs, smaller tiles
+    // for very sparse matrices so that the grid still fills 152 SMs.
+    double mean = rows > 0 ? (double)nnz / (double)rows : 0.0;
+    if (nnz < 152LL * 8 * 128) return 4;
+    if (mean < 2.0 || nnz < 152LL * 8 * 512 * 2) return 8;
+    return 16;
+}
+
+void build_tile_plan(const std::vector<int32_t>& ptr, int32_t rows, int items, TilePlan& plan,
+                     cudaStream_t s) {
+    plan.rows = rows;
+    plan.items = items;
+    const int tile = 32 * items;
+    std::vector<int4> longs, shorts;
+    plan.long_rows.clear();
+    int32_t slot = 0;
+    int32_t r = 0;
+    while (r < rows) {
+        int32_t len = ptr[r + 1] - ptr[r];
+        if (len > tile) {
+            int32_t lid = (int32_t)plan.long_rows.size();
+            int32_t np = (len + tile - 1) / tile;
+            for (int32_t p = 0; p < np; p++) longs.push_back(make_int4(r, p, lid, slot));
+            plan.long_rows.push_back(r);
+            slot += np;
+            r++;
+            continue;
+        }
+        int32_t r0 = r, nz = 0;
+        while (r < rows && r - r0 < MAX_TILE_ROWS) {
+            int32_t l = ptr[r + 1] - ptr[r];
+            if (l > tile || nz + l > tile) break;
+            nz += l;
+            r++;
+        }
+        shorts.push_back(make_int4(r0, r, -1, 0));
+    }
+    plan.nlong = (int32_t)plan.long_rows.size();
+    plan.npieces = slot;
+    plan.nshort = (int32_t)shorts.size();
+    // long-row pieces first: they start early and the short tiles fill the tail
+    std::vector<int4> all;
+    all.reserve(longs.size() + shorts.size());
+    all.insert(all.end(), longs.begin(), longs.end());
+    all.insert(all.end(), shorts.begin(), shorts.end());
+    plan.ntasks = (int32_t)all.size();
+    plan.tasks.alloc(all.size() ? all.size() : 1);
+    if (!all.empty())
+        CK(cudaMemcpyAsync(plan.tasks.p, all.data(), sizeof(int4) * all.size(),
+                           cudaMemcpyHostToDevice, s));
+    plan.counters.alloc(plan.nlong ? (size_t)plan.nlong : 1);
+    CK(cudaMemsetAsync(plan.counters.p, 0, sizeof(int32_t) * plan.counters.n, s));
+    CK(cudaStreamSynchronize(s));
+}
+
+namespace {
+__global__ void k_reduce_partials(const double* __restrict__ part, int64_t nrows, int q,
+                                  double* __restrict__ out) {
+    __shared__ double red[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int j = 0; j < q; j++) {
+        double s = 0.0;
+        for (int64_t r = threadIdx.x; r < nrows; r += blockDim.x) s += part[r * q + j];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) red[w] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int ww = 0; ww < (int)(blockDim.x >> 5); ww++) t += red[ww];
+            out[j] = t;
+        }
+        __syncthreads();
+    }
+}
+}  // namespace
+
+void reduce_partials(const double* partials, int64_t nrows, int q, double* out, cudaStream_t s) {
+    k_reduce_partials<<<1, 1024, 0, s>>>(partials, nrows, q, out);
+    CK_LAUNCH();
+}
+
+}  // namespace cpdlp

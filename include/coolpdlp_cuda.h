@@ -1,0 +1,309 @@
+/*
+ * coolpdlp_cuda.h -- C ABI of libcoolpdlp_cuda, the GB300 (sm_103a) PDLP/PDHG solver.
+ *
+ * Every entry point is plain C: pointers, sizes and status codes, no C++ or
+ * torch types.  A Julia package binds it with `ccall`, Python with `ctypes`.
+ * Each declaration names the CoolPDLP.jl interface it replaces (paths are
+ * relative to the CoolPDLP.jl source tree).
+ *
+ * Conventions
+ *  - Every call returns an int status: CPDLP_OK (0) or a CPDLP_ERR_* code.
+ *    The message of the last failure on a handle is cpdlp_last_error(h).
+ *    CPDLP_ERR_DIMENSION maps to Julia's DimensionMismatch, CPDLP_ERR_ARGUMENT
+ *    to ArgumentError (src/problems/milp.jl:72-90, src/utils/device.jl:9).
+ *  - Solver outcomes (OPTIMAL, TIME_LIMIT, ITERATION_LIMIT) are statuses in
+ *    cpdlp_stats, never errors (src/components/termination.jl:13).
+ *  - Index arrays cross the ABI 1-based, in Julia's SparseMatrixCSC layout, so
+ *    that exported CSR/ELL/COO indices compare bit-for-bit with the Julia ones.
+ *  - Host arrays belong to the caller and are copied in.  Device buffers made
+ *    by the library belong to the handle (or the object) and are freed by the
+ *    matching *_destroy call.  Pointers documented as "device" are CUDA device
+ *    pointers owned by the caller.
+ *  - A handle owns one CUDA stream; use one handle per host thread.
+ *  - Missing bounds are +-INFINITY, as in the reference.
+ */
+#ifndef COOLPDLP_CUDA_H
+#define COOLPDLP_CUDA_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CPDLP_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+    CPDLP_OK = 0,
+    CPDLP_ERR_ARGUMENT = 1,      /* ArgumentError: bad pointer, bad CSC, bad enum */
+    CPDLP_ERR_DIMENSION = 2,     /* DimensionMismatch */
+    CPDLP_ERR_CUDA = 3,          /* a CUDA runtime call failed */
+    CPDLP_ERR_OUT_OF_MEMORY = 4, /* device allocation failed or admission refused */
+    CPDLP_ERR_TIMEOUT = 5,       /* a bounded device wait ran out */
+    CPDLP_ERR_NOT_FOUND = 6,     /* unknown ticket / object */
+    CPDLP_ERR_UNSUPPORTED = 7    /* size or feature outside what this build handles */
+};
+
+/* ---- enums mirrored from the reference ---------------------------------- */
+/* TerminationStatus, same order as src/components/termination.jl:13 */
+enum {
+    CPDLP_OPTIMAL = 0,
+    CPDLP_TIME_LIMIT = 1,
+    CPDLP_ITERATION_LIMIT = 2,
+    CPDLP_STILL_RUNNING = 3
+};
+
+/* Algorithm{:PDLP} / Algorithm{:PDHG} (src/algorithms/pdlp.jl:6-11, pdhg.jl:6-16) */
+enum { CPDLP_ALGO_PDLP = 0, CPDLP_ALGO_PDHG = 1 };
+
+/* float_type of ConversionParameters (src/components/conversion.jl:14-30).
+ * CPDLP_VAL_PM1 stores matrix values of exactly +-1 as one signed byte. */
+enum { CPDLP_VAL_F64 = 0, CPDLP_VAL_F32 = 1, CPDLP_VAL_PM1 = 2 };
+
+/* matrix_type: GPUSparseMatrixCSR / ELL / COO (src/utils/mat_*.jl) */
+enum { CPDLP_FMT_CSR = 0, CPDLP_FMT_ELL = 1, CPDLP_FMT_COO = 2 };
+
+/* which iterate to read back from a solver state (src/algorithms/pdlp.jl:20-43) */
+enum {
+    CPDLP_VEC_SOL = 0,
+    CPDLP_VEC_SOL_LAST = 1,
+    CPDLP_VEC_SOL_AVG = 2,
+    CPDLP_VEC_SOL_AVG_LAST = 3,
+    CPDLP_VEC_SOL_RESTART = 4
+};
+
+/* ---- plain data ------------------------------------------------------- */
+
+/* KKTErrors (src/components/errors.jl:8-21), in unscaled units. */
+typedef struct cpdlp_kkt_errors {
+    double primal;
+    double primal_scale;
+    double dual;
+    double dual_scale;
+    double gap;
+    double gap_scale;
+} cpdlp_kkt_errors;
+
+/* Every keyword of Algorithm{A}(T, Ti, M; ...) (src/algorithms/common.jl:53-116)
+ * plus the power-method settings of spectral_norm (src/utils/linalg.jl:86-96)
+ * and the extensions of this library (marked EXT).  Fill with
+ * cpdlp_params_default() and override fields. */
+typedef struct cpdlp_params {
+    int32_t algorithm;              /* CPDLP_ALGO_* */
+    int32_t float_type;             /* CPDLP_VAL_F64 or CPDLP_VAL_F32: iterate precision */
+    /* preconditioning (src/components/preconditioning.jl:134-139) */
+    double chambolle_pock_alpha;    /* 1.0 */
+    int32_t ruiz_iter;              /* 10 (PDLP), 0 (PDHG) */
+    /* step sizes (src/components/step_size.jl:8-15) */
+    double invnorm_scaling;         /* 0.9 */
+    double primal_weight_damping;   /* 0.5 (PDLP), NaN (PDHG) */
+    double zero_tol;                /* 1e-8 */
+    /* restart (src/components/restart.jl:8-15) */
+    double sufficient_decay;        /* 0.2 */
+    double necessary_decay;         /* 0.8 */
+    double artificial_decay;        /* 0.36 */
+    /* generic (src/components/generic.jl:8-15) */
+    int32_t show_progress;          /* 0; progress is printed by the caller */
+    int32_t check_every;            /* 100 */
+    int32_t record_error_history;   /* 1 */
+    /* termination (src/components/termination.jl:22-29) */
+    double termination_reltol;      /* 1e-4 */
+    int64_t max_kkt_passes;         /* 100000 */
+    double time_limit;              /* 100.0 seconds */
+    /* spectral norm power method: IterativeSolvers.powm! defaults are
+     * tol = eps(T) * n^3 (Int64 arithmetic, wraps like Julia's) and
+     * maxiter = n.  power_tol_override > 0 or power_maxiter_override > 0
+     * replace them (EXT). */
+    double power_tol_override;      /* 0 = reference default */
+    int64_t power_maxiter_override; /* 0 = reference default */
+    uint64_t power_seed;            /* start vector seed (EXT; the reference uses StableRNG(0)) */
+    /* EXT: final FP64 refinement after an FP32 solve reaches termination_reltol:
+     * continue in FP64 from the FP32 iterate until refine_reltol (0 = off). */
+    double refine_reltol;
+    /* EXT: CSR tile size in nonzeros for the SpMV work partition (0 = autotune). */
+    int32_t tile_nnz;
+    int32_t reserved0;
+} cpdlp_params;
+
+/* An LP in the reference's "cuPDLPx form" (src/problems/milp.jl:1-20):
+ *   min c'x  s.t.  lv <= x <= uv,  lc <= A x <= uc
+ * A is m x n in Julia SparseMatrixCSC layout: 1-based colptr (n+1), 1-based
+ * rowval (nnz), rows strictly ascending inside each column. */
+typedef struct cpdlp_lp {
+    int64_t m;
+    int64_t n;
+    int64_t nnz;
+    const int64_t* colptr;
+    const int64_t* rowval;
+    const double* nzval;
+    const double* c;
+    const double* lv;
+    const double* uv;
+    const double* lc;
+    const double* uc;
+} cpdlp_lp;
+
+/* ConvergenceStats (src/components/termination.jl:44-76) + IterationCounter
+ * (src/components/iteration.jl) + StepSizes (src/components/step_size.jl:49-56). */
+typedef struct cpdlp_stats {
+    cpdlp_kkt_errors err;
+    double time_elapsed;
+    int64_t kkt_passes;
+    int32_t termination_status;     /* CPDLP_OPTIMAL ... */
+    int32_t restart_from_avg;
+    int64_t outer;
+    int64_t inner;
+    int64_t total;
+    double eta;
+    double eta_sum;
+    double omega;
+    int64_t history_length;         /* entries in the error history */
+    int64_t power_iterations;       /* EXT: power-method iterations run */
+    int64_t refine_kkt_passes;      /* EXT: passes spent in FP64 refinement */
+    double setup_seconds;           /* EXT: preprocess + initialize wall time */
+    int64_t kernel_launches;        /* EXT: this library's kernels launched by the state */
+} cpdlp_stats;
+
+typedef struct cpdlp_handle cpdlp_handle;
+typedef struct cpdlp_matrix cpdlp_matrix;
+typedef struct cpdlp_problem cpdlp_problem;
+typedef struct cpdlp_state cpdlp_state;
+
+/* ---- library & handle ----------------------------------------------------- */
+int cpdlp_abi_version(void);
+
+/* Default keywords of Algorithm{:PDLP} (src/algorithms/common.jl:53-116) or of
+ * PDHG() (src/algorithms/pdhg.jl:6-16, which sets ruiz_iter = 0 and NaN
+ * restart/weight parameters). */
+void cpdlp_params_default(cpdlp_params* params, int32_t algorithm);
+
+/* Backend selection: the KernelAbstractions backend object of the reference
+ * (src/components/conversion.jl:14-30); `device` is a CUDA ordinal. */
+int cpdlp_create(int32_t device, cpdlp_handle** out);
+int cpdlp_destroy(cpdlp_handle* h);
+const char* cpdlp_last_error(const cpdlp_handle* h);
+int cpdlp_synchronize(cpdlp_handle* h);
+/* The handle's CUDA stream (cudaStream_t), for callers that order their own work after ours. */
+void* cpdlp_stream(cpdlp_handle* h);
+
+/* ---- pluggable sparse matrices (src/utils/mat_csr.jl, mat_ell.jl, mat_coo.jl) ---- */
+
+/* M(::SparseMatrixCSC): GPUSparseMatrixCSR (mat_csr.jl:58-61),
+ * GPUSparseMatrixELL (mat_ell.jl:54-70), GPUSparseMatrixCOO (mat_coo.jl:50-53).
+ * The format is built on the device from the 1-based CSC arrays.
+ * value_type: CPDLP_VAL_F64 or CPDLP_VAL_F32 (the matrix eltype T). */
+int cpdlp_matrix_from_csc(cpdlp_handle* h, int64_t m, int64_t n, int64_t nnz,
+                          const int64_t* colptr, const int64_t* rowval,
+                          const double* nzval, int32_t format, int32_t value_type,
+                          cpdlp_matrix** out);
+int cpdlp_matrix_destroy(cpdlp_matrix* A);
+
+/* size(A), nnz(A) (mat_*.jl: size / SparseArrays.nnz) and the ELL width d. */
+int cpdlp_matrix_shape(const cpdlp_matrix* A, int64_t* m, int64_t* n, int64_t* nnz,
+                       int64_t* width);
+
+/* Copy the stored arrays to host, 1-based, exactly as the Julia struct fields:
+ *  CSR: ptr = rowptr (m+1), idx = colval (nnz), val = nzval (nnz)
+ *  ELL: ptr unused, idx = colval (m*d, column-major, 0 = padding), val = nzval (m*d)
+ *  COO: ptr = rowval (nnz), idx = colval (nnz), val = nzval (nnz)
+ * Values are widened to double. */
+int cpdlp_matrix_export(cpdlp_handle* h, const cpdlp_matrix* A, int64_t* ptr,
+                        int64_t* idx, double* val);
+
+/* LinearAlgebra.mul!(c, A, b, alpha, beta) (mat_csr.jl:81-92, mat_ell.jl:91-102,
+ * mat_coo.jl:68-80): c = alpha*A*b + beta*c with b, c DEVICE vectors of the
+ * matrix eltype.  beta == 0 is a strong zero: c is not read. */
+int cpdlp_spmv(cpdlp_handle* h, const cpdlp_matrix* A, const void* b, void* c,
+               double alpha, double beta);
+
+/* ---- solve path (src/algorithms/common.jl, pdlp.jl, pdhg.jl) ----------- */
+
+/* preprocess(milp, sol, algo) (common.jl:154-169): Ruiz + Pock-Chambolle
+ * scaling, conversion to params->float_type and the CSR builds of A and A',
+ * all on the device. */
+int cpdlp_problem_create(cpdlp_handle* h, const cpdlp_lp* lp, const cpdlp_params* params,
+                         cpdlp_problem** out);
+int cpdlp_problem_destroy(cpdlp_problem* p);
+/* The cumulative preconditioner D1 (m) and D2 (n) of the scaled MILP
+ * (preconditioning.jl:61-91). */
+int cpdlp_problem_scaling(cpdlp_handle* h, const cpdlp_problem* p, double* d1, double* d2);
+
+/* initialize(milp, sol, algo) (pdlp.jl:45-67, pdhg.jl:40-54): the starting
+ * point x0 (n), y0 (m) is in the ORIGINAL units (NULL = zeros) and is
+ * preconditioned like precondition(sol, prec) (preconditioning.jl:45-51);
+ * runs the power method for the fixed step size. */
+int cpdlp_state_create(cpdlp_handle* h, cpdlp_problem* p, const cpdlp_params* params,
+                       const double* x0, const double* y0, cpdlp_state** out);
+int cpdlp_state_destroy(cpdlp_state* s);
+
+/* solve!(state, milp, algo) (pdlp.jl:69-94, pdhg.jl:56-74). */
+int cpdlp_state_solve(cpdlp_handle* h, cpdlp_state* s, cpdlp_stats* stats);
+
+/* solve! with a budget (EXT): at most `max_blocks` rounds of (check_every
+ * steps + termination check + restart check) of pdlp.jl:75-91; returns with
+ * termination_status CPDLP_STILL_RUNNING when the budget ran out, and a later
+ * call continues where this one stopped. */
+int cpdlp_state_solve_blocks(cpdlp_handle* h, cpdlp_state* s, int64_t max_blocks,
+                             cpdlp_stats* stats);
+
+/* EXT, measurement: mean milliseconds per launch, over `reps` launches timed
+ * with CUDA events on the handle's stream, of ms[0] the fused primal step
+ * kernel, ms[1] the fused dual step kernel, ms[2] the four-iterate KKT pass.
+ * Outputs go to scratch buffers: the state is unchanged. */
+int cpdlp_state_profile(cpdlp_handle* h, cpdlp_state* s, int32_t reps, double* ms);
+
+/* EXT, measurement: algorithmic bytes moved by one launch of the same three
+ * kernels (each matrix array and vector read or written once). */
+int cpdlp_state_kernel_bytes(const cpdlp_state* s, double* bytes);
+
+/* `count` calls of step!(state, milp) (pdlp.jl:96-124, pdhg.jl:76-102)
+ * with no termination or restart check in between. */
+int cpdlp_state_step(cpdlp_handle* h, cpdlp_state* s, int64_t count);
+
+/* kkt_errors!(scratch, sol, milp) (errors.jl:65-109) of one stored iterate. */
+int cpdlp_state_kkt(cpdlp_handle* h, cpdlp_state* s, int32_t which, cpdlp_kkt_errors* err);
+
+/* Stored iterates in the SCALED units of the preconditioned problem, widened to
+ * double (x: n, y: m). */
+int cpdlp_state_vectors(cpdlp_handle* h, const cpdlp_state* s, int32_t which, double* x,
+                        double* y);
+
+/* get_solution(state, milp) (common.jl:233-235): the current iterate,
+ * unpreconditioned, in double. */
+int cpdlp_state_solution(cpdlp_handle* h, const cpdlp_state* s, double* x, double* y);
+
+/* Current stats without solving. */
+int cpdlp_state_stats(cpdlp_handle* h, const cpdlp_state* s, cpdlp_stats* stats);
+
+/* stats.error_history (termination.jl:44-76, pushed at common.jl:226-228):
+ * copies up to `capacity` entries, `count` receives the full length. */
+int cpdlp_state_history(const cpdlp_state* s, int64_t* kkt_passes, cpdlp_kkt_errors* errs,
+                        int64_t capacity, int64_t* count);
+
+/* solve(milp, sol, algo) (common.jl:186-209): preprocess, initialize, the
+ * empty-problem early exit, solve!, get_solution.  x0/y0 may be NULL (zeros);
+ * x_out (n) and y_out (m) receive the unpreconditioned solution. */
+int cpdlp_solve(cpdlp_handle* h, const cpdlp_lp* lp, const cpdlp_params* params,
+                const double* x0, const double* y0, double* x_out, double* y_out,
+                cpdlp_stats* stats);
+
+/* spectral_norm(A, A') (linalg.jl:86-96) of the problem's scaled matrix in its
+ * float type, with the power-method settings of `params`. */
+int cpdlp_problem_spectral_norm(cpdlp_handle* h, cpdlp_problem* p, const cpdlp_params* params,
+                                double* norm, int64_t* iterations);
+
+/* ---- batched solve (many independent LPs in one persistent launch) -------
+ * No counterpart in the reference, which solves one LP per call: this is the
+ * batched form of solve(milp, algo) (common.jl:203-209) over `count` LPs.
+ * x_out[k] / y_out[k] receive LP k's solution (NULL pointers skip the copy);
+ * stats[k] its ConvergenceStats.  All LPs share `params`. */
+int cpdlp_batch_solve(cpdlp_handle* h, int64_t count, const cpdlp_lp* lps,
+                      const cpdlp_params* params, double* const* x_out,
+                      double* const* y_out, cpdlp_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* COOLPDLP_CUDA_H */
