@@ -5,6 +5,7 @@
 #include <new>
 
 #include "batch.cuh"
+#include "tiles.cuh"
 #include "matrix.cuh"
 #include "solver.cuh"
 
@@ -164,6 +165,7 @@ int cpdlp_spmv(cpdlp_handle* h, const cpdlp_matrix* A, const void* b, void* c, d
     return guarded(h, [&] {
         matrix_spmv(*H(h), *reinterpret_cast<const Matrix*>(A), b, c, alpha, beta);
         CK(cudaStreamSynchronize(h->stream));
+        check_tile_error(h->stream);
     });
 }
 

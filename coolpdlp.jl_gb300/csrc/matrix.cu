@@ -16,13 +16,21 @@ struct MulEpi {  // c[i] = alpha*s + beta*c[i]; beta == 0 does not read c (mat_c
     T alpha, beta;
     int use_beta;
     struct Acc {};
+    struct Pre { T c; };
+    static constexpr int NPRE = 1;
+    static constexpr int pre_esz(int) { return (int)sizeof(T); }
+    __device__ const void* pre_src(int) const { return use_beta ? (const void*)out : nullptr; }
+    __device__ Pre pre_global(int r) const { return Pre{use_beta ? out[r] : T(0)}; }
+    __device__ Pre pre_staged(const Staged<NPRE>& st, int r) const {
+        return Pre{use_beta ? st.template get<T>(0, r) : T(0)};
+    }
     __device__ void init(Acc&) {}
-    __device__ __forceinline__ void row(int, int r, T s, Acc&) {
+    __device__ __forceinline__ void row(int, int r, T s, const Pre& q, Acc&) {
         T v = mul_rn(alpha, s);
-        if (use_beta) v = add_rn(v, mul_rn(beta, out[r]));
+        if (use_beta) v = add_rn(v, mul_rn(beta, q.c));
         out[r] = v;
     }
-    __device__ void row_long(int p, int r, T s, int, Acc& a) { row(p, r, s, a); }
+    __device__ void row_long(int p, int r, T s, int, Acc& a) { row(p, r, s, pre_global(r), a); }
     __device__ void finish(Acc&) {}
 };
 
@@ -117,8 +125,10 @@ void build_T(Handle& h, Matrix& M, CscPair& S) {
         CK(cudaStreamSynchronize(s));
         return;
     }
-    // CSR of A: S2 structure with A's values permuted into it
-    DBuf<T> v2(zn);
+    // CSR of A: S2 structure with A's values permuted into it (padded for the
+    // aligned 128-bit tile loads)
+    DBuf<T> v2(zn + PAD_ELEMS);
+    CK(cudaMemsetAsync(v2.p, 0, sizeof(T) * (zn + PAD_ELEMS), s));
     gather_values<T, double>(S.val1.p, S.p21.p, v2.p, nnz, s);
     std::vector<int32_t> hp((size_t)m + 1);
     CK(cudaMemcpyAsync(hp.data(), S.ptr2.p, sizeof(int32_t) * (m + 1), cudaMemcpyDeviceToHost, s));

@@ -147,8 +147,14 @@ template <class T>
 struct StoreEpi {  // out = s (mul! with alpha = true, beta = false)
     T* out;
     using Acc = NoAcc;
+    struct Pre {};
+    static constexpr int NPRE = 0;
+    static constexpr int pre_esz(int) { return (int)sizeof(T); }
+    __device__ const void* pre_src(int) const { return nullptr; }
+    __device__ Pre pre_global(int) const { return Pre{}; }
+    __device__ Pre pre_staged(const Staged<NPRE>&, int) const { return Pre{}; }
     __device__ void init(Acc&) {}
-    __device__ void row(int, int r, T s, Acc&) { out[r] = s; }
+    __device__ void row(int, int r, T s, const Pre&, Acc&) { out[r] = s; }
     __device__ void row_long(int, int r, T s, int, Acc&) { out[r] = s; }
     __device__ void finish(Acc&) {}
 };
@@ -166,16 +172,30 @@ struct PrimalEpi {
     const StepCoef<T>* __restrict__ coef;
     int avg;
     using Acc = NoAcc;
-    __device__ void init(Acc&) {}
-    __device__ __forceinline__ void row(int, int j, T s, Acc&) {
-        const T tau = coef->tau;
-        const T xj = x[j];
-        const T xp = proj_box(sub_rn(xj, mul_rn(tau, sub_rn(c[j], s))), lv[j], uv[j]);
-        xn[j] = xp;
-        xbar[j] = sub_rn(mul_rn(T(2), xp), xj);
-        if (avg) xa_new[j] = add_rn(mul_rn(xp, coef->a), mul_rn(xa_old[j], coef->b));
+    struct Pre { T x, c, lv, uv, xa; };
+    static constexpr int NPRE = 5;
+    static constexpr int pre_esz(int) { return (int)sizeof(T); }
+    __device__ const void* pre_src(int k) const {
+        return k == 0 ? (const void*)x : k == 1 ? (const void*)c : k == 2 ? (const void*)lv
+             : k == 3 ? (const void*)uv : (avg ? (const void*)xa_old : nullptr);
     }
-    __device__ void row_long(int p, int j, T s, int, Acc& a) { row(p, j, s, a); }
+    __device__ __forceinline__ Pre pre_global(int j) const {
+        return Pre{ld_stream(x + j), ld_stream(c + j), ld_stream(lv + j), ld_stream(uv + j),
+                   avg ? ld_stream(xa_old + j) : T(0)};
+    }
+    __device__ __forceinline__ Pre pre_staged(const Staged<NPRE>& st, int j) const {
+        return Pre{st.template get<T>(0, j), st.template get<T>(1, j), st.template get<T>(2, j), st.template get<T>(3, j),
+                   avg ? st.template get<T>(4, j) : T(0)};
+    }
+    __device__ void init(Acc&) {}
+    __device__ __forceinline__ void row(int, int j, T s, const Pre& q, Acc&) {
+        const T tau = coef->tau;
+        const T xp = proj_box(sub_rn(q.x, mul_rn(tau, sub_rn(q.c, s))), q.lv, q.uv);
+        __stcs(xn + j, xp);
+        xbar[j] = sub_rn(mul_rn(T(2), xp), q.x);
+        if (avg) __stcs(xa_new + j, add_rn(mul_rn(xp, coef->a), mul_rn(q.xa, coef->b)));
+    }
+    __device__ void row_long(int p, int j, T s, int, Acc& a) { row(p, j, s, pre_global(j), a); }
     __device__ void finish(Acc&) {}
 };
 
@@ -190,18 +210,31 @@ struct DualEpi {
     const StepCoef<T>* __restrict__ coef;
     int avg;
     using Acc = NoAcc;
+    struct Pre { T y, lc, uc, ya; };
+    static constexpr int NPRE = 4;
+    static constexpr int pre_esz(int) { return (int)sizeof(T); }
+    __device__ const void* pre_src(int k) const {
+        return k == 0 ? (const void*)y : k == 1 ? (const void*)lc : k == 2 ? (const void*)uc
+             : (avg ? (const void*)ya_old : nullptr);
+    }
+    __device__ __forceinline__ Pre pre_global(int i) const {
+        return Pre{ld_stream(y + i), ld_stream(lc + i), ld_stream(uc + i),
+                   avg ? ld_stream(ya_old + i) : T(0)};
+    }
+    __device__ __forceinline__ Pre pre_staged(const Staged<NPRE>& st, int i) const {
+        return Pre{st.template get<T>(0, i), st.template get<T>(1, i), st.template get<T>(2, i), avg ? st.template get<T>(3, i) : T(0)};
+    }
     __device__ void init(Acc&) {}
-    __device__ __forceinline__ void row(int, int i, T s, Acc&) {
+    __device__ __forceinline__ void row(int, int i, T s, const Pre& q, Acc&) {
         const T sigma = coef->sigma;
-        const T yi = y[i];
-        const T t2 = sub_rn(yi, mul_rn(sigma, s));
-        const T t4 = sub_rn(mul_rn(coef->inv_sigma, yi), s);
-        const T pr = proj_box(t4, -uc[i], -lc[i]);
+        const T t2 = sub_rn(q.y, mul_rn(sigma, s));
+        const T t4 = sub_rn(mul_rn(coef->inv_sigma, q.y), s);
+        const T pr = proj_box(t4, -q.uc, -q.lc);
         const T yp = sub_rn(t2, mul_rn(sigma, pr));
         yn[i] = yp;
-        if (avg) ya_new[i] = add_rn(mul_rn(yp, coef->a), mul_rn(ya_old[i], coef->b));
+        if (avg) __stcs(ya_new + i, add_rn(mul_rn(yp, coef->a), mul_rn(q.ya, coef->b)));
     }
-    __device__ void row_long(int p, int i, T s, int, Acc& a) { row(p, i, s, a); }
+    __device__ void row_long(int p, int i, T s, int, Acc& a) { row(p, i, s, pre_global(i), a); }
     __device__ void finish(Acc&) {}
 };
 
@@ -215,26 +248,51 @@ struct KktRowEpi {
     double* block_out;
     double* long_out;
     struct Acc { double v[2 * NV]; };
+    struct Pre { double l, u, d; double yy[NV]; };
+    static constexpr int NPRE = 3 + NV;
+    static constexpr int pre_esz(int k) { return k == 2 ? 8 : (int)sizeof(T); }
+    __device__ const void* pre_src(int k) const {
+        return k == 0 ? (const void*)lc : k == 1 ? (const void*)uc : k == 2 ? (const void*)invD1
+                                                                           : (const void*)y[k - 3];
+    }
     __device__ void init(Acc& a) {
 #pragma unroll
         for (int q = 0; q < 2 * NV; q++) a.v[q] = 0.0;
     }
-    __device__ __forceinline__ void terms(int p, int i, T s, double& pr2, double& pc) const {
-        const double sd = (double)s, l = (double)lc[i], u = (double)uc[i];
-        const double d = __dmul_rn(invD1[i], __dsub_rn(sd, proj_box(sd, l, u)));
-        pr2 = __dmul_rn(d, d);
-        const double yy = (double)y[p][i];
-        pc = __dsub_rn(safeprod_left(u, pos_part(-yy)), safeprod_left(l, neg_part(-yy)));
+    __device__ __forceinline__ Pre pre_global(int i) const {
+        Pre p;
+        p.l = (double)ld_stream(lc + i);
+        p.u = (double)ld_stream(uc + i);
+        p.d = ld_stream(invD1 + i);
+#pragma unroll
+        for (int k = 0; k < NV; k++) p.yy[k] = (double)ld_stream(y[k] + i);
+        return p;
     }
-    __device__ __forceinline__ void row(int p, int i, T s, Acc& a) {
+    __device__ __forceinline__ Pre pre_staged(const Staged<NPRE>& st, int i) const {
+        Pre p;
+        p.l = (double)st.template get<T>(0, i);
+        p.u = (double)st.template get<T>(1, i);
+        p.d = st.template get<double>(2, i);
+#pragma unroll
+        for (int k = 0; k < NV; k++) p.yy[k] = (double)st.template get<T>(3 + k, i);
+        return p;
+    }
+    __device__ __forceinline__ void terms(int p, T s, const Pre& q, double& pr2, double& pc) const {
+        const double sd = (double)s;
+        const double d = __dmul_rn(q.d, __dsub_rn(sd, proj_box(sd, q.l, q.u)));
+        pr2 = __dmul_rn(d, d);
+        const double yy = q.yy[p];
+        pc = __dsub_rn(safeprod_left(q.u, pos_part(-yy)), safeprod_left(q.l, neg_part(-yy)));
+    }
+    __device__ __forceinline__ void row(int p, int, T s, const Pre& q, Acc& a) {
         double pr2, pc;
-        terms(p, i, s, pr2, pc);
+        terms(p, s, q, pr2, pc);
         a.v[2 * p] += pr2;
         a.v[2 * p + 1] += pc;
     }
     __device__ void row_long(int p, int i, T s, int lid, Acc&) {
         double pr2, pc;
-        terms(p, i, s, pr2, pc);
+        terms(p, s, pre_global(i), pr2, pc);
         long_out[(size_t)lid * 2 * NV + 2 * p] = pr2;
         long_out[(size_t)lid * 2 * NV + 2 * p + 1] = pc;
     }
@@ -252,30 +310,56 @@ struct KktColEpi {
     double* block_out;
     double* long_out;
     struct Acc { double v[3 * NV]; };
+    struct Pre { double c, l, u, d; double xx[NV]; };
+    static constexpr int NPRE = 4 + NV;
+    static constexpr int pre_esz(int k) { return k == 3 ? 8 : (int)sizeof(T); }
+    __device__ const void* pre_src(int k) const {
+        return k == 0 ? (const void*)c : k == 1 ? (const void*)lv : k == 2 ? (const void*)uv
+             : k == 3 ? (const void*)invD2 : (const void*)x[k - 4];
+    }
     __device__ void init(Acc& a) {
 #pragma unroll
         for (int q = 0; q < 3 * NV; q++) a.v[q] = 0.0;
     }
-    __device__ __forceinline__ void terms(int p, int j, T s, double& du2, double& pv,
-                                          double& cx) const {
-        const double cj = (double)c[j], l = (double)lv[j], u = (double)uv[j];
-        const double g = __dsub_rn(cj, (double)s);
-        const double r = proj_multiplier(g, l, u);
-        const double d = __dmul_rn(invD2[j], __dsub_rn(g, r));
-        du2 = __dmul_rn(d, d);
-        pv = __dsub_rn(safeprod_left(u, pos_part(-r)), safeprod_left(l, neg_part(-r)));
-        cx = __dmul_rn(cj, (double)x[p][j]);
+    __device__ __forceinline__ Pre pre_global(int j) const {
+        Pre p;
+        p.c = (double)ld_stream(c + j);
+        p.l = (double)ld_stream(lv + j);
+        p.u = (double)ld_stream(uv + j);
+        p.d = ld_stream(invD2 + j);
+#pragma unroll
+        for (int k = 0; k < NV; k++) p.xx[k] = (double)ld_stream(x[k] + j);
+        return p;
     }
-    __device__ __forceinline__ void row(int p, int j, T s, Acc& a) {
+    __device__ __forceinline__ Pre pre_staged(const Staged<NPRE>& st, int j) const {
+        Pre p;
+        p.c = (double)st.template get<T>(0, j);
+        p.l = (double)st.template get<T>(1, j);
+        p.u = (double)st.template get<T>(2, j);
+        p.d = st.template get<double>(3, j);
+#pragma unroll
+        for (int k = 0; k < NV; k++) p.xx[k] = (double)st.template get<T>(4 + k, j);
+        return p;
+    }
+    __device__ __forceinline__ void terms(int p, T s, const Pre& q, double& du2, double& pv,
+                                          double& cx) const {
+        const double g = __dsub_rn(q.c, (double)s);
+        const double r = proj_multiplier(g, q.l, q.u);
+        const double d = __dmul_rn(q.d, __dsub_rn(g, r));
+        du2 = __dmul_rn(d, d);
+        pv = __dsub_rn(safeprod_left(q.u, pos_part(-r)), safeprod_left(q.l, neg_part(-r)));
+        cx = __dmul_rn(q.c, q.xx[p]);
+    }
+    __device__ __forceinline__ void row(int p, int, T s, const Pre& q, Acc& a) {
         double du2, pv, cx;
-        terms(p, j, s, du2, pv, cx);
+        terms(p, s, q, du2, pv, cx);
         a.v[3 * p] += du2;
         a.v[3 * p + 1] += pv;
         a.v[3 * p + 2] += cx;
     }
     __device__ void row_long(int p, int j, T s, int lid, Acc&) {
         double du2, pv, cx;
-        terms(p, j, s, du2, pv, cx);
+        terms(p, s, pre_global(j), du2, pv, cx);
         double* o = long_out + (size_t)lid * 3 * NV + 3 * p;
         o[0] = du2;
         o[1] = pv;
@@ -292,10 +376,16 @@ struct PowerEpi {
     double* block_out;
     double* long_out;
     struct Acc { double v[2]; };
+    struct Pre { T x; };
+    static constexpr int NPRE = 1;
+    static constexpr int pre_esz(int) { return (int)sizeof(T); }
+    __device__ const void* pre_src(int) const { return x; }
+    __device__ Pre pre_global(int j) const { return Pre{ld_stream(x + j)}; }
+    __device__ Pre pre_staged(const Staged<NPRE>& st, int j) const { return Pre{st.template get<T>(0, j)}; }
     __device__ void init(Acc& a) { a.v[0] = a.v[1] = 0.0; }
-    __device__ __forceinline__ void row(int, int j, T s, Acc& a) {
+    __device__ __forceinline__ void row(int, int j, T s, const Pre& q, Acc& a) {
         out[j] = s;
-        a.v[0] += (double)x[j] * (double)s;
+        a.v[0] += (double)q.x * (double)s;
         a.v[1] += (double)s * (double)s;
     }
     __device__ void row_long(int, int j, T s, int lid, Acc&) {
@@ -479,8 +569,10 @@ ProblemBase* make_problem(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm
         k_invert_perm<<<gz, 256, 0, s>>>(S.p21.p, p12.p, nnz);
         CK_LAUNCH();
     }
-    P->a_val.alloc(zn);
-    P->at_val.alloc(zn);
+    P->a_val.alloc(zn + PAD_ELEMS);
+    P->at_val.alloc(zn + PAD_ELEMS);
+    CK(cudaMemsetAsync(P->a_val.p, 0, sizeof(T) * (zn + PAD_ELEMS), s));
+    CK(cudaMemsetAsync(P->at_val.p, 0, sizeof(T) * (zn + PAD_ELEMS), s));
     gather_values<T, double>(tA.p, S.p21.p, P->a_val.p, nnz, s);
     gather_values<T, double>(tAt.p, p12.p, P->at_val.p, nnz, s);
     P->a_ptr = std::move(S.ptr2);
@@ -720,6 +812,7 @@ struct StateT : StateBase {
         }
         while (count-- > 0) run_single();
         CK(cudaStreamSynchronize(h->stream));
+        check_tile_error(h->stream);
     }
 
     // KKT errors of NV (x, y) pairs in one pass (errors.jl:65-109)
@@ -750,6 +843,7 @@ struct StateT : StateBase {
         double* pin = h->pinned_area(sizeof(double) * 64);
         CK(cudaMemcpyAsync(pin, P.red_out.p, sizeof(double) * 5 * NV, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
+        check_tile_error(s);
         for (int p = 0; p < NV; p++) {
             const double pr2 = pin[2 * p], pc = pin[2 * p + 1];
             const double du2 = pin[2 * NV + 3 * p], pv = pin[2 * NV + 3 * p + 1],

@@ -306,7 +306,9 @@ void build_csc_pair(Handle& h, int64_t m, int64_t n, int64_t nnz, const int64_t*
     if (hflags & BAD_MONO) fail(CPDLP_ERR_ARGUMENT, "invalid CSC: colptr is not monotone");
     if (hflags & BAD_END) fail(CPDLP_ERR_DIMENSION, "invalid CSC: colptr[n+1] != nnz + 1");
     size_t zn = (size_t)(nnz > 0 ? nnz : 1);
-    out.idx1.alloc(zn);
+    // index arrays carry 16 padding elements for the tile engine's aligned loads
+    out.idx1.alloc(zn + 16);
+    CK(cudaMemsetAsync(out.idx1.p, 0, sizeof(int32_t) * (zn + 16), s));
     out.col1.alloc(zn);
     if (nnz > 0) {
         k_check_rows<<<grid_for(nnz, 256), 256, 0, s>>>(rv.p, out.ptr1.p, m, n, nnz, out.idx1.p,
@@ -320,7 +322,8 @@ void build_csc_pair(Handle& h, int64_t m, int64_t n, int64_t nnz, const int64_t*
     }
     // transpose: stable sort of the entries by row
     out.ptr2.alloc((size_t)m + 1);
-    out.idx2.alloc(zn);
+    out.idx2.alloc(zn + 16);
+    CK(cudaMemsetAsync(out.idx2.p, 0, sizeof(int32_t) * (zn + 16), s));
     out.row2.alloc(zn);
     out.p21.alloc(zn);
     DBuf<int32_t> cnt((size_t)(m > 0 ? m : 1));

@@ -30,19 +30,20 @@ void build_tile_plan(const std::vector<int32_t>& ptr, int32_t rows, int items, T
     int32_t r = 0;
     while (r < rows) {
         int32_t len = ptr[r + 1] - ptr[r];
-        if (len > tile) {
+        if (len > LONG_ROW) {
+            // warp path: one piece per TILE nonzeros; only multi-piece rows use slots
             int32_t lid = (int32_t)plan.long_rows.size();
             int32_t np = (len + tile - 1) / tile;
             for (int32_t p = 0; p < np; p++) longs.push_back(make_int4(r, p, lid, slot));
             plan.long_rows.push_back(r);
-            slot += np;
+            if (np > 1) slot += np;
             r++;
             continue;
         }
         int32_t r0 = r, nz = 0;
         while (r < rows && r - r0 < MAX_TILE_ROWS) {
             int32_t l = ptr[r + 1] - ptr[r];
-            if (l > tile || nz + l > tile) break;
+            if (l > LONG_ROW || nz + l > tile) break;
             nz += l;
             r++;
         }
@@ -64,6 +65,31 @@ void build_tile_plan(const std::vector<int32_t>& ptr, int32_t rows, int items, T
     plan.counters.alloc(plan.nlong ? (size_t)plan.nlong : 1);
     CK(cudaMemsetAsync(plan.counters.p, 0, sizeof(int32_t) * plan.counters.n, s));
     CK(cudaStreamSynchronize(s));
+}
+
+namespace {
+__device__ int g_tile_error = 0;
+}  // namespace
+
+int* tile_error_word() {
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    static int* addr[64] = {nullptr};
+    if (dev < 0 || dev >= 64) fail(CPDLP_ERR_UNSUPPORTED, "device ordinal above 63");
+    if (!addr[dev]) CK(cudaGetSymbolAddress((void**)&addr[dev], g_tile_error));
+    return addr[dev];
+}
+
+void check_tile_error(cudaStream_t s) {
+    int* w = tile_error_word();
+    int h = 0;
+    CK(cudaMemcpyAsync(&h, w, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (h) {
+        CK(cudaMemsetAsync(w, 0, sizeof(int), s));
+        CK(cudaStreamSynchronize(s));
+        fail(CPDLP_ERR_TIMEOUT, "a tile kernel timed out waiting for its staged data");
+    }
 }
 
 namespace {

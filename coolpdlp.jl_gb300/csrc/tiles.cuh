@@ -1,27 +1,36 @@
 // tiles.cuh -- the warp-tile CSR SpMV engine with fused per-row epilogues.
 //
 // Work partition (built once per matrix on the host from its row pointer):
-//  * short tile  {r0, r1, -1, 0}: consecutive rows [r0, r1) holding at most
-//    TILE = 32*ITEMS nonzeros and at most MAX_TILE_ROWS rows.  One warp loads
-//    the tile's values and column indices coalesced into registers, writes
-//    value*x[col] products to shared memory and then every lane reduces whole
-//    rows in ascending column order (the reference's order) and applies the
-//    epilogue of that row.
-//  * long-row piece {row, piece, long_id, slot_base}: a row longer than TILE is
-//    cut into TILE-sized pieces, one warp each.  Each warp writes its partial
-//    sum to a scratch slot; the warp that completes the row (atomic counter,
-//    no waiting) adds the partials in piece order and applies the epilogue, so
-//    results do not depend on scheduling.
-// All arithmetic of the row sums uses explicit round-to-nearest multiply/add
-// (no FMA contraction); short rows therefore reproduce a sequential CPU sum
-// exactly.
+//  * short tile {r0, r1, -1, 0}: consecutive rows [r0, r1), each at most
+//    LONG_ROW nonzeros, together at most TILE = 32*ITEMS nonzeros and at most
+//    MAX_TILE_ROWS rows.  One warp
+//      1. prefetches the row pointers and the epilogue inputs of its rows,
+//      2. loads the tile's values and column indices with 128-bit loads
+//         (window aligned down to 4 elements), all issued before any use,
+//      3. gathers x[col] for the whole tile in one batch,
+//      4. writes value*x products to shared memory, and
+//      5. lets every lane reduce whole rows in ascending column order (the
+//         reference's order) and apply the fused epilogue.
+//  * long-row piece {row, piece, long_id, slot_base}: a row longer than
+//    LONG_ROW is cut into TILE-sized pieces, one warp each, reduced with warp
+//    shuffles.  A row of several pieces writes each partial to a scratch slot;
+//    the warp that completes the row (atomic counter, no waiting) adds the
+//    partials in piece order and applies the epilogue, so results do not
+//    depend on scheduling.
+// Row sums use explicit round-to-nearest multiply/add (no FMA contraction), so
+// rows of at most LONG_ROW nonzeros reproduce a sequential CPU sum exactly.
+// Index and value arrays must be allocated with PAD_ELEMS extra elements:
+// the aligned 128-bit window may read up to 3 elements past the last row.
 #pragma once
 
 #include "cpdlp_common.cuh"
 
 namespace cpdlp {
 
-constexpr int MAX_TILE_ROWS = 256;
+constexpr int MAX_TILE_ROWS = 128;
+constexpr int ROWS_PER_LANE = MAX_TILE_ROWS / 32;
+constexpr int LONG_ROW = 64;
+constexpr int PAD_ELEMS = 16;
 constexpr unsigned FULL_MASK = 0xffffffffu;
 
 struct TilePlan {
@@ -29,7 +38,7 @@ struct TilePlan {
     int32_t items = 16;     // nonzeros per lane of a short tile
     int32_t ntasks = 0;
     int32_t nshort = 0;
-    int32_t nlong = 0;      // rows longer than a tile
+    int32_t nlong = 0;      // rows that take the warp path
     int32_t npieces = 0;    // pieces of all long rows
     DBuf<int4> tasks;
     DBuf<int32_t> counters; // per long row, zero between launches
@@ -41,7 +50,7 @@ struct TilePlan {
 void build_tile_plan(const std::vector<int32_t>& ptr, int32_t rows, int items, TilePlan& plan,
                      cudaStream_t s);
 
-// Picks nonzeros-per-lane from the mean row length (autotuner default).
+// Picks nonzeros-per-lane from the size and mean row length (autotuner default).
 int choose_items(int64_t nnz, int64_t rows, int requested_tile_nnz);
 
 template <class V, class T>
@@ -60,16 +69,59 @@ struct VecSet {
     const T* v[NVEC];
 };
 
+// ---- 4-element chunk loads (the chunk start is a multiple of 4 elements) ----
+// Streaming (evict-first) loads written as volatile PTX: they keep their
+// program order, so a batch of them is issued back to back before the first
+// result is consumed.  The matrix is read once per pass; evict-first keeps
+// the gathered vectors resident in L2.
+__device__ __forceinline__ void load4(const int32_t* p, int (&o)[4]) {
+    asm volatile("ld.global.cs.v4.s32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(o[0]), "=r"(o[1]), "=r"(o[2]), "=r"(o[3])
+                 : "l"(p));
+}
+template <class T>
+__device__ __forceinline__ void load4v(const float* p, T (&o)[4]) {
+    float a, b, c, d;
+    asm volatile("ld.global.cs.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(a), "=f"(b), "=f"(c), "=f"(d)
+                 : "l"(p));
+    o[0] = (T)a; o[1] = (T)b; o[2] = (T)c; o[3] = (T)d;
+}
+template <class T>
+__device__ __forceinline__ void load4v(const double* p, T (&o)[4]) {
+    double a, b, c, d;
+    asm volatile("ld.global.cs.v2.f64 {%0, %1}, [%2];" : "=d"(a), "=d"(b) : "l"(p));
+    asm volatile("ld.global.cs.v2.f64 {%0, %1}, [%2];" : "=d"(c), "=d"(d) : "l"(p + 2));
+    o[0] = (T)a; o[1] = (T)b; o[2] = (T)c; o[3] = (T)d;
+}
+template <class T>
+__device__ __forceinline__ void load4v(const int8_t* p, T (&o)[4]) {
+    int v;
+    asm volatile("ld.global.cs.s32 %0, [%1];" : "=r"(v) : "l"(p));
+    o[0] = (T)(int8_t)(v & 0xff); o[1] = (T)(int8_t)((v >> 8) & 0xff);
+    o[2] = (T)(int8_t)((v >> 16) & 0xff); o[3] = (T)(int8_t)((v >> 24) & 0xff);
+}
+// read-only gather through the texture/L1 path, same ordering property
+__device__ __forceinline__ float gather(const float* p) {
+    float v;
+    asm volatile("ld.global.nc.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ double gather(const double* p) {
+    double v;
+    asm volatile("ld.global.nc.f64 %0, [%1];" : "=d"(v) : "l"(p));
+    return v;
+}
 template <class V, class T>
-__device__ __forceinline__ T load_val(const V* p) {
+__device__ __forceinline__ T load1v(const V* p) {
     return (T)__ldcs(p);
 }
 template <>
-__device__ __forceinline__ float load_val<int8_t, float>(const int8_t* p) {
+__device__ __forceinline__ float load1v<int8_t, float>(const int8_t* p) {
     return (float)__ldcs(reinterpret_cast<const signed char*>(p));
 }
 template <>
-__device__ __forceinline__ double load_val<int8_t, double>(const int8_t* p) {
+__device__ __forceinline__ double load1v<int8_t, double>(const int8_t* p) {
     return (double)__ldcs(reinterpret_cast<const signed char*>(p));
 }
 
@@ -80,85 +132,193 @@ __device__ __forceinline__ T warp_sum_tree(T v) {
     return v;
 }
 
-// One warp processes one task.  `prod` is this warp's shared-memory slice of
-// 32*ITEMS products, reused for each of the NVEC input vectors.
+// ---- TMA bulk copies and mbarriers (PTX) -------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* m, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(m)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* m, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(m)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* m, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(m)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// 1-D bulk copy global -> shared (TMA engine), completion counted on `m`.
+// src, dst and bytes must be multiples of 16.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* m) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(m))
+        : "memory");
+}
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Waits for phase `parity` of `m` for at most ~1 s (wall clock on the GPU) and
+// at most 2^30 polls; returns false on timeout.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* m, uint32_t parity) {
+    if (mbar_try_wait(m, parity)) return true;
+    const uint64_t t0 = global_ns();
+    for (uint32_t it = 0; it < (1u << 30); it++) {
+        if (mbar_try_wait(m, parity)) return true;
+        if ((it & 255u) == 0 && global_ns() - t0 > 1000000000ull) break;
+    }
+    return false;
+}
+
+// Epilogue interface (per row r, per input vector p):
+//   static constexpr int NPRE;               number of per-row input vectors
+//   const void* pre_src(int k) const;       global base of input k (nullptr: skip)
+//   static constexpr int pre_esz(int k);    its element size (4 or 8 bytes)
+//   struct Pre;                              the inputs of one row
+//   Pre pre_global(int r) const;            read from global memory
+//   Pre pre_staged(Staged<NPRE>, int r);    read from the staged shared copy
+//   void row(int p, int r, T s, const Pre&, Acc&)   short-tile rows
+//   void row_long(int p, int r, T s, int lid, Acc&)  long rows (one lane)
+//   void init(Acc&); void finish(Acc&);             block reductions
+template <int NPRE>
+struct Staged {
+    const unsigned char* base[NPRE > 0 ? NPRE : 1];
+    int first[NPRE > 0 ? NPRE : 1];
+    template <class E>
+    __device__ __forceinline__ E get(int k, int r) const {
+        return reinterpret_cast<const E*>(base[k])[r - first[k]];
+    }
+};
+
+// One warp, one short tile.  All loads of a phase are volatile PTX issued back
+// to back, so they are in flight together: (1) row pointers and the epilogue
+// inputs of this lane's rows, (2) the tile's indices and values with 128-bit
+// loads over the 4-element-aligned window, (3) the gathers.
 template <int ITEMS, int NVEC, class V, class T, class Epi>
-__device__ __forceinline__ void tile_task(const CsrView<V, T>& A, const VecSet<T, NVEC>& xs,
-                                          Epi& epi, typename Epi::Acc& acc, int task, int lane,
-                                          T* prod) {
-    constexpr int TILE = 32 * ITEMS;
-    const int4 t = A.tasks[task];
-    if (t.z < 0) {
-        const int r0 = t.x, r1 = t.y;
-        const int nz0 = __ldg(&A.ptr[r0]);
-        const int len = __ldg(&A.ptr[r1]) - nz0;
-        T v[ITEMS];
-        int c[ITEMS];
+__device__ __forceinline__ void short_tile(const CsrView<V, T>& A, const VecSet<T, NVEC>& xs,
+                                           Epi& epi, typename Epi::Acc& acc, int r0, int r1,
+                                           int lane, T* prod) {
+    constexpr int NV4 = ITEMS / 4 + 1;  // 4-element chunks per lane (+1: alignment slack)
+    const int nz0 = ld_keep(A.ptr + r0);
+    const int nz1 = ld_keep(A.ptr + r1);
+    const int base = nz0 & ~3;
+    int ra[ROWS_PER_LANE], rb[ROWS_PER_LANE];
+    typename Epi::Pre pre[ROWS_PER_LANE];
 #pragma unroll
-        for (int i = 0; i < ITEMS; i++) {
-            const int e = lane + 32 * i;
-            if (e < len) {
-                v[i] = load_val<V, T>(A.val + nz0 + e);
-                c[i] = __ldcs(A.idx + nz0 + e);
-            } else {
-                v[i] = T(0);
-                c[i] = 0;
-            }
+    for (int k = 0; k < ROWS_PER_LANE; k++) {
+        const int r = r0 + lane + 32 * k;
+        if (r < r1) {
+            ra[k] = ld_keep(A.ptr + r);
+            rb[k] = ld_keep(A.ptr + r + 1);
+            pre[k] = epi.pre_global(r);
+        } else {
+            ra[k] = rb[k] = 0;
+        }
+    }
+    int cc[NV4][4];
+    T vv[NV4][4];
+#pragma unroll
+    for (int j = 0; j < NV4; j++) {
+        const int e = base + 4 * (lane + 32 * j);
+        if (e < nz1) {
+            load4(A.idx + e, cc[j]);
+            load4v<T>(A.val + e, vv[j]);
+        } else {
+#pragma unroll
+            for (int q = 0; q < 4; q++) { cc[j][q] = 0; vv[j][q] = T(0); }
+        }
+    }
+#pragma unroll
+    for (int p = 0; p < NVEC; p++) {
+        T xg[NV4][4];
+#pragma unroll
+        for (int j = 0; j < NV4; j++) {
+            const int e = base + 4 * (lane + 32 * j);
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                xg[j][q] = (e + q >= nz0 && e + q < nz1) ? gather(xs.v[p] + cc[j][q]) : T(0);
         }
 #pragma unroll
-        for (int p = 0; p < NVEC; p++) {
+        for (int j = 0; j < NV4; j++) {
+            const int e = base + 4 * (lane + 32 * j);
 #pragma unroll
-            for (int i = 0; i < ITEMS; i++) {
-                const int e = lane + 32 * i;
-                if (e < len) prod[e] = mul_rn(v[i], __ldg(xs.v[p] + c[i]));
-            }
-            __syncwarp();
-            for (int r = r0 + lane; r < r1; r += 32) {
-                const int a = __ldg(&A.ptr[r]) - nz0, b = __ldg(&A.ptr[r + 1]) - nz0;
+            for (int q = 0; q < 4; q++)
+                if (e + q >= nz0 && e + q < nz1) prod[e + q - nz0] = mul_rn(vv[j][q], xg[j][q]);
+        }
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < ROWS_PER_LANE; k++) {
+            const int r = r0 + lane + 32 * k;
+            if (r < r1) {
                 T s = T(0);
-                for (int k = a; k < b; k++) s = add_rn(s, prod[k]);
-                epi.row(p, r, s, acc);
+                for (int i = ra[k] - nz0; i < rb[k] - nz0; i++) s = add_rn(s, prod[i]);
+                epi.row(p, r, s, pre[k], acc);
             }
-            __syncwarp();
         }
-        (void)TILE;
-    } else {
-        const int row = t.x, piece = t.y, lid = t.z, base = t.w;
-        const int rb = __ldg(&A.ptr[row]), re = __ldg(&A.ptr[row + 1]);
-        const int npieces = (re - rb + TILE - 1) / TILE;
-        const int a = rb + piece * TILE;
-        const int b = min(a + TILE, re);
-        T s[NVEC];
+        __syncwarp();
+    }
+}
+
+template <int ITEMS, int NVEC, class V, class T, class Epi>
+__device__ __forceinline__ void long_piece(const CsrView<V, T>& A, const VecSet<T, NVEC>& xs,
+                                           Epi& epi, typename Epi::Acc& acc, int4 t, int lane) {
+    constexpr int TILE = 32 * ITEMS;
+    const int row = t.x, piece = t.y, lid = t.z, base_slot = t.w;
+    const int rb = ld_keep(A.ptr + row), re = ld_keep(A.ptr + row + 1);
+    const int npieces = (re - rb + TILE - 1) / TILE;
+    const int a = rb + piece * TILE;
+    const int b = min(a + TILE, re);
+    T s[NVEC];
 #pragma unroll
-        for (int p = 0; p < NVEC; p++) s[p] = T(0);
-        for (int e = a + lane; e < b; e += 32) {
-            const T vv = load_val<V, T>(A.val + e);
-            const int cc = __ldcs(A.idx + e);
+    for (int p = 0; p < NVEC; p++) s[p] = T(0);
+    for (int e = a + lane; e < b; e += 32) {
+        const T vv = load1v<V, T>(A.val + e);
+        const int cc = __ldcs(A.idx + e);
 #pragma unroll
-            for (int p = 0; p < NVEC; p++) s[p] = add_rn(s[p], mul_rn(vv, __ldg(xs.v[p] + cc)));
-        }
+        for (int p = 0; p < NVEC; p++) s[p] = add_rn(s[p], mul_rn(vv, __ldg(xs.v[p] + cc)));
+    }
 #pragma unroll
-        for (int p = 0; p < NVEC; p++) s[p] = warp_sum_tree(s[p]);
-        int done = 0;
+    for (int p = 0; p < NVEC; p++) s[p] = warp_sum_tree(s[p]);
+    if (npieces == 1) {
         if (lane == 0) {
 #pragma unroll
-            for (int p = 0; p < NVEC; p++) A.partials[(size_t)(base + piece) * NVEC + p] = s[p];
-            __threadfence();
-            done = atomicAdd(&A.counters[lid], 1);
+            for (int p = 0; p < NVEC; p++) epi.row_long(p, row, s[p], lid, acc);
         }
-        done = __shfl_sync(FULL_MASK, done, 0);
-        if (done == npieces - 1) {
-            __threadfence();
-            if (lane == 0) {
+        return;
+    }
+    int done = 0;
+    if (lane == 0) {
 #pragma unroll
-                for (int p = 0; p < NVEC; p++) {
-                    T tot = T(0);
-                    for (int q = 0; q < npieces; q++)
-                        tot = add_rn(tot, __ldcg(A.partials + (size_t)(base + q) * NVEC + p));
-                    epi.row_long(p, row, tot, lid, acc);
-                }
-                A.counters[lid] = 0;
+        for (int p = 0; p < NVEC; p++) A.partials[(size_t)(base_slot + piece) * NVEC + p] = s[p];
+        __threadfence();
+        done = atomicAdd(&A.counters[lid], 1);
+    }
+    done = __shfl_sync(FULL_MASK, done, 0);
+    if (done == npieces - 1) {
+        __threadfence();
+        if (lane == 0) {
+#pragma unroll
+            for (int p = 0; p < NVEC; p++) {
+                T tot = T(0);
+                for (int q = 0; q < npieces; q++)
+                    tot = add_rn(tot, __ldcg(A.partials + (size_t)(base_slot + q) * NVEC + p));
+                epi.row_long(p, row, tot, lid, acc);
             }
+            A.counters[lid] = 0;
         }
     }
 }
@@ -171,11 +331,21 @@ __global__ void __launch_bounds__(WARPS * 32)
     const int task = blockIdx.x * WARPS + w;
     typename Epi::Acc acc;
     epi.init(acc);
-    if (task < A.ntasks) tile_task<ITEMS, NVEC>(A, xs, epi, acc, task, lane, prod[w]);
+    if (task < A.ntasks) {
+        const int4 t = A.tasks[task];
+        if (t.z < 0) short_tile<ITEMS, NVEC>(A, xs, epi, acc, t.x, t.y, lane, prod[w]);
+        else long_piece<ITEMS, NVEC>(A, xs, epi, acc, t, lane);
+    }
     epi.finish(acc);
 }
 
 constexpr int TILE_WARPS = 8;
+
+// The device error word that bounded waits in this library report into.
+int* tile_error_word();
+// Reads (and clears) the error word on `s`; throws Error(CPDLP_ERR_TIMEOUT)
+// if a kernel gave up a bounded wait.
+void check_tile_error(cudaStream_t s);
 
 template <int NVEC, class V, class T, class Epi>
 void launch_tiles(const TilePlan& plan, const CsrView<V, T>& view, const VecSet<T, NVEC>& xs,
@@ -217,8 +387,7 @@ __device__ __forceinline__ void block_reduce_store(const double (&v)[Q], double*
     }
 }
 
-// Sums `nblocks` rows of Q partials (plus `nextra` extra rows) into out[Q], in
-// a fixed order: one block, thread-strided then tree.
+// Sums `nrows` rows of q partials into out[q] in a fixed order (one block).
 void reduce_partials(const double* partials, int64_t nrows, int q, double* out, cudaStream_t s);
 
 }  // namespace cpdlp

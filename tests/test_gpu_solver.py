@@ -23,12 +23,15 @@ def _native_problem(handle, lp, prm):
     return L, native.Problem(handle, L, prm)
 
 
-def _lps():
+def _lps(solvable_only: bool = False):
+    """Feasible, bounded LPs (solve parity) plus, for the scaling / step tests,
+    a random LP with random infinite bounds that PDLP does not solve."""
     from coolpdlp import generators as G
-    out = [G.random_sparse_lp(200, 400, 5, seed=3), G.random_sparse_lp(1000, 2000, 5, seed=0)]
-    lp, _, _ = G.random_milp_and_sol(60, 120, 0.1, seed=4)
-    out.append(lp)
-    out.append(G.multicommodity_flow_lp(side=8, K=3, seed=2))
+    out = [G.random_sparse_lp(200, 400, 5, seed=3), G.random_sparse_lp(1000, 2000, 5, seed=0),
+           G.multicommodity_flow_lp(side=8, K=3, seed=2)]
+    if not solvable_only:
+        lp, _, _ = G.random_milp_and_sol(60, 120, 0.1, seed=4)
+        out.append(lp)
     return out
 
 
@@ -65,7 +68,7 @@ def test_step_size_and_primal_weight(handle, oracle):
 @pytest.mark.parametrize("algorithm", [0, 1])
 def test_steps_match_oracle(handle, oracle, algorithm):
     from coolpdlp import native
-    for lp in _lps()[:3]:
+    for lp in (_lps()[0], _lps()[1], _lps()[3]):
         prm = oracle.params(algorithm)
         _, P = _native_problem(handle, lp, prm)
         st = native.State(P, prm)
@@ -96,7 +99,7 @@ def test_steps_match_oracle(handle, oracle, algorithm):
 @pytest.mark.parametrize("algorithm", [0, 1])
 def test_solve_matches_oracle_f64(handle, oracle, algorithm):
     import coolpdlp as cp
-    for lp in _lps():
+    for lp in _lps(solvable_only=True):
         kw = {} if algorithm == 0 else {"termination_reltol": 1e-3, "max_kkt_passes": 200000}
         prm = oracle.params(algorithm, **kw)
         xo, yo, so = oracle.solve(lp, prm)
