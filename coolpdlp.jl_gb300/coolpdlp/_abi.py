@@ -62,7 +62,7 @@ class ParamsC(Structure):
         ("power_seed", c_uint64),
         ("refine_reltol", c_double),
         ("tile_nnz", c_int32),
-        ("reserved0", c_int32),
+        ("tile_flags", c_int32),
     ]
 
 
@@ -119,7 +119,7 @@ def default_params_py(algorithm: int = ALGO_PDLP) -> ParamsC:
     p.power_seed = 0
     p.refine_reltol = 0.0
     p.tile_nnz = 0
-    p.reserved0 = 0
+    p.tile_flags = 0
     return p
 
 

@@ -100,7 +100,7 @@ class Algorithm:
                 "zero_tol", "sufficient_decay", "necessary_decay", "artificial_decay",
                 "show_progress", "check_every", "record_error_history", "termination_reltol",
                 "max_kkt_passes", "time_limit", "power_tol_override", "power_maxiter_override",
-                "power_seed", "refine_reltol", "tile_nnz")
+                "power_seed", "refine_reltol", "tile_nnz", "tile_flags")
 
     def __init__(self, name: str = "PDLP", T=np.float64, Ti=np.int64, M="CSR", *, device: int = 0,
                  backend=None, **kw):

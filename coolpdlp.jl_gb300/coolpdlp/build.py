@@ -40,7 +40,7 @@ def build_library(verbose: bool = False, force: bool = False, extra_flags=None) 
     sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     headers = glob.glob(os.path.join(CSRC, "*.cuh")) + [_abi.HEADER_PATH]
     hdr_time = _newest(headers)
-    flags = NVCC_FLAGS + list(extra_flags or [])
+    flags = NVCC_FLAGS + list(extra_flags or []) + os.environ.get("CPDLP_NVCC_EXTRA", "").split()
     exe = nvcc()
 
     def compile_one(src):

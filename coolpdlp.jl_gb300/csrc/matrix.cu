@@ -16,6 +16,7 @@ struct MulEpi {  // c[i] = alpha*s + beta*c[i]; beta == 0 does not read c (mat_c
     T alpha, beta;
     int use_beta;
     struct Acc {};
+    MulEpi shifted(unsigned) const { return *this; }
     struct Pre { T c; };
     static constexpr int NPRE = 1;
     static constexpr int pre_esz(int) { return (int)sizeof(T); }
@@ -174,7 +175,8 @@ void spmv_T(Handle& h, const Matrix& M, const T* b, T* c, double alpha, double b
     const DBuf<T>& vals = vals_of<T>(const_cast<Matrix&>(M));
     if (M.format == CPDLP_FMT_CSR) {
         CsrView<T, T> v{M.ptr.p, M.idx.p, vals.p, M.plan.tasks.p, M.plan.ntasks,
-                        M.plan.counters.p, reinterpret_cast<T*>(M.part.p)};
+                        M.plan.ltasks.p, M.plan.nltasks, M.plan.counters.p,
+                        reinterpret_cast<T*>(M.part.p)};
         MulEpi<T> e{c, a, bb, ub};
         launch_tiles<1>(M.plan, v, VecSet<T, 1>{{b}}, e, s);
     } else if (M.format == CPDLP_FMT_ELL) {

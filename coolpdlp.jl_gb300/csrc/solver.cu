@@ -39,27 +39,65 @@ constexpr int RED_THREADS = TILE_WARPS * 32;
 enum NormKind { NK_INF = 0, NK_ONE = 1, NK_TWO = 2, NK_ZERO = 3, NK_P = 4 };
 
 // d[r] = 1/sqrt(norm(row r)), 1 when the norm is zero (preconditioning.jl:102-111).
-// Sequential in storage order, like the reference's column_norm (linalg.jl:98-99).
+// One warp per 32 consecutive rows.  Rows of at most 64 entries are summed by
+// one lane sequentially in storage order, like the reference's column_norm
+// (linalg.jl:98-99) on short columns, so they match the oracle bit for bit;
+// longer rows are reduced by the whole warp (lane-strided partials, fixed
+// shuffle tree), as the reference's BLAS-backed norm also reorders long sums.
+__device__ __forceinline__ double norm_term(int kind, double x, double p) {
+    switch (kind) {
+        case NK_ONE: return fabs(x);
+        case NK_TWO: return __dmul_rn(x, x);
+        case NK_ZERO: return (x != 0.0) ? 1.0 : 0.0;
+        case NK_P: return pow(fabs(x), p);
+        default: return fabs(x);
+    }
+}
+__device__ __forceinline__ double norm_finish(int kind, double s, double p, bool nonempty) {
+    if (kind == NK_TWO) return sqrt(s);
+    if (kind == NK_P && nonempty) return pow(s, 1.0 / p);
+    return s;
+}
 __global__ void k_row_norm_scale(const int32_t* __restrict__ ptr, const double* __restrict__ v,
                                  int64_t rows, int kind, double p, double* __restrict__ d) {
-    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= rows) return;
-    const int a = ptr[r], b = ptr[r + 1];
-    double s = 0.0;
-    if (kind == NK_INF) {
-        for (int k = a; k < b; k++) s = jl_max(s, fabs(v[k]));
-    } else if (kind == NK_ONE) {
-        for (int k = a; k < b; k++) s = __dadd_rn(s, fabs(v[k]));
-    } else if (kind == NK_TWO) {
-        for (int k = a; k < b; k++) s = __dadd_rn(s, __dmul_rn(v[k], v[k]));
-        s = sqrt(s);
-    } else if (kind == NK_ZERO) {
-        for (int k = a; k < b; k++) s += (v[k] != 0.0) ? 1.0 : 0.0;
-    } else {
-        for (int k = a; k < b; k++) s = __dadd_rn(s, pow(fabs(v[k]), p));
-        if (b > a) s = pow(s, 1.0 / p);
+    const int lane = threadIdx.x & 31;
+    const int64_t r0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x - lane);
+    if (r0 >= rows) return;
+    const int64_t r = r0 + lane;
+    int a = 0, b = 0;
+    if (r < rows) {
+        a = ptr[r];
+        b = ptr[r + 1];
+        if (b - a <= 64) {
+            double s = 0.0;
+            for (int k = a; k < b; k++) {
+                const double t = norm_term(kind, v[k], p);
+                s = (kind == NK_INF) ? jl_max(s, t) : __dadd_rn(s, t);
+            }
+            s = norm_finish(kind, s, p, b > a);
+            d[r] = (s == 0.0) ? 1.0 : 1.0 / sqrt(s);
+        }
     }
-    d[r] = (s == 0.0) ? 1.0 : 1.0 / sqrt(s);
+    unsigned longs = __ballot_sync(0xffffffffu, r < rows && b - a > 64);
+    while (longs) {
+        const int l = __ffs(longs) - 1;
+        longs &= longs - 1;
+        const int la = __shfl_sync(0xffffffffu, a, l), lb = __shfl_sync(0xffffffffu, b, l);
+        double s = 0.0;
+        for (int k = la + lane; k < lb; k += 32) {
+            const double t = norm_term(kind, v[k], p);
+            s = (kind == NK_INF) ? jl_max(s, t) : __dadd_rn(s, t);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double t = __shfl_xor_sync(0xffffffffu, s, o);
+            s = (kind == NK_INF) ? jl_max(s, t) : __dadd_rn(s, t);
+        }
+        if (lane == 0) {
+            s = norm_finish(kind, s, p, true);
+            d[r0 + l] = (s == 0.0) ? 1.0 : 1.0 / sqrt(s);
+        }
+    }
 }
 
 // A_p = D1*A*D2 on A's CSC values (S1 order): (d1_i * a_ij) * d2_j
@@ -147,6 +185,7 @@ template <class T>
 struct StoreEpi {  // out = s (mul! with alpha = true, beta = false)
     T* out;
     using Acc = NoAcc;
+    StoreEpi shifted(unsigned) const { return *this; }
     struct Pre {};
     static constexpr int NPRE = 0;
     static constexpr int pre_esz(int) { return (int)sizeof(T); }
@@ -172,6 +211,7 @@ struct PrimalEpi {
     const StepCoef<T>* __restrict__ coef;
     int avg;
     using Acc = NoAcc;
+    PrimalEpi shifted(unsigned) const { return *this; }
     struct Pre { T x, c, lv, uv, xa; };
     static constexpr int NPRE = 5;
     static constexpr int pre_esz(int) { return (int)sizeof(T); }
@@ -210,6 +250,7 @@ struct DualEpi {
     const StepCoef<T>* __restrict__ coef;
     int avg;
     using Acc = NoAcc;
+    DualEpi shifted(unsigned) const { return *this; }
     struct Pre { T y, lc, uc, ya; };
     static constexpr int NPRE = 4;
     static constexpr int pre_esz(int) { return (int)sizeof(T); }
@@ -248,7 +289,14 @@ struct KktRowEpi {
     double* block_out;
     double* long_out;
     struct Acc { double v[2 * NV]; };
-    struct Pre { double l, u, d; double yy[NV]; };
+    KktRowEpi shifted(unsigned blocks) const {
+        KktRowEpi e = *this;
+        e.block_out += (size_t)blocks * 2 * NV;
+        return e;
+    }
+    // inputs are read when the row is reduced (no prefetch): four iterates
+    // per row would cost too many registers
+    struct Pre {};
     static constexpr int NPRE = 3 + NV;
     static constexpr int pre_esz(int k) { return k == 2 ? 8 : (int)sizeof(T); }
     __device__ const void* pre_src(int k) const {
@@ -259,40 +307,24 @@ struct KktRowEpi {
 #pragma unroll
         for (int q = 0; q < 2 * NV; q++) a.v[q] = 0.0;
     }
-    __device__ __forceinline__ Pre pre_global(int i) const {
-        Pre p;
-        p.l = (double)ld_stream(lc + i);
-        p.u = (double)ld_stream(uc + i);
-        p.d = ld_stream(invD1 + i);
-#pragma unroll
-        for (int k = 0; k < NV; k++) p.yy[k] = (double)ld_stream(y[k] + i);
-        return p;
-    }
-    __device__ __forceinline__ Pre pre_staged(const Staged<NPRE>& st, int i) const {
-        Pre p;
-        p.l = (double)st.template get<T>(0, i);
-        p.u = (double)st.template get<T>(1, i);
-        p.d = st.template get<double>(2, i);
-#pragma unroll
-        for (int k = 0; k < NV; k++) p.yy[k] = (double)st.template get<T>(3 + k, i);
-        return p;
-    }
-    __device__ __forceinline__ void terms(int p, T s, const Pre& q, double& pr2, double& pc) const {
+    __device__ __forceinline__ Pre pre_global(int) const { return Pre{}; }
+    __device__ __forceinline__ void terms(int p, int i, T s, double& pr2, double& pc) const {
+        const double l = (double)lc[i], u = (double)uc[i];
         const double sd = (double)s;
-        const double d = __dmul_rn(q.d, __dsub_rn(sd, proj_box(sd, q.l, q.u)));
+        const double d = __dmul_rn(invD1[i], __dsub_rn(sd, proj_box(sd, l, u)));
         pr2 = __dmul_rn(d, d);
-        const double yy = q.yy[p];
-        pc = __dsub_rn(safeprod_left(q.u, pos_part(-yy)), safeprod_left(q.l, neg_part(-yy)));
+        const double yy = (double)y[p][i];
+        pc = __dsub_rn(safeprod_left(u, pos_part(-yy)), safeprod_left(l, neg_part(-yy)));
     }
-    __device__ __forceinline__ void row(int p, int, T s, const Pre& q, Acc& a) {
+    __device__ __forceinline__ void row(int p, int i, T s, const Pre&, Acc& a) {
         double pr2, pc;
-        terms(p, s, q, pr2, pc);
+        terms(p, i, s, pr2, pc);
         a.v[2 * p] += pr2;
         a.v[2 * p + 1] += pc;
     }
     __device__ void row_long(int p, int i, T s, int lid, Acc&) {
         double pr2, pc;
-        terms(p, s, pre_global(i), pr2, pc);
+        terms(p, i, s, pr2, pc);
         long_out[(size_t)lid * 2 * NV + 2 * p] = pr2;
         long_out[(size_t)lid * 2 * NV + 2 * p + 1] = pc;
     }
@@ -310,7 +342,12 @@ struct KktColEpi {
     double* block_out;
     double* long_out;
     struct Acc { double v[3 * NV]; };
-    struct Pre { double c, l, u, d; double xx[NV]; };
+    KktColEpi shifted(unsigned blocks) const {
+        KktColEpi e = *this;
+        e.block_out += (size_t)blocks * 3 * NV;
+        return e;
+    }
+    struct Pre {};
     static constexpr int NPRE = 4 + NV;
     static constexpr int pre_esz(int k) { return k == 3 ? 8 : (int)sizeof(T); }
     __device__ const void* pre_src(int k) const {
@@ -321,45 +358,27 @@ struct KktColEpi {
 #pragma unroll
         for (int q = 0; q < 3 * NV; q++) a.v[q] = 0.0;
     }
-    __device__ __forceinline__ Pre pre_global(int j) const {
-        Pre p;
-        p.c = (double)ld_stream(c + j);
-        p.l = (double)ld_stream(lv + j);
-        p.u = (double)ld_stream(uv + j);
-        p.d = ld_stream(invD2 + j);
-#pragma unroll
-        for (int k = 0; k < NV; k++) p.xx[k] = (double)ld_stream(x[k] + j);
-        return p;
-    }
-    __device__ __forceinline__ Pre pre_staged(const Staged<NPRE>& st, int j) const {
-        Pre p;
-        p.c = (double)st.template get<T>(0, j);
-        p.l = (double)st.template get<T>(1, j);
-        p.u = (double)st.template get<T>(2, j);
-        p.d = st.template get<double>(3, j);
-#pragma unroll
-        for (int k = 0; k < NV; k++) p.xx[k] = (double)st.template get<T>(4 + k, j);
-        return p;
-    }
-    __device__ __forceinline__ void terms(int p, T s, const Pre& q, double& du2, double& pv,
+    __device__ __forceinline__ Pre pre_global(int) const { return Pre{}; }
+    __device__ __forceinline__ void terms(int p, int j, T s, double& du2, double& pv,
                                           double& cx) const {
-        const double g = __dsub_rn(q.c, (double)s);
-        const double r = proj_multiplier(g, q.l, q.u);
-        const double d = __dmul_rn(q.d, __dsub_rn(g, r));
+        const double cj = (double)c[j], l = (double)lv[j], u = (double)uv[j];
+        const double g = __dsub_rn(cj, (double)s);
+        const double r = proj_multiplier(g, l, u);
+        const double d = __dmul_rn(invD2[j], __dsub_rn(g, r));
         du2 = __dmul_rn(d, d);
-        pv = __dsub_rn(safeprod_left(q.u, pos_part(-r)), safeprod_left(q.l, neg_part(-r)));
-        cx = __dmul_rn(q.c, q.xx[p]);
+        pv = __dsub_rn(safeprod_left(u, pos_part(-r)), safeprod_left(l, neg_part(-r)));
+        cx = __dmul_rn(cj, (double)x[p][j]);
     }
-    __device__ __forceinline__ void row(int p, int, T s, const Pre& q, Acc& a) {
+    __device__ __forceinline__ void row(int p, int j, T s, const Pre&, Acc& a) {
         double du2, pv, cx;
-        terms(p, s, q, du2, pv, cx);
+        terms(p, j, s, du2, pv, cx);
         a.v[3 * p] += du2;
         a.v[3 * p + 1] += pv;
         a.v[3 * p + 2] += cx;
     }
     __device__ void row_long(int p, int j, T s, int lid, Acc&) {
         double du2, pv, cx;
-        terms(p, s, pre_global(j), du2, pv, cx);
+        terms(p, j, s, du2, pv, cx);
         double* o = long_out + (size_t)lid * 3 * NV + 3 * p;
         o[0] = du2;
         o[1] = pv;
@@ -376,6 +395,11 @@ struct PowerEpi {
     double* block_out;
     double* long_out;
     struct Acc { double v[2]; };
+    PowerEpi shifted(unsigned blocks) const {
+        PowerEpi e = *this;
+        e.block_out += (size_t)blocks * 2;
+        return e;
+    }
     struct Pre { T x; };
     static constexpr int NPRE = 1;
     static constexpr int pre_esz(int) { return (int)sizeof(T); }
@@ -464,12 +488,12 @@ inline unsigned red_grid(Handle& h, int64_t items) {
 template <class T>
 CsrView<T, T> view_A(ProblemT<T>& P) {
     return CsrView<T, T>{P.a_ptr.p, P.a_idx.p, P.a_val.p, P.planA.tasks.p, P.planA.ntasks,
-                         P.planA.counters.p, P.partA.p};
+                         P.planA.ltasks.p, P.planA.nltasks, P.planA.counters.p, P.partA.p};
 }
 template <class T>
 CsrView<T, T> view_At(ProblemT<T>& P) {
     return CsrView<T, T>{P.at_ptr.p, P.at_idx.p, P.at_val.p, P.planAt.tasks.p, P.planAt.ntasks,
-                         P.planAt.counters.p, P.partAt.p};
+                         P.planAt.ltasks.p, P.planAt.nltasks, P.planAt.counters.p, P.partAt.p};
 }
 
 // device reduction of (rows x q) partials into host doubles
@@ -719,6 +743,7 @@ struct StateT : StateBase {
     }
 
     bool pdlp() const { return prm.algorithm == CPDLP_ALGO_PDLP; }
+    int step_launches() const { return tiles_launches(PT->planA) + tiles_launches(PT->planAt); }
 
     StepCoef<T> coef_for(double eta_sum_k) const {
         StepCoef<T> k;
@@ -785,7 +810,7 @@ struct StateT : StateBase {
         CK(cudaMemcpyAsync(coef.p, coef_host.data(), sizeof(StepCoef<T>) * len,
                            cudaMemcpyHostToDevice, s));
         CK(cudaGraphLaunch(graph[cur], s));
-        launches += 2 * (int64_t)len;
+        launches += (int64_t)len * step_launches();
         eta_sum = es;
         if (len & 1) cur ^= 1;
         advance_counters(len);
@@ -798,7 +823,7 @@ struct StateT : StateBase {
         CK(cudaMemcpyAsync(coef1.p, &k, sizeof(k), cudaMemcpyHostToDevice, s));
         CK(cudaStreamSynchronize(s));
         enqueue_step(cur, coef1.p, s);
-        launches += 2;
+        launches += step_launches();
         cur ^= 1;
         if (pdlp()) eta_sum += eta;
         advance_counters(1);
@@ -815,31 +840,36 @@ struct StateT : StateBase {
         check_tile_error(h->stream);
     }
 
-    // KKT errors of NV (x, y) pairs in one pass (errors.jl:65-109)
+    // KKT errors (errors.jl:65-109) of NV (x, y) pairs: one row-side and one
+    // column-side tile pass per pair, each pair's FP64 block partials in its
+    // own segment, one segmented reduction per side and one read-back.  A
+    // pair's result does not depend on its slot (same kernels, same order).
+    void enqueue_kkt_pair(int p, const T* xp, const T* yp) {
+        ProblemT<T>& P = *PT;
+        cudaStream_t s = h->stream;
+        const unsigned gA = tiles_grid(P.planA), gAt = tiles_grid(P.planAt);
+        KktRowEpi<T, 1> re;
+        re.lc = P.lc.p; re.uc = P.uc.p; re.invD1 = P.invD1.p;
+        re.y[0] = yp;
+        re.block_out = P.red_rows.p + (size_t)p * P.rows_A_partials * 2;
+        re.long_out = re.block_out + (size_t)gA * 2;
+        launch_tiles<1>(P.planA, view_A(P), VecSet<T, 1>{{xp}}, re, s);
+        KktColEpi<T, 1> ce;
+        ce.c = P.c.p; ce.lv = P.lv.p; ce.uv = P.uv.p; ce.invD2 = P.invD2.p;
+        ce.x[0] = xp;
+        ce.block_out = P.red_cols.p + (size_t)p * P.rows_At_partials * 3;
+        ce.long_out = ce.block_out + (size_t)gAt * 3;
+        launch_tiles<1>(P.planAt, view_At(P), VecSet<T, 1>{{yp}}, ce, s);
+    }
+
     template <int NV>
     void kkt_multi(const T* const (&xs)[NV], const T* const (&ys)[NV], cpdlp_kkt_errors* out) {
         ProblemT<T>& P = *PT;
         cudaStream_t s = h->stream;
-        const unsigned gA = tiles_grid(P.planA), gAt = tiles_grid(P.planAt);
-        KktRowEpi<T, NV> re;
-        re.lc = P.lc.p; re.uc = P.uc.p; re.invD1 = P.invD1.p;
-        for (int p = 0; p < NV; p++) re.y[p] = ys[p];
-        re.block_out = P.red_rows.p;
-        re.long_out = P.red_rows.p + (size_t)gA * 2 * NV;
-        VecSet<T, NV> vx;
-        for (int p = 0; p < NV; p++) vx.v[p] = xs[p];
-        launch_tiles<NV>(P.planA, view_A(P), vx, re, s);
-        KktColEpi<T, NV> ce;
-        ce.c = P.c.p; ce.lv = P.lv.p; ce.uv = P.uv.p; ce.invD2 = P.invD2.p;
-        for (int p = 0; p < NV; p++) ce.x[p] = xs[p];
-        ce.block_out = P.red_cols.p;
-        ce.long_out = P.red_cols.p + (size_t)gAt * 3 * NV;
-        VecSet<T, NV> vy;
-        for (int p = 0; p < NV; p++) vy.v[p] = ys[p];
-        launch_tiles<NV>(P.planAt, view_At(P), vy, ce, s);
-        reduce_partials(P.red_rows.p, P.rows_A_partials, 2 * NV, P.red_out.p, s);
-        reduce_partials(P.red_cols.p, P.rows_At_partials, 3 * NV, P.red_out.p + 2 * NV, s);
-        launches += 4;
+        for (int p = 0; p < NV; p++) enqueue_kkt_pair(p, xs[p], ys[p]);
+        reduce_partials(P.red_rows.p, P.rows_A_partials, 2, P.red_out.p, s, NV);
+        reduce_partials(P.red_cols.p, P.rows_At_partials, 3, P.red_out.p + 2 * NV, s, NV);
+        launches += NV * (tiles_launches(P.planA) + tiles_launches(P.planAt)) + 2;
         double* pin = h->pinned_area(sizeof(double) * 64);
         CK(cudaMemcpyAsync(pin, P.red_out.p, sizeof(double) * 5 * NV, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
@@ -1030,21 +1060,10 @@ struct StateT : StateBase {
             launch_tiles<1>(P.planA, view_A(P), VecSet<T, 1>{{xbar.p}}, de, s);
         });
         ms[2] = timed([&] {
-            const unsigned gA = tiles_grid(P.planA), gAt = tiles_grid(P.planAt);
-            KktRowEpi<T, 4> re;
-            re.lc = P.lc.p; re.uc = P.uc.p; re.invD1 = P.invD1.p;
-            re.y[0] = y[cur].p; re.y[1] = ya[cur].p; re.y[2] = y[cur ^ 1].p; re.y[3] = ya[cur ^ 1].p;
-            re.block_out = P.red_rows.p;
-            re.long_out = P.red_rows.p + (size_t)gA * 8;
-            VecSet<T, 4> vx{{x[cur].p, xa[cur].p, x[cur ^ 1].p, xa[cur ^ 1].p}};
-            launch_tiles<4>(P.planA, view_A(P), vx, re, s);
-            KktColEpi<T, 4> ce;
-            ce.c = P.c.p; ce.lv = P.lv.p; ce.uv = P.uv.p; ce.invD2 = P.invD2.p;
-            ce.x[0] = x[cur].p; ce.x[1] = xa[cur].p; ce.x[2] = x[cur ^ 1].p; ce.x[3] = xa[cur ^ 1].p;
-            ce.block_out = P.red_cols.p;
-            ce.long_out = P.red_cols.p + (size_t)gAt * 12;
-            VecSet<T, 4> vy{{y[cur].p, ya[cur].p, y[cur ^ 1].p, ya[cur ^ 1].p}};
-            launch_tiles<4>(P.planAt, view_At(P), vy, ce, s);
+            enqueue_kkt_pair(0, x[cur].p, y[cur].p);
+            enqueue_kkt_pair(1, xa[cur].p, ya[cur].p);
+            enqueue_kkt_pair(2, x[cur ^ 1].p, y[cur ^ 1].p);
+            enqueue_kkt_pair(3, xa[cur ^ 1].p, ya[cur ^ 1].p);
         });
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);

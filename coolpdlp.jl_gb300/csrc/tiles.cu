@@ -34,7 +34,7 @@ void build_tile_plan(const std::vector<int32_t>& ptr, int32_t rows, int items, T
             // warp path: one piece per TILE nonzeros; only multi-piece rows use slots
             int32_t lid = (int32_t)plan.long_rows.size();
             int32_t np = (len + tile - 1) / tile;
-            for (int32_t p = 0; p < np; p++) longs.push_back(make_int4(r, p, lid, slot));
+            for (int32_t p = 0; p < np; p++) longs.push_back(make_int4(r, -(p + 1), lid, slot));
             plan.long_rows.push_back(r);
             if (np > 1) slot += np;
             r++;
@@ -47,20 +47,20 @@ void build_tile_plan(const std::vector<int32_t>& ptr, int32_t rows, int items, T
             nz += l;
             r++;
         }
-        shorts.push_back(make_int4(r0, r, -1, 0));
+        shorts.push_back(make_int4(r0, r, ptr[r0], ptr[r]));
     }
     plan.nlong = (int32_t)plan.long_rows.size();
     plan.npieces = slot;
     plan.nshort = (int32_t)shorts.size();
-    // long-row pieces first: they start early and the short tiles fill the tail
-    std::vector<int4> all;
-    all.reserve(longs.size() + shorts.size());
-    all.insert(all.end(), longs.begin(), longs.end());
-    all.insert(all.end(), shorts.begin(), shorts.end());
-    plan.ntasks = (int32_t)all.size();
-    plan.tasks.alloc(all.size() ? all.size() : 1);
-    if (!all.empty())
-        CK(cudaMemcpyAsync(plan.tasks.p, all.data(), sizeof(int4) * all.size(),
+    plan.ntasks = (int32_t)shorts.size();
+    plan.nltasks = (int32_t)longs.size();
+    plan.tasks.alloc(shorts.size() ? shorts.size() : 1);
+    plan.ltasks.alloc(longs.size() ? longs.size() : 1);
+    if (!shorts.empty())
+        CK(cudaMemcpyAsync(plan.tasks.p, shorts.data(), sizeof(int4) * shorts.size(),
+                           cudaMemcpyHostToDevice, s));
+    if (!longs.empty())
+        CK(cudaMemcpyAsync(plan.ltasks.p, longs.data(), sizeof(int4) * longs.size(),
                            cudaMemcpyHostToDevice, s));
     plan.counters.alloc(plan.nlong ? (size_t)plan.nlong : 1);
     CK(cudaMemsetAsync(plan.counters.p, 0, sizeof(int32_t) * plan.counters.n, s));
@@ -93,10 +93,13 @@ void check_tile_error(cudaStream_t s) {
 }
 
 namespace {
+// block b reduces segment b: rows [b*nrows, (b+1)*nrows) -> out[b*q + j]
 __global__ void k_reduce_partials(const double* __restrict__ part, int64_t nrows, int q,
                                   double* __restrict__ out) {
     __shared__ double red[32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    part += (size_t)blockIdx.x * nrows * q;
+    out += (size_t)blockIdx.x * q;
     for (int j = 0; j < q; j++) {
         double s = 0.0;
         for (int64_t r = threadIdx.x; r < nrows; r += blockDim.x) s += part[r * q + j];
@@ -114,8 +117,9 @@ __global__ void k_reduce_partials(const double* __restrict__ part, int64_t nrows
 }
 }  // namespace
 
-void reduce_partials(const double* partials, int64_t nrows, int q, double* out, cudaStream_t s) {
-    k_reduce_partials<<<1, 1024, 0, s>>>(partials, nrows, q, out);
+void reduce_partials(const double* partials, int64_t nrows, int q, double* out, cudaStream_t s,
+                     int nseg) {
+    k_reduce_partials<<<nseg, 1024, 0, s>>>(partials, nrows, q, out);
     CK_LAUNCH();
 }
 

@@ -1,7 +1,7 @@
 // tiles.cuh -- the warp-tile CSR SpMV engine with fused per-row epilogues.
 //
 // Work partition (built once per matrix on the host from its row pointer):
-//  * short tile {r0, r1, -1, 0}: consecutive rows [r0, r1), each at most
+//  * short tile {r0, r1, nz0, nz1}: consecutive rows [r0, r1), each at most
 //    LONG_ROW nonzeros, together at most TILE = 32*ITEMS nonzeros and at most
 //    MAX_TILE_ROWS rows.  One warp
 //      1. prefetches the row pointers and the epilogue inputs of its rows,
@@ -11,7 +11,7 @@
 //      4. writes value*x products to shared memory, and
 //      5. lets every lane reduce whole rows in ascending column order (the
 //         reference's order) and apply the fused epilogue.
-//  * long-row piece {row, piece, long_id, slot_base}: a row longer than
+//  * long-row piece {row, -(piece+1), long_id, slot_base}: a row longer than
 //    LONG_ROW is cut into TILE-sized pieces, one warp each, reduced with warp
 //    shuffles.  A row of several pieces writes each partial to a scratch slot;
 //    the warp that completes the row (atomic counter, no waiting) adds the
@@ -40,7 +40,9 @@ struct TilePlan {
     int32_t nshort = 0;
     int32_t nlong = 0;      // rows that take the warp path
     int32_t npieces = 0;    // pieces of all long rows
-    DBuf<int4> tasks;
+    int32_t nltasks = 0;    // long-row pieces (tasks of the long-row kernel)
+    DBuf<int4> tasks;       // short tiles
+    DBuf<int4> ltasks;      // long-row pieces
     DBuf<int32_t> counters; // per long row, zero between launches
     std::vector<int32_t> long_rows;
     int tile_nnz() const { return 32 * items; }
@@ -58,8 +60,10 @@ struct CsrView {
     const int32_t* __restrict__ ptr;
     const int32_t* __restrict__ idx;
     const V* __restrict__ val;
-    const int4* __restrict__ tasks;
+    const int4* __restrict__ tasks;       // short tiles
     int32_t ntasks;
+    const int4* __restrict__ ltasks;      // long-row pieces
+    int32_t nltasks;
     int32_t* counters;
     T* partials;   // npieces * NVEC
 };
@@ -101,7 +105,8 @@ __device__ __forceinline__ void load4v(const int8_t* p, T (&o)[4]) {
     o[0] = (T)(int8_t)(v & 0xff); o[1] = (T)(int8_t)((v >> 8) & 0xff);
     o[2] = (T)(int8_t)((v >> 16) & 0xff); o[3] = (T)(int8_t)((v >> 24) & 0xff);
 }
-// read-only gather through the texture/L1 path, same ordering property
+// gathers of x[col] through the read-only path; same ordering property as
+// the loads above
 __device__ __forceinline__ float gather(const float* p) {
     float v;
     asm volatile("ld.global.nc.f32 %0, [%1];" : "=f"(v) : "l"(p));
@@ -205,16 +210,16 @@ struct Staged {
 };
 
 // One warp, one short tile.  All loads of a phase are volatile PTX issued back
-// to back, so they are in flight together: (1) row pointers and the epilogue
-// inputs of this lane's rows, (2) the tile's indices and values with 128-bit
-// loads over the 4-element-aligned window, (3) the gathers.
+// to back, so they are in flight together: (1) the tile's indices and values
+// with 128-bit loads over the 4-element-aligned window plus the row pointers
+// and epilogue inputs of this lane's rows, (2) one batch of gathers.  Then
+// products go to shared memory and every lane reduces whole rows in column
+// order before the fused epilogue.
 template <int ITEMS, int NVEC, class V, class T, class Epi>
 __device__ __forceinline__ void short_tile(const CsrView<V, T>& A, const VecSet<T, NVEC>& xs,
                                            Epi& epi, typename Epi::Acc& acc, int r0, int r1,
-                                           int lane, T* prod) {
+                                           int nz0, int nz1, int lane, T* prod) {
     constexpr int NV4 = ITEMS / 4 + 1;  // 4-element chunks per lane (+1: alignment slack)
-    const int nz0 = ld_keep(A.ptr + r0);
-    const int nz1 = ld_keep(A.ptr + r1);
     const int base = nz0 & ~3;
     int ra[ROWS_PER_LANE], rb[ROWS_PER_LANE];
     typename Epi::Pre pre[ROWS_PER_LANE];
@@ -242,7 +247,9 @@ __device__ __forceinline__ void short_tile(const CsrView<V, T>& A, const VecSet<
             for (int q = 0; q < 4; q++) { cc[j][q] = 0; vv[j][q] = T(0); }
         }
     }
-#pragma unroll
+    // one input vector at a time (not unrolled): with several vectors (the KKT
+    // pass) this keeps one batch of gathers in registers instead of all of them
+#pragma unroll 1
     for (int p = 0; p < NVEC; p++) {
         T xg[NV4][4];
 #pragma unroll
@@ -250,7 +257,8 @@ __device__ __forceinline__ void short_tile(const CsrView<V, T>& A, const VecSet<
             const int e = base + 4 * (lane + 32 * j);
 #pragma unroll
             for (int q = 0; q < 4; q++)
-                xg[j][q] = (e + q >= nz0 && e + q < nz1) ? gather(xs.v[p] + cc[j][q]) : T(0);
+                xg[j][q] = (e + q >= nz0 && e + q < nz1) ? gather(xs.v[p] + cc[j][q])
+                                                         : T(0);
         }
 #pragma unroll
         for (int j = 0; j < NV4; j++) {
@@ -264,20 +272,25 @@ __device__ __forceinline__ void short_tile(const CsrView<V, T>& A, const VecSet<
         for (int k = 0; k < ROWS_PER_LANE; k++) {
             const int r = r0 + lane + 32 * k;
             if (r < r1) {
-                T s = T(0);
-                for (int i = ra[k] - nz0; i < rb[k] - nz0; i++) s = add_rn(s, prod[i]);
-                epi.row(p, r, s, pre[k], acc);
+                T sum = T(0);
+                for (int i = ra[k] - nz0; i < rb[k] - nz0; i++) sum = add_rn(sum, prod[i]);
+                epi.row(p, r, sum, pre[k], acc);
             }
         }
         __syncwarp();
     }
 }
 
+// One warp, one TILE-sized piece of a row longer than LONG_ROW: lane-strided
+// coalesced loads, lane partial sums, a fixed shuffle tree.  Multi-piece rows
+// combine through scratch slots: the warp that completes the row (atomic
+// counter, no waiting) adds the partials in piece order and applies the
+// epilogue.
 template <int ITEMS, int NVEC, class V, class T, class Epi>
 __device__ __forceinline__ void long_piece(const CsrView<V, T>& A, const VecSet<T, NVEC>& xs,
                                            Epi& epi, typename Epi::Acc& acc, int4 t, int lane) {
     constexpr int TILE = 32 * ITEMS;
-    const int row = t.x, piece = t.y, lid = t.z, base_slot = t.w;
+    const int row = t.x, piece = -t.y - 1, lid = t.z, base_slot = t.w;
     const int rb = ld_keep(A.ptr + row), re = ld_keep(A.ptr + row + 1);
     const int npieces = (re - rb + TILE - 1) / TILE;
     const int a = rb + piece * TILE;
@@ -323,6 +336,8 @@ __device__ __forceinline__ void long_piece(const CsrView<V, T>& A, const VecSet<
     }
 }
 
+// One launch covers both kinds of work: the first warps take the long-row
+// pieces (so they start early), the rest the short tiles.
 template <int ITEMS, int WARPS, int NVEC, class V, class T, class Epi>
 __global__ void __launch_bounds__(WARPS * 32)
     k_tiles(CsrView<V, T> A, VecSet<T, NVEC> xs, Epi epi) {
@@ -331,10 +346,11 @@ __global__ void __launch_bounds__(WARPS * 32)
     const int task = blockIdx.x * WARPS + w;
     typename Epi::Acc acc;
     epi.init(acc);
-    if (task < A.ntasks) {
-        const int4 t = A.tasks[task];
-        if (t.z < 0) short_tile<ITEMS, NVEC>(A, xs, epi, acc, t.x, t.y, lane, prod[w]);
-        else long_piece<ITEMS, NVEC>(A, xs, epi, acc, t, lane);
+    if (task < A.nltasks) {
+        long_piece<ITEMS, NVEC>(A, xs, epi, acc, A.ltasks[task], lane);
+    } else if (task - A.nltasks < A.ntasks) {
+        const int4 t = A.tasks[task - A.nltasks];
+        short_tile<ITEMS, NVEC>(A, xs, epi, acc, t.x, t.y, t.z, t.w, lane, prod[w]);
     }
     epi.finish(acc);
 }
@@ -347,11 +363,14 @@ int* tile_error_word();
 // if a kernel gave up a bounded wait.
 void check_tile_error(cudaStream_t s);
 
+// Launches the tile kernel on `s`.  Reducing epilogues write one row of
+// block partials per block.
 template <int NVEC, class V, class T, class Epi>
 void launch_tiles(const TilePlan& plan, const CsrView<V, T>& view, const VecSet<T, NVEC>& xs,
                   const Epi& epi, cudaStream_t s) {
-    if (plan.ntasks == 0) return;
-    const unsigned grid = (unsigned)((plan.ntasks + TILE_WARPS - 1) / TILE_WARPS);
+    const int64_t tasks = (int64_t)plan.ntasks + plan.nltasks;
+    if (tasks == 0) return;
+    const unsigned grid = (unsigned)((tasks + TILE_WARPS - 1) / TILE_WARPS);
     switch (plan.items) {
         case 4: k_tiles<4, TILE_WARPS, NVEC, V, T, Epi><<<grid, TILE_WARPS * 32, 0, s>>>(view, xs, epi); break;
         case 8: k_tiles<8, TILE_WARPS, NVEC, V, T, Epi><<<grid, TILE_WARPS * 32, 0, s>>>(view, xs, epi); break;
@@ -360,8 +379,12 @@ void launch_tiles(const TilePlan& plan, const CsrView<V, T>& view, const VecSet<
     CK_LAUNCH();
 }
 
+// number of kernels launch_tiles issues for this plan
+inline int tiles_launches(const TilePlan& plan) { return (plan.ntasks + plan.nltasks) ? 1 : 0; }
+
+// block-partial rows written by a reducing epilogue
 inline unsigned tiles_grid(const TilePlan& plan) {
-    return (unsigned)((plan.ntasks + TILE_WARPS - 1) / TILE_WARPS);
+    return (unsigned)(((int64_t)plan.ntasks + plan.nltasks + TILE_WARPS - 1) / TILE_WARPS);
 }
 
 // ---- block reduction of per-thread FP64 accumulators -------------------------
@@ -387,7 +410,9 @@ __device__ __forceinline__ void block_reduce_store(const double (&v)[Q], double*
     }
 }
 
-// Sums `nrows` rows of q partials into out[q] in a fixed order (one block).
-void reduce_partials(const double* partials, int64_t nrows, int q, double* out, cudaStream_t s);
+// Sums `nrows` rows of q partials into out[q] in a fixed order (one block);
+// with nseg > 1, segment k (rows [k*nrows, (k+1)*nrows)) goes to out[k*q..].
+void reduce_partials(const double* partials, int64_t nrows, int q, double* out, cudaStream_t s,
+                     int nseg = 1);
 
 }  // namespace cpdlp

@@ -123,7 +123,8 @@ typedef struct cpdlp_params {
     double refine_reltol;
     /* EXT: CSR tile size in nonzeros for the SpMV work partition (0 = autotune). */
     int32_t tile_nnz;
-    int32_t reserved0;
+    /* EXT: reserved for autotuner flags; must be 0. */
+    int32_t tile_flags;
 } cpdlp_params;
 
 /* An LP in the reference's "cuPDLPx form" (src/problems/milp.jl:1-20):
