@@ -160,7 +160,7 @@ EXPORTED_SYMBOLS = (
     "cpdlp_state_kkt", "cpdlp_state_vectors", "cpdlp_state_solution", "cpdlp_state_stats",
     "cpdlp_state_history", "cpdlp_solve", "cpdlp_problem_spectral_norm",
     "cpdlp_batch_solve", "cpdlp_state_solve_blocks", "cpdlp_state_profile",
-    "cpdlp_state_kernel_bytes",
+    "cpdlp_state_kernel_bytes", "cpdlp_spmv_csr_noalloc",
 )
 
 _LIB = None
@@ -204,6 +204,9 @@ def _declare(lib):
         "cpdlp_state_solve_blocks": (c_int32, [H, H, c_int64, POINTER(StatsC)]),
         "cpdlp_state_profile": (c_int32, [H, H, c_int32, PD]),
         "cpdlp_state_kernel_bytes": (c_int32, [H, PD]),
+        "cpdlp_spmv_csr_noalloc": (c_int32, [H, c_int64, c_int64, c_int64, c_void_p, c_void_p,
+                                             c_void_p, c_int32, c_void_p, c_void_p, c_double,
+                                             c_double]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

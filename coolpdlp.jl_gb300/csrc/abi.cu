@@ -7,6 +7,7 @@
 #include "batch.cuh"
 #include "tiles.cuh"
 #include "matrix.cuh"
+#include "noalloc.cuh"
 #include "solver.cuh"
 
 using namespace cpdlp;
@@ -166,6 +167,16 @@ int cpdlp_spmv(cpdlp_handle* h, const cpdlp_matrix* A, const void* b, void* c, d
         matrix_spmv(*H(h), *reinterpret_cast<const Matrix*>(A), b, c, alpha, beta);
         CK(cudaStreamSynchronize(h->stream));
         check_tile_error(h->stream);
+    });
+}
+
+int cpdlp_spmv_csr_noalloc(cpdlp_handle* h, int64_t m, int64_t n, int64_t nnz,
+                           const int32_t* rowptr, const int32_t* colval, const void* nzval,
+                           int32_t value_type, const void* b, void* c, double alpha,
+                           double beta) {
+    NEED(h);
+    return guarded(h, [&] {
+        spmv_csr_noalloc(*H(h), m, n, nnz, rowptr, colval, nzval, value_type, b, c, alpha, beta);
     });
 }
 

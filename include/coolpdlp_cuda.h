@@ -294,6 +294,24 @@ int cpdlp_solve(cpdlp_handle* h, const cpdlp_lp* lp, const cpdlp_params* params,
 int cpdlp_problem_spectral_norm(cpdlp_handle* h, cpdlp_problem* p, const cpdlp_params* params,
                                 double* norm, int64_t* iterations);
 
+/* c = alpha*A*b + beta*c on caller-owned DEVICE arrays of a 1-based CSR in
+ * the layout of a CuArray-backed GPUSparseMatrixCSR{T,Int32}: rowptr (m+1),
+ * colval (nnz), nzval (nnz, double or float per value_type), b (n), c (m).
+ * beta == 0 does not read c.  No counterpart in the reference: an extra entry
+ * point that allocates nothing, for callers that may not call cudaMalloc when
+ * they need the product (fixed pre-reserved device budgets, host callbacks or
+ * finalizers, CuArray-backed matrices that should not be copied into a
+ * cpdlp_matrix).  Its scratch is a fixed 1 MiB device array of this library,
+ * shared by all calls and kept until process exit: at most 33,554,432
+ * nonzeros (larger inputs return CPDLP_ERR_UNSUPPORTED).  The first call on a
+ * device looks up that array's address (make it before any stream capture);
+ * calls that overlap on the GPU race on the array.  Invalid indices return
+ * CPDLP_ERR_ARGUMENT after the call (offending entries are skipped). */
+int cpdlp_spmv_csr_noalloc(cpdlp_handle* h, int64_t m, int64_t n, int64_t nnz,
+                           const int32_t* rowptr, const int32_t* colval, const void* nzval,
+                           int32_t value_type, const void* b, void* c, double alpha,
+                           double beta);
+
 /* ---- batched solve (many independent LPs in one persistent launch) -------
  * No counterpart in the reference, which solves one LP per call: this is the
  * batched form of solve(milp, algo) (common.jl:203-209) over `count` LPs.
