@@ -81,6 +81,7 @@ class ConvergenceStats:
     omega: float = math.nan
     power_iterations: int = 0
     setup_seconds: float = 0.0
+    refine_kkt_passes: int = 0
 
     def __str__(self):
         return (f"Convergence stats with termination status {self.termination_status.name}:\n"
@@ -241,7 +242,30 @@ def solve(milp: MILP, *args):
     dmilp, sol = preprocess(milp, sol, algo)
     state = initialize(dmilp, sol, algo, starting_time=t0)
     solve_inplace(state)
-    return state.solution(), state.stats()
+    stats = state.stats()
+    sol_out = state.solution()
+    p = algo.params
+    if (p.float_type == A.VAL_F32 and p.refine_reltol > 0
+            and stats.termination_status == OPTIMAL):
+        # FP64 refinement: continue from the FP32 solution in Float64 until
+        # refine_reltol (same scaling, recomputed in FP64)
+        kw = algo.kwargs()
+        kw.update(termination_reltol=p.refine_reltol,
+                  max_kkt_passes=max(p.max_kkt_passes - stats.kkt_passes, 1),
+                  time_limit=p.time_limit - (time.time() - t0), refine_reltol=0.0)
+        algo64 = Algorithm(algo.name, np.float64, algo.Ti, algo.M, device=algo.device, **kw)
+        dm64, _ = preprocess(milp, sol_out, algo64)
+        st64 = initialize(dm64, sol_out, algo64, starting_time=t0)
+        solve_inplace(st64)
+        s64 = st64.stats()
+        hist = stats.error_history + [(stats.kkt_passes + k, e) for k, e in s64.error_history]
+        passes32 = stats.kkt_passes
+        stats = s64
+        stats.error_history = hist
+        stats.kkt_passes = passes32 + s64.kkt_passes
+        stats.refine_kkt_passes = s64.kkt_passes
+        sol_out = st64.solution()
+    return sol_out, stats
 
 
 def nbcons_zero_cost(milp: MILP) -> bool:

@@ -325,16 +325,7 @@ int cpdlp_solve(cpdlp_handle* h, const cpdlp_lp* lp, const cpdlp_params* params,
                 const double* x0, const double* y0, double* x_out, double* y_out,
                 cpdlp_stats* stats) {
     NEED(h);
-    return guarded(h, [&] {
-        double t0 = now_seconds();
-        std::unique_ptr<ProblemBase> P(problem_create(*H(h), lp, params));
-        std::unique_ptr<StateBase> S(state_create(*H(h), P.get(), params, x0, y0));
-        S->starting_time = t0;
-        if (P->m == 0 && P->zero_cost) S->early_exit_zero_problem();  // common.jl:194-198
-        else S->solve();
-        S->solution(x_out, y_out);
-        if (stats) S->stats(stats);
-    });
+    return guarded(h, [&] { solve_full(*H(h), lp, params, x0, y0, x_out, y_out, stats); });
 }
 
 int cpdlp_batch_solve(cpdlp_handle* h, int64_t count, const cpdlp_lp* lps,

@@ -77,6 +77,13 @@ ProblemBase* problem_create(Handle& h, const cpdlp_lp* lp, const cpdlp_params* p
 StateBase* state_create(Handle& h, ProblemBase* P, const cpdlp_params* prm, const double* x0,
                         const double* y0);
 double problem_spectral_norm(Handle& h, ProblemBase* P, const cpdlp_params* prm, int64_t* iters);
+
+// solve(milp, sol, algo) (common.jl:186-209) on the device, plus the FP64
+// refinement phase: when params->float_type is FP32, refine_reltol > 0 and the
+// FP32 solve ends OPTIMAL, PDLP continues in FP64 from the FP32 solution
+// until refine_reltol.  x_out (n) / y_out (m) may be null.
+void solve_full(Handle& h, const cpdlp_lp* lp, const cpdlp_params* params, const double* x0,
+                const double* y0, double* x_out, double* y_out, cpdlp_stats* stats);
 void problem_scaling(Handle& h, ProblemBase* P, double* d1, double* d2);
 
 }  // namespace cpdlp

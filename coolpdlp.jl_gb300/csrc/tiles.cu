@@ -20,35 +20,52 @@ int choose_items(int64_t nnz, int64_t rows, int requested_tile_nnz) {
 }
 
 void build_tile_plan(const std::vector<int32_t>& ptr, int32_t rows, int items, TilePlan& plan,
-                     cudaStream_t s) {
+                     cudaStream_t s, const std::vector<int64_t>* seg_rows,
+                     std::vector<int32_t>* seg_tasks, std::vector<int32_t>* seg_ltasks,
+                     std::vector<int32_t>* seg_lids) {
     plan.rows = rows;
     plan.items = items;
     const int tile = 32 * items;
     std::vector<int4> longs, shorts;
     plan.long_rows.clear();
     int32_t slot = 0;
-    int32_t r = 0;
-    while (r < rows) {
-        int32_t len = ptr[r + 1] - ptr[r];
-        if (len > LONG_ROW) {
-            // warp path: one piece per TILE nonzeros; only multi-piece rows use slots
-            int32_t lid = (int32_t)plan.long_rows.size();
-            int32_t np = (len + tile - 1) / tile;
-            for (int32_t p = 0; p < np; p++) longs.push_back(make_int4(r, -(p + 1), lid, slot));
-            plan.long_rows.push_back(r);
-            if (np > 1) slot += np;
-            r++;
-            continue;
+    const std::vector<int64_t> whole = {0, (int64_t)rows};
+    const std::vector<int64_t>& segs = seg_rows ? *seg_rows : whole;
+    const size_t nseg = segs.size() - 1;
+    if (seg_tasks) seg_tasks->assign(nseg + 1, 0);
+    if (seg_ltasks) seg_ltasks->assign(nseg + 1, 0);
+    if (seg_lids) seg_lids->assign(nseg + 1, 0);
+    for (size_t k = 0; k < nseg; k++) {
+        if (seg_tasks) (*seg_tasks)[k] = (int32_t)shorts.size();
+        if (seg_ltasks) (*seg_ltasks)[k] = (int32_t)longs.size();
+        if (seg_lids) (*seg_lids)[k] = (int32_t)plan.long_rows.size();
+        const int32_t end = (int32_t)segs[k + 1];
+        int32_t r = (int32_t)segs[k];
+        while (r < end) {
+            int32_t len = ptr[r + 1] - ptr[r];
+            if (len > LONG_ROW) {
+                // warp path: one piece per TILE nonzeros; only multi-piece rows use slots
+                int32_t lid = (int32_t)plan.long_rows.size();
+                int32_t np = (len + tile - 1) / tile;
+                for (int32_t p = 0; p < np; p++) longs.push_back(make_int4(r, -(p + 1), lid, slot));
+                plan.long_rows.push_back(r);
+                if (np > 1) slot += np;
+                r++;
+                continue;
+            }
+            int32_t r0 = r, nz = 0;
+            while (r < end && r - r0 < MAX_TILE_ROWS) {
+                int32_t l = ptr[r + 1] - ptr[r];
+                if (l > LONG_ROW || nz + l > tile) break;
+                nz += l;
+                r++;
+            }
+            shorts.push_back(make_int4(r0, r, ptr[r0], ptr[r]));
         }
-        int32_t r0 = r, nz = 0;
-        while (r < rows && r - r0 < MAX_TILE_ROWS) {
-            int32_t l = ptr[r + 1] - ptr[r];
-            if (l > LONG_ROW || nz + l > tile) break;
-            nz += l;
-            r++;
-        }
-        shorts.push_back(make_int4(r0, r, ptr[r0], ptr[r]));
     }
+    if (seg_tasks) (*seg_tasks)[nseg] = (int32_t)shorts.size();
+    if (seg_ltasks) (*seg_ltasks)[nseg] = (int32_t)longs.size();
+    if (seg_lids) (*seg_lids)[nseg] = (int32_t)plan.long_rows.size();
     plan.nlong = (int32_t)plan.long_rows.size();
     plan.npieces = slot;
     plan.nshort = (int32_t)shorts.size();

@@ -49,8 +49,14 @@ struct TilePlan {
 };
 
 // Host-side partition of the rows of a CSR (ptr on the host, 0-based, rows+1).
+// With seg_rows (segment start rows, last = rows) no tile crosses a segment
+// start, and seg_tasks / seg_ltasks / seg_lids receive, per segment, the first
+// short task, long task and long-row id (one extra final entry = totals).
 void build_tile_plan(const std::vector<int32_t>& ptr, int32_t rows, int items, TilePlan& plan,
-                     cudaStream_t s);
+                     cudaStream_t s, const std::vector<int64_t>* seg_rows = nullptr,
+                     std::vector<int32_t>* seg_tasks = nullptr,
+                     std::vector<int32_t>* seg_ltasks = nullptr,
+                     std::vector<int32_t>* seg_lids = nullptr);
 
 // Picks nonzeros-per-lane from the size and mean row length (autotuner default).
 int choose_items(int64_t nnz, int64_t rows, int requested_tile_nnz);

@@ -176,3 +176,28 @@ def test_warm_start_matches_oracle(handle, oracle):
     assert int(st.termination_status) == so["termination_status"]
     assert st.kkt_passes == so["kkt_passes"]
     np.testing.assert_allclose(sol.x, xo, rtol=1e-6, atol=1e-8)
+
+
+def test_fp32_with_fp64_refinement_reaches_1e8(handle, oracle):
+    """FP32 iterates to 1e-4, then FP64 refinement to 1e-8 relative KKT; the
+    objective must agree with the Float64 oracle solved to 1e-8."""
+    import coolpdlp as cp
+    from coolpdlp import generators as G
+    lp = G.random_sparse_lp(300, 600, 5, seed=7)
+    xo, yo, so = oracle.solve(lp, oracle.params(termination_reltol=1e-8, max_kkt_passes=200000))
+    assert so["termination_status"] == 0
+    milp = cp.MILP.from_lpdata(lp)
+    sol, st = cp.solve(milp, cp.PDLP(np.float32, refine_reltol=1e-8, max_kkt_passes=200000))
+    assert st.termination_status == cp.OPTIMAL
+    assert cp.relative(st.err) <= 1e-8
+    assert st.refine_kkt_passes > 0 and st.kkt_passes > st.refine_kkt_passes
+    og, oo = float(lp.c @ sol.x), float(lp.c @ xo)
+    assert abs(og - oo) <= 1e-6 * max(1.0, abs(oo)), (og, oo)
+    # the same through the C ABI (cpdlp_solve)
+    from coolpdlp import native, _abi as A
+    L = native.LPStruct(lp.m, lp.n, lp.colptr, lp.rowval, lp.nzval, lp.c, lp.lv, lp.uv, lp.lc, lp.uc)
+    p = A.default_params_py(); p.float_type = A.VAL_F32; p.refine_reltol = 1e-8
+    p.max_kkt_passes = 200000
+    x, y, s = native.solve_lp(handle, L, p)
+    assert s.termination_status == 0 and s.refine_kkt_passes > 0
+    assert abs(float(lp.c @ x) - oo) <= 1e-6 * max(1.0, abs(oo))
