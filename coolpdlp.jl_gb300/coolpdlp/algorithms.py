@@ -259,11 +259,11 @@ def solve(milp: MILP, *args):
         solve_inplace(st64)
         s64 = st64.stats()
         hist = stats.error_history + [(stats.kkt_passes + k, e) for k, e in s64.error_history]
-        passes32 = stats.kkt_passes
+        passes32, passes64 = stats.kkt_passes, s64.kkt_passes
         stats = s64
         stats.error_history = hist
-        stats.kkt_passes = passes32 + s64.kkt_passes
-        stats.refine_kkt_passes = s64.kkt_passes
+        stats.kkt_passes = passes32 + passes64
+        stats.refine_kkt_passes = passes64
         sol_out = st64.solution()
     return sol_out, stats
 

@@ -3,7 +3,7 @@ from __future__ import annotations
 
 import ctypes
 import threading
-from ctypes import POINTER, byref, c_double, c_int64, c_void_p
+from ctypes import POINTER, byref, c_double, c_int32, c_int64, c_void_p
 
 import numpy as np
 
@@ -246,3 +246,77 @@ def batch_solve(handle: Handle, lps: list, params: A.ParamsC):
     handle.check(handle.lib.cpdlp_batch_solve(handle.h, k, arr, byref(params), xp, yp, st),
                  "cpdlp_batch_solve")
     return xs, ys, [st[i] for i in range(k)]
+
+
+class Job:
+    """An asynchronous batch (cpdlp_submit): the LPs are copied, preprocessed
+    on the job's own stream and solved by a persistent kernel while the
+    caller continues.  poll() never blocks; result() waits and collects."""
+
+    def __init__(self, handle: Handle, lps: list, params: A.ParamsC, reltol=None,
+                 x0=None, y0=None):
+        self.handle = handle
+        self.j = None
+        self.k = len(lps)
+        self.shapes = [(lp.s.m, lp.s.n) for lp in lps]
+        arr = (A.LPC * max(self.k, 1))(*[lp.s for lp in lps])
+        rt = None if reltol is None else f64(np.broadcast_to(np.asarray(reltol, dtype=np.float64),
+                                                             (self.k,)).copy())
+        self._keep = [rt]
+        x0p = y0p = None
+        if x0 is not None:
+            xs = [None if v is None else f64(v) for v in x0]
+            self._keep.append(xs)
+            x0p = (_PD * max(self.k, 1))(*[_pd(v) for v in xs])
+        if y0 is not None:
+            ys = [None if v is None else f64(v) for v in y0]
+            self._keep.append(ys)
+            y0p = (_PD * max(self.k, 1))(*[_pd(v) for v in ys])
+        out = c_void_p()
+        handle.check(handle.lib.cpdlp_submit(handle.h, self.k, arr, byref(params), _pd(rt),
+                                             x0p, y0p, byref(out)), "cpdlp_submit")
+        self.j = out.value
+        self._keep = None
+
+    def poll(self) -> bool:
+        done = c_int32()
+        self.handle.check(self.handle.lib.cpdlp_poll(self.handle.h, self.j, byref(done)),
+                          "cpdlp_poll")
+        return bool(done.value)
+
+    def wait(self):
+        self.handle.check(self.handle.lib.cpdlp_wait(self.handle.h, self.j), "cpdlp_wait")
+
+    def cancel(self):
+        self.handle.check(self.handle.lib.cpdlp_cancel(self.handle.h, self.j), "cpdlp_cancel")
+
+    def result(self):
+        """waits, then returns lists of x, y and StatsC (original units)"""
+        self.wait()
+        xs = [np.empty(n) for (_, n) in self.shapes]
+        ys = [np.empty(m) for (m, _) in self.shapes]
+        xp = (_PD * max(self.k, 1))(*[_pd(x) for x in xs])
+        yp = (_PD * max(self.k, 1))(*[_pd(y) for y in ys])
+        st = (A.StatsC * max(self.k, 1))()
+        self.handle.check(self.handle.lib.cpdlp_collect(self.handle.h, self.j, xp, yp, st),
+                          "cpdlp_collect")
+        return xs, ys, [st[i] for i in range(self.k)]
+
+    def close(self):
+        if getattr(self, "j", None):
+            self.handle.lib.cpdlp_job_destroy(self.j)
+            self.j = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def batch_footprint(lps: list, params: A.ParamsC) -> int:
+    """Upper bound of the device bytes a job over these LPs holds."""
+    lib = A.load_library()
+    k = len(lps)
+    arr = (A.LPC * max(k, 1))(*[lp.s for lp in lps])
+    return int(lib.cpdlp_batch_footprint(k, arr, byref(params)))

@@ -22,6 +22,7 @@ template <class F>
 int guarded(cpdlp_handle* h, F&& f) {
     try {
         if (h) CK(cudaSetDevice(h->device));
+        AllocScope scope(h ? h->stream : nullptr);
         f();
         if (h) h->last_error.clear();
         return CPDLP_OK;
@@ -86,6 +87,12 @@ int cpdlp_create(int32_t device, cpdlp_handle** out) {
         CK(cudaSetDevice(device));
         CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
         CK(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, device));
+        // keep up to 16 GiB of freed stream-ordered memory in this process's
+        // pool instead of returning it to the driver at every synchronisation
+        cudaMemPool_t pool;
+        CK(cudaDeviceGetDefaultMemPool(&pool, device));
+        uint64_t keep = 16ull << 30;
+        CK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
     });
     if (rc != CPDLP_OK) {
         delete h;
@@ -166,7 +173,6 @@ int cpdlp_spmv(cpdlp_handle* h, const cpdlp_matrix* A, const void* b, void* c, d
     return guarded(h, [&] {
         matrix_spmv(*H(h), *reinterpret_cast<const Matrix*>(A), b, c, alpha, beta);
         CK(cudaStreamSynchronize(h->stream));
-        check_tile_error(h->stream);
     });
 }
 
@@ -334,6 +340,57 @@ int cpdlp_batch_solve(cpdlp_handle* h, int64_t count, const cpdlp_lp* lps,
     NEED(h);
     if (count < 0 || (count > 0 && (!lps || !params))) return CPDLP_ERR_ARGUMENT;
     return guarded(h, [&] { batch_solve(*H(h), count, lps, params, x_out, y_out, stats); });
+}
+
+int cpdlp_submit(cpdlp_handle* h, int64_t count, const cpdlp_lp* lps, const cpdlp_params* params,
+                 const double* reltol, const double* const* x0, const double* const* y0,
+                 cpdlp_job** out) {
+    NEED(h);
+    if (!out) return CPDLP_ERR_ARGUMENT;
+    *out = nullptr;
+    return guarded(h, [&] {
+        *out = reinterpret_cast<cpdlp_job*>(job_submit(*H(h), count, lps, params, reltol, x0, y0));
+    });
+}
+
+int cpdlp_poll(cpdlp_handle* h, cpdlp_job* job, int32_t* done) {
+    NEED(h);
+    if (!job || !done) return CPDLP_ERR_ARGUMENT;
+    return guarded(h, [&] { *done = job_poll(reinterpret_cast<Job*>(job)) ? 1 : 0; });
+}
+
+int cpdlp_wait(cpdlp_handle* h, cpdlp_job* job) {
+    NEED(h);
+    if (!job) return CPDLP_ERR_ARGUMENT;
+    return guarded(h, [&] { job_wait(reinterpret_cast<Job*>(job)); });
+}
+
+int cpdlp_cancel(cpdlp_handle* h, cpdlp_job* job) {
+    NEED(h);
+    if (!job) return CPDLP_ERR_ARGUMENT;
+    return guarded(h, [&] { job_cancel(reinterpret_cast<Job*>(job)); });
+}
+
+int cpdlp_collect(cpdlp_handle* h, cpdlp_job* job, double* const* x_out, double* const* y_out,
+                  cpdlp_stats* stats) {
+    NEED(h);
+    if (!job) return CPDLP_ERR_ARGUMENT;
+    return guarded(h, [&] { job_collect(reinterpret_cast<Job*>(job), x_out, y_out, stats); });
+}
+
+int64_t cpdlp_job_count(const cpdlp_job* job) {
+    return job ? job_count(reinterpret_cast<const Job*>(job)) : -1;
+}
+
+int cpdlp_job_destroy(cpdlp_job* job) {
+    if (!job) return CPDLP_ERR_ARGUMENT;
+    job_destroy(reinterpret_cast<Job*>(job));
+    return CPDLP_OK;
+}
+
+int64_t cpdlp_batch_footprint(int64_t count, const cpdlp_lp* lps, const cpdlp_params* params) {
+    if (count < 0 || (count > 0 && !lps)) return -1;
+    return batch_footprint(count, lps, params);
 }
 
 }  // extern "C"

@@ -1,21 +1,31 @@
 // batch.cu -- many independent LPs in one persistent launch.
 //
-// The LPs are concatenated block-diagonally on the host and preprocessed once
-// by the single-LP device pipeline: Ruiz and Pock-Chambolle scaling work on
-// rows and columns, so the scaling of the concatenation equals the scaling of
-// each LP.  The tile partitions are then rebuilt so that no tile crosses an LP
-// boundary.  One CTA solves one LP at a time and takes the next LP from an
-// atomic counter when it finishes: power method (linalg.jl:86-96), primal
-// weight (step_size.jl:29-40), then blocks of check_every fused PDHG steps
-// (pdlp.jl:96-136) with the four-iterate KKT check, restart and termination
-// logic (pdlp.jl:138-196, restart.jl:40-57, termination.jl:89-101) run by the
-// CTA itself, thread 0 taking the FP64 decisions.  Every loop is bounded by
-// max_kkt_passes and the time limit; no CTA waits on another.
+// The LPs of a job are concatenated block-diagonally on the host and
+// preprocessed once by the single-LP device pipeline: Ruiz and Pock-Chambolle
+// scaling work on rows and columns, so the scaling of the concatenation equals
+// the scaling of each LP.  The tile partitions are rebuilt so that no tile
+// crosses an LP boundary.  One CTA solves one LP at a time and takes the next
+// LP from an atomic counter over a largest-first order when it finishes: power
+// method (linalg.jl:86-96), primal weight (step_size.jl:29-40), then blocks of
+// check_every fused PDHG steps (pdlp.jl:96-136) with the four-iterate KKT
+// check, restart and termination logic (pdlp.jl:138-196, restart.jl:40-57,
+// termination.jl:89-101) run by the CTA itself, thread 0 taking the FP64
+// decisions.  Every loop is bounded by the LP's pass limit and time limit; no
+// CTA waits on another.
 //
-// The solve(milp, algo) semantics per LP are those of the single-LP path
-// (common.jl:186-209) except that no error history is recorded.
+// An LP's arithmetic depends only on the LP and the tile size (its tiles, the
+// thread that owns each row, the order of every sum), never on the other LPs
+// of the job or on which CTA runs it, so an LP gives the same result alone and
+// in any mix.
+//
+// The per-LP semantics are those of solve(milp, algo) (common.jl:186-209)
+// except that no error history is recorded.  With FP32 iterates, LPs whose
+// target tolerance is below the FP32 phase's tolerance continue in a second,
+// FP64 job phase warm-started from the FP32 solution (the refinement of
+// cpdlp_solve, batched).
 #include <algorithm>
 #include <memory>
+#include <numeric>
 #include <type_traits>
 
 #include "batch.cuh"
@@ -28,28 +38,35 @@ namespace {
 
 constexpr int BW = TILE_WARPS;  // warps per CTA
 constexpr int BT = BW * 32;
+constexpr int BATCH_ITEMS = 4;  // default nonzeros per lane of a short tile (128-nonzero tiles)
+constexpr int BATCH_RPL = 1;    // rows per lane: short tiles of at most 32 rows
+// FP32 iterates whose relative KKT error has not halved over this many checks
+// hand the LP to the FP64 phase (warm-started from where they stopped)
+constexpr int64_t FP32_STALL_CHECKS = 30;
+#ifndef CPDLP_BATCH_MINB
+#define CPDLP_BATCH_MINB 2      // resident CTAs per SM the solve kernel is compiled for
+#endif
 
 struct BatchLP {
     int32_t m, n, row_off, col_off;
     int32_t a_t0, a_t1, a_l0, a_l1;
     int32_t at_t0, at_t1, at_l0, at_l1;
     int32_t a_lid0, a_lid1, at_lid0, at_lid1;
-    int32_t zero_cost, pad;
-    double power_tol;
-    int64_t power_maxiter;
+    int32_t zero_cost, warm;
+    double power_tol, reltol, time_limit;
+    int64_t power_maxiter, max_passes;
+    int64_t stall_passes;  // > 0: stop when the error has not halved for this many passes
 };
 
 struct BatchResult {
     cpdlp_kkt_errors err;
     int64_t kkt_passes, outer, inner, total, power_iterations;
     double eta, omega, eta_sum, time_elapsed;
-    int32_t status, restart_from_avg;
+    int32_t status, restart_from_avg, stalled, pad;
 };
 
 struct BatchParams {
     int32_t algorithm, check_every;
-    int64_t max_kkt_passes;
-    double termination_reltol, time_limit;
     double invnorm_scaling, primal_weight_damping, zero_tol;
     double sufficient_decay, necessary_decay, artificial_decay;
 };
@@ -60,21 +77,57 @@ struct BatchArgs {
     const T *c, *lv, *uv, *lc, *uc;
     const double *invD1, *invD2, *D1, *D2;
     T *x[2], *y[2], *xa[2], *ya[2], *xr, *yr, *xbar;
-    const double* x_start;
+    const double* theta;     // per LP: the power method's estimate of |A|^2
+    const int64_t* power_iters;
+    const double* x_init;    // warm starts (original units) or null
+    const double* y_init;
     const BatchLP* lps;
+    const int32_t* order;    // queue order of the LPs
     BatchResult* res;
     double* out_x;
     double* out_y;
-    double* red;      // per CTA: 32 doubles
     double* longA;    // row-side long-row terms (2 per long row of A)
     double* longAt;   // column-side long-row terms (3 per long row of A')
-    StepCoef<T>* coef;  // per CTA
     int* next;
+    const int* cancel;
     int32_t count;
     BatchParams prm;
 };
 
+// The power method of every LP, in FP64 arithmetic over the matrix values as
+// stored (V = float or double: the product of the stored values and FP64
+// vectors is exact before rounding), so that FP32 iterates step with an
+// estimate of |A|^2 as accurate as the FP64 path's.
+template <class V>
+struct PowerArgs {
+    CsrView<V, double> A, At;
+    double *x, *Atx, *s;     // x (n), A'Ax (n), Ax (m)
+    const double* x_start;   // power-method start vectors
+    const BatchLP* lps;
+    const int32_t* order;
+    double* theta;
+    int64_t* iters;
+    double* longAt;
+    int* next;
+    int32_t count;
+};
+
+// per-CTA control state of the LP in progress (shared memory; thread 0 writes
+// the decisions, every thread reads them after a barrier)
+struct BatchCtl {
+    BatchLP L;
+    cpdlp_kkt_errors e[4], e_cand, e_restart, e_sol;
+    double omega, pscale, dscale;
+    uint64_t t_start;
+    int64_t passes, outer, inner, total, power_it;
+    double best_rel;       // smallest relative error at a halving mark
+    int64_t mark;          // passes at that mark
+    int32_t lp, status, flag, from_avg, restart_valid, cancelled, stop, stalled;
+};
+
 // -- block-wide helpers ---------------------------------------------------------
+// Sums Q per-thread values over the CTA in a fixed order (warp trees, then the
+// warps in order); every thread receives the sums.
 template <int Q>
 __device__ __forceinline__ void block_sum(double (&v)[Q], double* sh) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -97,17 +150,19 @@ __device__ __forceinline__ void block_sum(double (&v)[Q], double* sh) {
     __syncthreads();
 }
 
-// the LP's tiles of one matrix, warps striding over its tasks
-template <int ITEMS, class T, class Epi>
-__device__ __forceinline__ void lp_tiles(const CsrView<T, T>& V, int t0, int t1, int l0, int l1,
+// the LP's tiles of one matrix, warps striding over its tasks; the vectors are
+// gathered with coherent loads (this kernel rewrites them between products)
+template <int ITEMS, class V, class T, class Epi>
+__device__ __forceinline__ void lp_tiles(const CsrView<V, T>& A, int t0, int t1, int l0, int l1,
                                          const T* xin, Epi& epi, typename Epi::Acc& acc,
                                          T* prod) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const VecSet<T, 1> xs{{xin}};
-    for (int t = l0 + w; t < l1; t += BW) long_piece<ITEMS, 1>(V, xs, epi, acc, V.ltasks[t], lane);
+    const VecSet<T, 1, true> xs{{xin}};
+    for (int t = l0 + w; t < l1; t += BW) long_piece<ITEMS, 1>(A, xs, epi, acc, A.ltasks[t], lane);
     for (int t = t0 + w; t < t1; t += BW) {
-        const int4 tk = V.tasks[t];
-        short_tile<ITEMS, 1>(V, xs, epi, acc, tk.x, tk.y, tk.z, tk.w, lane, prod + w * 32 * ITEMS);
+        const int4 tk = A.tasks[t];
+        short_tile<ITEMS, 1, V, T, Epi, true, BATCH_RPL>(A, xs, epi, acc, tk.x, tk.y, tk.z, tk.w,
+                                                       lane, prod + w * 32 * ITEMS);
     }
 }
 
@@ -118,345 +173,380 @@ __device__ __forceinline__ double abs_err(const cpdlp_kkt_errors& e, double w) {
     return sqrt((w * w) * (e.primal * e.primal) + (1.0 / (w * w)) * (e.dual * e.dual) +
                 e.gap * e.gap);
 }
+__device__ __forceinline__ bool should_restart(const BatchParams& p, double ac, double ar,
+                                               double acl, int64_t inner, int64_t total) {
+    return (ac <= p.sufficient_decay * ar) || ((ac <= p.necessary_decay * ar) && (ac > acl)) ||
+           ((double)inner >= p.artificial_decay * (double)total);
+}
 
+// KKT errors of (xv, yv) (errors.jl:65-109) into *out (thread 0); all threads
+// take part; ends with a barrier
 template <int ITEMS, class T>
-__global__ void __launch_bounds__(BT) k_batch_pdlp(BatchArgs<T> g) {
-    __shared__ T prod[BW * 32 * ITEMS];
-    __shared__ double sh[BW * 8 + 8];
-    __shared__ int s_lp;
-    __shared__ double s_eta, s_omega, s_eta_sum, s_pscale, s_dscale;
-    __shared__ T s_theta, s_inv;
-    __shared__ int s_flag;
-    __shared__ cpdlp_kkt_errors s_e[4];
-    StepCoef<T>* coef = g.coef + blockIdx.x;
-    double* red = g.red + (size_t)blockIdx.x * 32;
+__device__ __forceinline__ void lp_kkt(const BatchArgs<T>& g, const BatchCtl& C, const T* xv,
+                                       const T* yv, cpdlp_kkt_errors* out, T* prod, double* sh) {
+    const BatchLP& L = C.L;
+    double rs[2], cs[3];
+    {
+        KktRowEpi<T, 1> re;
+        re.lc = g.lc; re.uc = g.uc; re.invD1 = g.invD1; re.y[0] = yv;
+        re.block_out = nullptr; re.long_out = g.longA;
+        typename KktRowEpi<T, 1>::Acc a;
+        re.init(a);
+        lp_tiles<ITEMS, T>(g.A, L.a_t0, L.a_t1, L.a_l0, L.a_l1, xv, re, a, prod);
+        block_sum<2>(a.v, sh);
+        rs[0] = a.v[0]; rs[1] = a.v[1];
+    }
+    {
+        KktColEpi<T, 1> ce;
+        ce.c = g.c; ce.lv = g.lv; ce.uv = g.uv; ce.invD2 = g.invD2; ce.x[0] = xv;
+        ce.block_out = nullptr; ce.long_out = g.longAt;
+        typename KktColEpi<T, 1>::Acc a;
+        ce.init(a);
+        lp_tiles<ITEMS, T>(g.At, L.at_t0, L.at_t1, L.at_l0, L.at_l1, yv, ce, a, prod);
+        block_sum<3>(a.v, sh);
+        cs[0] = a.v[0]; cs[1] = a.v[1]; cs[2] = a.v[2];
+    }
+    if (threadIdx.x == 0) {
+        for (int l = L.a_lid0; l < L.a_lid1; l++) {
+            rs[0] += g.longA[(size_t)l * 2];
+            rs[1] += g.longA[(size_t)l * 2 + 1];
+        }
+        for (int l = L.at_lid0; l < L.at_lid1; l++) {
+            cs[0] += g.longAt[(size_t)l * 3];
+            cs[1] += g.longAt[(size_t)l * 3 + 1];
+            cs[2] += g.longAt[(size_t)l * 3 + 2];
+        }
+        out->primal = sqrt(rs[0]);
+        out->primal_scale = C.pscale;
+        out->dual = sqrt(cs[0]);
+        out->dual_scale = C.dscale;
+        out->gap = fabs((cs[2] + rs[1]) + cs[1]);
+        out->gap_scale = (1.0 + fabs(rs[1] + cs[1])) + fabs(cs[2]);
+    }
+    __syncthreads();  // the long-row terms are rewritten by the next pass
+}
+
+// solve(milp, algo) for the LP in C (dequeued by thread 0)
+template <int ITEMS, class T>
+__device__ __forceinline__ void solve_one(const BatchArgs<T>& g, BatchCtl& C, T* prod,
+                                          double* sh) {
     const int tid = threadIdx.x;
     const bool pdlp = g.prm.algorithm == CPDLP_ALGO_PDLP;
-    for (int iter_guard = 0; iter_guard < g.count; iter_guard++) {
-        if (tid == 0) s_lp = atomicAdd(g.next, 1);
+    const int c0 = C.L.col_off, c1 = c0 + C.L.n, r0 = C.L.row_off, r1 = r0 + C.L.m;
+    // ---- step size from the power method's estimate (step_size.jl:22-27),
+    // scales and primal weight (step_size.jl:29-40, errors.jl:79-85)
+    const double eta = g.prm.invnorm_scaling * (1.0 / sqrt(g.theta[C.lp]));
+    double omega;
+    {
+        double q[4] = {0, 0, 0, 0};
+        for (int i = r0 + tid; i < r1; i += BT) {
+            const double cb = combine((double)g.lc[i], (double)g.uc[i]);
+            const double sv = g.invD1[i] * cb;
+            q[0] += sv * sv;
+            q[1] += cb * cb;
+        }
+        for (int j = c0 + tid; j < c1; j += BT) {
+            const double cj = (double)g.c[j];
+            const double sv = g.invD2[j] * cj;
+            q[2] += sv * sv;
+            q[3] += cj * cj;
+        }
+        block_sum<4>(q, sh);
+        const double cn = sqrt(q[3]), bn = sqrt(q[1]);
+        omega = !pdlp ? 1.0 : (cn > g.prm.zero_tol && bn > g.prm.zero_tol) ? cn / bn : 1.0;
+        if (tid == 0) {
+            C.pscale = 1.0 + sqrt(q[0]);
+            C.dscale = 1.0 + sqrt(q[2]);
+            C.power_it = g.power_iters[C.lp];
+        }
+    }
+    double eta_sum = 0.0;
+    // ---- initial iterates: sol = precondition(sol_init) (preconditioning.jl:45-51),
+    // sol_last = 0, avg = sol, avg_last = 0, restart = sol (pdlp.jl:45-67)
+    for (int j = c0 + tid; j < c1; j += BT) {
+        const T v = (C.L.warm && g.x_init) ? (T)__ddiv_rn(g.x_init[j], g.D2[j]) : T(0);
+        g.x[0][j] = v; g.x[1][j] = T(0); g.xa[0][j] = v; g.xa[1][j] = T(0);
+        g.xr[j] = v; g.xbar[j] = T(0);
+    }
+    for (int i = r0 + tid; i < r1; i += BT) {
+        const T v = (C.L.warm && g.y_init) ? (T)__ddiv_rn(g.y_init[i], g.D1[i]) : T(0);
+        g.y[0][i] = v; g.y[1][i] = T(0); g.ya[0][i] = v; g.ya[1][i] = T(0);
+        g.yr[i] = v;
+    }
+    int cur = 0;
+    if (tid == 0) {
+        C.passes = C.outer = C.inner = C.total = 0;
+        C.best_rel = INFINITY;
+        C.mark = 0;
+        C.stalled = 0;
+        C.restart_valid = 0;
+        C.from_avg = 0;
+        C.status = CPDLP_STILL_RUNNING;
+        C.stop = 0;
+        C.omega = omega;
+    }
+    __syncthreads();
+    if (C.L.m == 0 && C.L.zero_cost) {  // early exit (common.jl:194-198)
+        for (int j = c0 + tid; j < c1; j += BT) g.x[0][j] = proj_box(T(0), g.lv[j], g.uv[j]);
+        if (tid == 0) {
+            C.status = CPDLP_OPTIMAL;
+            C.stop = 1;
+            const double nan = __longlong_as_double(0x7ff8000000000000ll);
+            C.e_sol = cpdlp_kkt_errors{nan, nan, nan, nan, nan, nan};
+        }
         __syncthreads();
-        const int k = s_lp;
+    }
+    const double tlim_ns = C.L.time_limit * 1e9;
+    while (!C.stop) {
+        // ---- check_every steps (pdlp.jl:96-124, averaging :126-136)
+        for (int st = 0; st < g.prm.check_every; st++) {
+            const double sigma = eta * omega;
+            StepCoef<T> k;
+            k.tau = (T)(eta / omega);
+            k.sigma = (T)sigma;
+            k.inv_sigma = (T)(1.0 / sigma);
+            k.a = (T)(eta / (eta + eta_sum));
+            k.b = (T)(eta_sum / (eta + eta_sum));
+            if (pdlp) eta_sum += eta;
+            const int o = cur, nw = cur ^ 1;
+            {
+                PrimalEpi<T, true> pe{g.x[o], g.c, g.lv, g.uv, g.x[nw], g.xbar, g.xa[o], g.xa[nw],
+                                      {k}, pdlp ? 1 : 0};
+                NoAcc a;
+                lp_tiles<ITEMS, T>(g.At, C.L.at_t0, C.L.at_t1, C.L.at_l0, C.L.at_l1, g.y[o], pe, a, prod);
+            }
+            __syncthreads();
+            {
+                DualEpi<T, true> de{g.y[o], g.lc, g.uc, g.y[nw], g.ya[o], g.ya[nw], {k}, pdlp ? 1 : 0};
+                NoAcc a;
+                lp_tiles<ITEMS, T>(g.A, C.L.a_t0, C.L.a_t1, C.L.a_l0, C.L.a_l1, g.xbar, de, a, prod);
+            }
+            __syncthreads();
+            cur ^= 1;
+        }
+        // ---- KKT errors of sol, avg, sol_last, avg_last (errors.jl:65-109)
+        const int nv = pdlp ? 4 : 1;
+        for (int p = 0; p < nv; p++) {
+            const T* xv = p == 0 ? g.x[cur] : p == 1 ? g.xa[cur] : p == 2 ? g.x[cur ^ 1] : g.xa[cur ^ 1];
+            const T* yv = p == 0 ? g.y[cur] : p == 1 ? g.ya[cur] : p == 2 ? g.y[cur ^ 1] : g.ya[cur ^ 1];
+            lp_kkt<ITEMS, T>(g, C, xv, yv, &C.e[p], prod, sh);
+        }
+        // ---- termination (common.jl:218-231) and restart decision (pdlp.jl:138-170)
+        if (tid == 0) {
+            C.passes += g.prm.check_every;
+            if (pdlp) {
+                C.inner += g.prm.check_every;
+                C.total += g.prm.check_every;
+            }
+            C.e_sol = C.e[0];
+            const double elapsed = (double)(global_ns() - C.t_start);
+            int32_t stt = CPDLP_STILL_RUNNING;
+            if (rel_err(C.e_sol) <= C.L.reltol) stt = CPDLP_OPTIMAL;
+            else if (elapsed >= tlim_ns) stt = CPDLP_TIME_LIMIT;
+            else if (C.passes >= C.L.max_passes) stt = CPDLP_ITERATION_LIMIT;
+            // stall: the relative error has not halved over stall_passes passes
+            const double rel = rel_err(C.e_sol);
+            if (rel < 0.5 * C.best_rel) {
+                C.best_rel = rel;
+                C.mark = C.passes;
+            } else if (stt == CPDLP_STILL_RUNNING && C.L.stall_passes > 0 &&
+                       C.passes - C.mark >= C.L.stall_passes) {
+                stt = CPDLP_ITERATION_LIMIT;
+                C.stalled = 1;
+            }
+            const int cancelled = *(volatile const int*)g.cancel;
+            int flag = 0;
+            if (stt == CPDLP_STILL_RUNNING && !cancelled && pdlp) {
+                const double w = C.omega;
+                if (abs_err(C.e[0], w) < abs_err(C.e[1], w)) { C.from_avg = 0; C.e_cand = C.e[0]; }
+                else { C.from_avg = 1; C.e_cand = C.e[1]; }
+                C.e[2] = (abs_err(C.e[2], w) < abs_err(C.e[3], w)) ? C.e[2] : C.e[3];
+                flag = 2;  // the restart point's errors are needed first
+                if (C.restart_valid)
+                    flag = should_restart(g.prm, abs_err(C.e_cand, w), abs_err(C.e_restart, w),
+                                          abs_err(C.e[2], w), C.inner, C.total) ? 3 : 0;
+            }
+            C.status = stt;
+            C.cancelled = cancelled;
+            C.stop = (stt != CPDLP_STILL_RUNNING) || cancelled;
+            C.flag = flag;
+        }
         __syncthreads();
-        if (k >= g.count) break;
-        const BatchLP L = g.lps[k];
-        const uint64_t t_start = global_ns();
-        const int c0 = L.col_off, c1 = L.col_off + L.n, r0 = L.row_off, r1 = L.row_off + L.m;
+        int flag = C.flag;
+        __syncthreads();
+        if (flag == 2) {
+            // errors of the initial restart point (sol_restart = the start)
+            lp_kkt<ITEMS, T>(g, C, g.xr, g.yr, &C.e_restart, prod, sh);
+            if (tid == 0) {
+                C.restart_valid = 1;
+                const double w = C.omega;
+                C.flag = should_restart(g.prm, abs_err(C.e_cand, w), abs_err(C.e_restart, w),
+                                        abs_err(C.e[2], w), C.inner, C.total) ? 3 : 0;
+            }
+            __syncthreads();
+            flag = C.flag;
+            __syncthreads();
+        }
+        if (flag == 3) {
+            // restart! + primal_weight_update! (pdlp.jl:172-196, step_size.jl:58-75)
+            const T* cx = C.from_avg ? g.xa[cur] : g.x[cur];
+            const T* cy = C.from_avg ? g.ya[cur] : g.y[cur];
+            double q[2] = {0.0, 0.0};
+            for (int j = c0 + tid; j < c1; j += BT) {
+                const double d = (double)cx[j] - (double)g.xr[j];
+                q[0] += d * d;
+            }
+            for (int i = r0 + tid; i < r1; i += BT) {
+                const double d = (double)cy[i] - (double)g.yr[i];
+                q[1] += d * d;
+            }
+            block_sum<2>(q, sh);
+            eta_sum = 0.0;
+            const double dx = sqrt(q[0]), dy = sqrt(q[1]), th = g.prm.primal_weight_damping;
+            if (dx > g.prm.zero_tol && dy > g.prm.zero_tol)
+                omega = exp(th * log(dy / dx) + (1.0 - th) * log(omega));
+            for (int j = c0 + tid; j < c1; j += BT) {
+                const T v = cx[j];
+                g.x[cur][j] = v;
+                g.xr[j] = v;
+                g.xa[cur][j] = T(0);
+            }
+            for (int i = r0 + tid; i < r1; i += BT) {
+                const T v = cy[i];
+                g.y[cur][i] = v;
+                g.yr[i] = v;
+                g.ya[cur][i] = T(0);
+            }
+            if (tid == 0) {
+                C.omega = omega;
+                C.e_restart = C.e_cand;
+                C.outer += 1;
+                C.inner = 0;
+            }
+            __syncthreads();
+        }
+    }
+    // ---- get_solution (common.jl:233-235): unscaled, double
+    for (int j = c0 + tid; j < c1; j += BT) g.out_x[j] = g.D2[j] * (double)g.x[cur][j];
+    for (int i = r0 + tid; i < r1; i += BT) g.out_y[i] = g.D1[i] * (double)g.y[cur][i];
+    if (tid == 0) {
+        BatchResult R;
+        R.err = C.e_sol;
+        R.kkt_passes = C.passes;
+        R.outer = C.outer;
+        R.inner = C.inner;
+        R.total = C.total;
+        R.power_iterations = C.power_it;
+        R.eta = eta;
+        R.omega = omega;
+        R.eta_sum = eta_sum;
+        R.time_elapsed = (double)(global_ns() - C.t_start) * 1e-9;
+        R.status = C.status;
+        R.restart_from_avg = C.from_avg;
+        R.stalled = C.stalled;
+        R.pad = 0;
+        g.res[C.lp] = R;
+    }
+}
+
+// an LP dequeued after a cancellation: not started
+template <class T>
+__device__ __forceinline__ void skip_one(const BatchArgs<T>& g, const BatchCtl& C) {
+    const int tid = threadIdx.x;
+    for (int j = C.L.col_off + tid; j < C.L.col_off + C.L.n; j += BT) g.out_x[j] = 0.0;
+    for (int i = C.L.row_off + tid; i < C.L.row_off + C.L.m; i += BT) g.out_y[i] = 0.0;
+    if (tid == 0) {
         BatchResult R;
         memset(&R, 0, sizeof(R));
-        // ---- power method on A'A (linalg.jl:86-96): buffers xa[1] (x), xbar (Ax), ya[1] (A x)
-        T* px = g.xa[1];
-        T* pAx = g.xbar;
-        T* ps = g.ya[1];
-        for (int j = c0 + tid; j < c1; j += BT) px[j] = (T)g.x_start[j];
+        const double nan = __longlong_as_double(0x7ff8000000000000ll);
+        R.err = cpdlp_kkt_errors{nan, nan, nan, nan, nan, nan};
+        R.status = CPDLP_STILL_RUNNING;
+        g.res[C.lp] = R;
+    }
+}
+
+// powm! on A'A with IterativeSolvers' stopping rule (linalg.jl:86-96): one CTA
+// per LP from a queue, FP64 vectors
+template <int ITEMS, class V>
+__global__ void __launch_bounds__(BT) k_batch_power(PowerArgs<V> g) {
+    __shared__ double prod[BW * 32 * ITEMS];
+    __shared__ double sh[BW * 8 + 8];
+    __shared__ BatchLP L;
+    __shared__ int s_lp;
+    const int tid = threadIdx.x;
+    for (int guard = 0; guard <= g.count; guard++) {
+        if (tid == 0) {
+            const int q = atomicAdd(g.next, 1);
+            s_lp = q < g.count ? g.order[q] : -1;
+            if (s_lp >= 0) L = g.lps[s_lp];
+        }
         __syncthreads();
-        double theta_d = 0.0, residual = INFINITY;
+        if (s_lp < 0) break;
+        const int c0 = L.col_off, c1 = c0 + L.n;
+        for (int j = c0 + tid; j < c1; j += BT) g.x[j] = g.x_start[j];
+        __syncthreads();
+        double theta = 0.0, residual = INFINITY;
         int64_t it = 0;
         while (!(it > L.power_maxiter || residual <= L.power_tol)) {
             {
-                StoreEpi<T> se{ps};
+                StoreEpi<double> se{g.s};
                 NoAcc a;
-                lp_tiles<ITEMS, T>(g.A, L.a_t0, L.a_t1, L.a_l0, L.a_l1, px, se, a, prod);
+                lp_tiles<ITEMS, V, double>(g.A, L.a_t0, L.a_t1, L.a_l0, L.a_l1, g.x, se, a, prod);
             }
             __syncthreads();
+            double th, inv;
             {
-                PowerEpi<T> pe{px, pAx, red, g.longAt};
-                typename PowerEpi<T>::Acc a;
+                PowerEpi<double> pe{g.x, g.Atx, nullptr, g.longAt};
+                PowerEpi<double>::Acc a;
                 pe.init(a);
-                lp_tiles<ITEMS, T>(g.At, L.at_t0, L.at_t1, L.at_l0, L.at_l1, ps, pe, a, prod);
+                lp_tiles<ITEMS, V, double>(g.At, L.at_t0, L.at_t1, L.at_l0, L.at_l1, g.s, pe, a, prod);
                 block_sum<2>(a.v, sh);
-                if (tid == 0) {
-                    double s0 = a.v[0], s1 = a.v[1];
-                    for (int l = L.at_lid0; l < L.at_lid1; l++) {
-                        s0 += g.longAt[(size_t)l * 2];
-                        s1 += g.longAt[(size_t)l * 2 + 1];
-                    }
-                    s_theta = (T)s0;
-                    const T nrm = (T)sqrt(s1);
-                    s_inv = T(1) / nrm;
+                double s0 = a.v[0], s1 = a.v[1];
+                for (int l = L.at_lid0; l < L.at_lid1; l++) {
+                    s0 += g.longAt[(size_t)l * 2];
+                    s1 += g.longAt[(size_t)l * 2 + 1];
                 }
-                __syncthreads();
+                th = s0;
+                inv = 1.0 / sqrt(s1);
             }
             double racc[1] = {0.0};
-            const T th = s_theta, inv = s_inv;
             for (int j = c0 + tid; j < c1; j += BT) {
-                const T r = add_rn(mul_rn(-th, px[j]), pAx[j]);
-                racc[0] += (double)r * (double)r;
-                px[j] = mul_rn(pAx[j], inv);
+                const double r = add_rn(mul_rn(-th, g.x[j]), g.Atx[j]);
+                racc[0] += r * r;
+                g.x[j] = mul_rn(g.Atx[j], inv);
             }
-            block_sum<1>(racc, sh);
+            block_sum<1>(racc, sh);  // its barriers also order the long-row terms' reuse
             residual = sqrt(racc[0]);
-            theta_d = (double)th;
+            theta = th;
             it++;
         }
-        R.power_iterations = it;
-        // ---- scales and primal weight (errors.jl:79-85, step_size.jl:29-40)
-        {
-            double q[4] = {0, 0, 0, 0};
-            for (int i = r0 + tid; i < r1; i += BT) {
-                const double cb = combine((double)g.lc[i], (double)g.uc[i]);
-                const double sv = g.invD1[i] * cb;
-                q[0] += sv * sv;
-                q[1] += cb * cb;
-            }
-            for (int j = c0 + tid; j < c1; j += BT) {
-                const double cj = (double)g.c[j];
-                const double sv = g.invD2[j] * cj;
-                q[2] += sv * sv;
-                q[3] += cj * cj;
-            }
-            block_sum<4>(q, sh);
-            if (tid == 0) {
-                s_pscale = 1.0 + sqrt(q[0]);
-                s_dscale = 1.0 + sqrt(q[2]);
-                s_eta = g.prm.invnorm_scaling * (1.0 / sqrt(theta_d));
-                const double cn = sqrt(q[3]), bn = sqrt(q[1]);
-                s_omega = !pdlp ? 1.0
-                        : (cn > g.prm.zero_tol && bn > g.prm.zero_tol) ? cn / bn : 1.0;
-                s_eta_sum = 0.0;
-            }
-        }
-        // ---- initial iterates: x = 0, y = 0 (solve(milp, algo), common.jl:203-209)
-        for (int j = c0 + tid; j < c1; j += BT) {
-            g.x[0][j] = T(0); g.x[1][j] = T(0); g.xa[0][j] = T(0); g.xa[1][j] = T(0);
-            g.xr[j] = T(0); g.xbar[j] = T(0);
-        }
-        for (int i = r0 + tid; i < r1; i += BT) {
-            g.y[0][i] = T(0); g.y[1][i] = T(0); g.ya[0][i] = T(0); g.ya[1][i] = T(0);
-            g.yr[i] = T(0);
+        if (tid == 0) {
+            g.theta[s_lp] = theta;
+            g.iters[s_lp] = it;
         }
         __syncthreads();
-        int cur = 0;
-        int32_t status = CPDLP_STILL_RUNNING;
-        int32_t from_avg = 0;
-        int64_t passes = 0, outer = 0, inner = 0, total = 0;
-        bool restart_valid = false;
-        cpdlp_kkt_errors e_cand{}, e_restart{}, e_sol{};
-        if (L.m == 0 && L.zero_cost) {  // common.jl:194-198
-            for (int j = c0 + tid; j < c1; j += BT) g.x[0][j] = proj_box(T(0), g.lv[j], g.uv[j]);
-            status = CPDLP_OPTIMAL;
-        }
-        const double tlim_ns = g.prm.time_limit * 1e9;
-        while (status == CPDLP_STILL_RUNNING) {
-            // ---- check_every steps (pdlp.jl:96-124)
-            for (int st = 0; st < g.prm.check_every; st++) {
-                if (tid == 0) {
-                    const double eta = s_eta, om = s_omega, es = s_eta_sum;
-                    const double sigma = eta * om;
-                    coef->tau = (T)(eta / om);
-                    coef->sigma = (T)sigma;
-                    coef->inv_sigma = (T)(1.0 / sigma);
-                    coef->a = (T)(eta / (eta + es));
-                    coef->b = (T)(es / (eta + es));
-                    if (pdlp) s_eta_sum = es + eta;
-                }
-                __syncthreads();
-                const int o = cur, nw = cur ^ 1;
-                {
-                    PrimalEpi<T> pe{g.x[o], g.c, g.lv, g.uv, g.x[nw], g.xbar, g.xa[o], g.xa[nw],
-                                    coef, pdlp ? 1 : 0};
-                    NoAcc a;
-                    lp_tiles<ITEMS, T>(g.At, L.at_t0, L.at_t1, L.at_l0, L.at_l1, g.y[o], pe, a, prod);
-                }
-                __syncthreads();
-                {
-                    DualEpi<T> de{g.y[o], g.lc, g.uc, g.y[nw], g.ya[o], g.ya[nw], coef, pdlp ? 1 : 0};
-                    NoAcc a;
-                    lp_tiles<ITEMS, T>(g.A, L.a_t0, L.a_t1, L.a_l0, L.a_l1, g.xbar, de, a, prod);
-                }
-                __syncthreads();
-                cur ^= 1;
-            }
-            passes += g.prm.check_every;
-            if (pdlp) {
-                inner += g.prm.check_every;
-                total += g.prm.check_every;
-            }
-            // ---- KKT errors of sol, avg, sol_last, avg_last (errors.jl:65-109)
-            const int nv = pdlp ? 4 : 1;
-            for (int p = 0; p < nv; p++) {
-                const T* xv = p == 0 ? g.x[cur] : p == 1 ? g.xa[cur] : p == 2 ? g.x[cur ^ 1] : g.xa[cur ^ 1];
-                const T* yv = p == 0 ? g.y[cur] : p == 1 ? g.ya[cur] : p == 2 ? g.y[cur ^ 1] : g.ya[cur ^ 1];
-                double rs[2], cs[3];
-                {
-                    KktRowEpi<T, 1> re;
-                    re.lc = g.lc; re.uc = g.uc; re.invD1 = g.invD1; re.y[0] = yv;
-                    re.block_out = red; re.long_out = g.longA;
-                    typename KktRowEpi<T, 1>::Acc a;
-                    re.init(a);
-                    lp_tiles<ITEMS, T>(g.A, L.a_t0, L.a_t1, L.a_l0, L.a_l1, xv, re, a, prod);
-                    block_sum<2>(a.v, sh);
-                    rs[0] = a.v[0]; rs[1] = a.v[1];
-                }
-                {
-                    KktColEpi<T, 1> ce;
-                    ce.c = g.c; ce.lv = g.lv; ce.uv = g.uv; ce.invD2 = g.invD2; ce.x[0] = xv;
-                    ce.block_out = red; ce.long_out = g.longAt;
-                    typename KktColEpi<T, 1>::Acc a;
-                    ce.init(a);
-                    lp_tiles<ITEMS, T>(g.At, L.at_t0, L.at_t1, L.at_l0, L.at_l1, yv, ce, a, prod);
-                    block_sum<3>(a.v, sh);
-                    cs[0] = a.v[0]; cs[1] = a.v[1]; cs[2] = a.v[2];
-                }
-                if (tid == 0) {
-                    for (int l = L.a_lid0; l < L.a_lid1; l++) {
-                        rs[0] += g.longA[(size_t)l * 2];
-                        rs[1] += g.longA[(size_t)l * 2 + 1];
-                    }
-                    for (int l = L.at_lid0; l < L.at_lid1; l++) {
-                        cs[0] += g.longAt[(size_t)l * 3];
-                        cs[1] += g.longAt[(size_t)l * 3 + 1];
-                        cs[2] += g.longAt[(size_t)l * 3 + 2];
-                    }
-                    cpdlp_kkt_errors& e = s_e[p];
-                    e.primal = sqrt(rs[0]);
-                    e.primal_scale = s_pscale;
-                    e.dual = sqrt(cs[0]);
-                    e.dual_scale = s_dscale;
-                    e.gap = fabs((cs[2] + rs[1]) + cs[1]);
-                    e.gap_scale = (1.0 + fabs(rs[1] + cs[1])) + fabs(cs[2]);
-                }
-                __syncthreads();
-            }
-            // ---- termination (common.jl:218-231) and restart (pdlp.jl:138-196)
-            if (tid == 0) {
-                e_sol = s_e[0];
-                const double elapsed = (double)(global_ns() - t_start);
-                int32_t stt = CPDLP_STILL_RUNNING;
-                if (rel_err(e_sol) <= g.prm.termination_reltol) stt = CPDLP_OPTIMAL;
-                else if (elapsed >= tlim_ns) stt = CPDLP_TIME_LIMIT;
-                else if (passes >= g.prm.max_kkt_passes) stt = CPDLP_ITERATION_LIMIT;
-                int flag = 0;
-                if (stt == CPDLP_STILL_RUNNING && pdlp) {
-                    const double w = s_omega;
-                    if (abs_err(s_e[0], w) < abs_err(s_e[1], w)) { from_avg = 0; e_cand = s_e[0]; }
-                    else { from_avg = 1; e_cand = s_e[1]; }
-                    const cpdlp_kkt_errors el = (abs_err(s_e[2], w) < abs_err(s_e[3], w)) ? s_e[2] : s_e[3];
-                    flag = restart_valid ? 1 : 2;  // 2: the restart point's errors are needed first
-                    if (restart_valid) {
-                        const double ac = abs_err(e_cand, w), ar = abs_err(e_restart, w),
-                                     acl = abs_err(el, w);
-                        const bool restart = (ac <= g.prm.sufficient_decay * ar) ||
-                                             ((ac <= g.prm.necessary_decay * ar) && (ac > acl)) ||
-                                             ((double)inner >= g.prm.artificial_decay * (double)total);
-                        flag = restart ? 3 : 0;
-                    }
-                    s_e[2] = el;
-                }
-                status = stt;
-                s_flag = flag;
-                sh[0] = (double)stt;
-            }
-            __syncthreads();
-            status = (int32_t)sh[0];
-            int flag = s_flag;
-            __syncthreads();
-            if (flag == 2) {
-                // errors of the initial restart point (sol_restart = the start)
-                double rs[2], cs[3];
-                {
-                    KktRowEpi<T, 1> re;
-                    re.lc = g.lc; re.uc = g.uc; re.invD1 = g.invD1; re.y[0] = g.yr;
-                    re.block_out = red; re.long_out = g.longA;
-                    typename KktRowEpi<T, 1>::Acc a;
-                    re.init(a);
-                    lp_tiles<ITEMS, T>(g.A, L.a_t0, L.a_t1, L.a_l0, L.a_l1, g.xr, re, a, prod);
-                    block_sum<2>(a.v, sh);
-                    rs[0] = a.v[0]; rs[1] = a.v[1];
-                }
-                {
-                    KktColEpi<T, 1> ce;
-                    ce.c = g.c; ce.lv = g.lv; ce.uv = g.uv; ce.invD2 = g.invD2; ce.x[0] = g.xr;
-                    ce.block_out = red; ce.long_out = g.longAt;
-                    typename KktColEpi<T, 1>::Acc a;
-                    ce.init(a);
-                    lp_tiles<ITEMS, T>(g.At, L.at_t0, L.at_t1, L.at_l0, L.at_l1, g.yr, ce, a, prod);
-                    block_sum<3>(a.v, sh);
-                    cs[0] = a.v[0]; cs[1] = a.v[1]; cs[2] = a.v[2];
-                }
-                if (tid == 0) {
-                    for (int l = L.a_lid0; l < L.a_lid1; l++) {
-                        rs[0] += g.longA[(size_t)l * 2];
-                        rs[1] += g.longA[(size_t)l * 2 + 1];
-                    }
-                    for (int l = L.at_lid0; l < L.at_lid1; l++) {
-                        cs[0] += g.longAt[(size_t)l * 3];
-                        cs[1] += g.longAt[(size_t)l * 3 + 1];
-                        cs[2] += g.longAt[(size_t)l * 3 + 2];
-                    }
-                    e_restart.primal = sqrt(rs[0]);
-                    e_restart.primal_scale = s_pscale;
-                    e_restart.dual = sqrt(cs[0]);
-                    e_restart.dual_scale = s_dscale;
-                    e_restart.gap = fabs((cs[2] + rs[1]) + cs[1]);
-                    e_restart.gap_scale = (1.0 + fabs(rs[1] + cs[1])) + fabs(cs[2]);
-                    restart_valid = true;
-                    const double w = s_omega;
-                    const double ac = abs_err(e_cand, w), ar = abs_err(e_restart, w),
-                                 acl = abs_err(s_e[2], w);
-                    const bool restart = (ac <= g.prm.sufficient_decay * ar) ||
-                                         ((ac <= g.prm.necessary_decay * ar) && (ac > acl)) ||
-                                         ((double)inner >= g.prm.artificial_decay * (double)total);
-                    s_flag = restart ? 3 : 0;
-                }
-                __syncthreads();
-                flag = s_flag;
-                __syncthreads();
-            }
-            if (flag == 3) {
-                // restart! + primal_weight_update! (pdlp.jl:172-196, step_size.jl:58-75)
-                const T* cx = from_avg ? g.xa[cur] : g.x[cur];
-                const T* cy = from_avg ? g.ya[cur] : g.y[cur];
-                double q[2] = {0.0, 0.0};
-                for (int j = c0 + tid; j < c1; j += BT) {
-                    const double d = (double)cx[j] - (double)g.xr[j];
-                    q[0] += d * d;
-                }
-                for (int i = r0 + tid; i < r1; i += BT) {
-                    const double d = (double)cy[i] - (double)g.yr[i];
-                    q[1] += d * d;
-                }
-                block_sum<2>(q, sh);
-                if (tid == 0) {
-                    s_eta_sum = 0.0;
-                    const double dx = sqrt(q[0]), dy = sqrt(q[1]), th = g.prm.primal_weight_damping;
-                    if (dx > g.prm.zero_tol && dy > g.prm.zero_tol)
-                        s_omega = exp(th * log(dy / dx) + (1.0 - th) * log(s_omega));
-                    e_restart = e_cand;
-                }
-                for (int j = c0 + tid; j < c1; j += BT) {
-                    const T v = cx[j];
-                    g.x[cur][j] = v;
-                    g.xr[j] = v;
-                    g.xa[cur][j] = T(0);
-                }
-                for (int i = r0 + tid; i < r1; i += BT) {
-                    const T v = cy[i];
-                    g.y[cur][i] = v;
-                    g.yr[i] = v;
-                    g.ya[cur][i] = T(0);
-                }
-                outer += 1;
-                inner = 0;
-                __syncthreads();
+    }
+}
+
+template <int ITEMS, class T>
+__global__ void __launch_bounds__(BT, CPDLP_BATCH_MINB) k_batch_pdlp(BatchArgs<T> g) {
+    __shared__ T prod[BW * 32 * ITEMS];
+    __shared__ double sh[BW * 8 + 8];
+    __shared__ BatchCtl C;
+    for (int guard = 0; guard <= g.count; guard++) {
+        if (threadIdx.x == 0) {
+            const int q = atomicAdd(g.next, 1);
+            C.lp = q < g.count ? g.order[q] : -1;
+            if (C.lp >= 0) {
+                C.L = g.lps[C.lp];
+                C.t_start = global_ns();
+                C.cancelled = *(volatile const int*)g.cancel;
             }
         }
-        // ---- get_solution (common.jl:233-235): unscaled, double
-        for (int j = c0 + tid; j < c1; j += BT) g.out_x[j] = g.D2[j] * (double)g.x[cur][j];
-        for (int i = r0 + tid; i < r1; i += BT) g.out_y[i] = g.D1[i] * (double)g.y[cur][i];
-        if (tid == 0) {
-            R.err = (L.m == 0 && L.zero_cost) ? cpdlp_kkt_errors{NAN, NAN, NAN, NAN, NAN, NAN} : e_sol;
-            R.kkt_passes = passes;
-            R.outer = outer;
-            R.inner = inner;
-            R.total = total;
-            R.eta = s_eta;
-            R.omega = s_omega;
-            R.eta_sum = s_eta_sum;
-            R.time_elapsed = (double)(global_ns() - t_start) * 1e-9;
-            R.status = status;
-            R.restart_from_avg = from_avg;
-            g.res[k] = R;
-        }
+        __syncthreads();
+        if (C.lp < 0) break;
+        if (C.cancelled) skip_one<T>(g, C);
+        else solve_one<ITEMS, T>(g, C, prod, sh);
         __syncthreads();
     }
 }
@@ -474,170 +564,504 @@ double powm_tol(int64_t n, bool f32) {
     return (f32 ? 1.1920928955078125e-07 : 2.220446049250313e-16) * (double)n3;
 }
 
+// one LP as the job keeps it: its own copies of the caller's arrays
+struct LPData {
+    cpdlp_lp v{};
+    std::vector<int64_t> colptr, rowval;
+    std::vector<double> nzval, c, lv, uv, lc, uc;
+    void own() {
+        colptr.assign(v.colptr, v.colptr + v.n + 1);
+        rowval.assign(v.rowval, v.rowval + v.nnz);
+        nzval.assign(v.nzval, v.nzval + v.nnz);
+        c.assign(v.c, v.c + v.n); lv.assign(v.lv, v.lv + v.n); uv.assign(v.uv, v.uv + v.n);
+        lc.assign(v.lc, v.lc + v.m); uc.assign(v.uc, v.uc + v.m);
+        v.colptr = colptr.data(); v.rowval = rowval.data(); v.nzval = nzval.data();
+        v.c = c.data(); v.lv = lv.data(); v.uv = uv.data(); v.lc = lc.data(); v.uc = uc.data();
+    }
+};
+
+void check_lp(const cpdlp_lp& L) {
+    if (L.m < 0 || L.n < 0 || L.nnz < 0) fail(CPDLP_ERR_DIMENSION, "negative LP size in batch");
+    if (!L.colptr || (L.nnz > 0 && (!L.rowval || !L.nzval)))
+        fail(CPDLP_ERR_ARGUMENT, "null CSC array in batch");
+    if (L.n > 0 && (!L.c || !L.lv || !L.uv)) fail(CPDLP_ERR_ARGUMENT, "null c/lv/uv in batch");
+    if (L.m > 0 && (!L.lc || !L.uc)) fail(CPDLP_ERR_ARGUMENT, "null lc/uc in batch");
+    if (L.colptr[0] != 1 || L.colptr[L.n] != L.nnz + 1)
+        fail(CPDLP_ERR_ARGUMENT, "invalid CSC column pointer in batch");
+    for (int64_t q = 0; q < L.nnz; q++)
+        if (L.rowval[q] < 1 || L.rowval[q] > L.m)
+            fail(CPDLP_ERR_ARGUMENT, "invalid CSC in batch: row index out of range");
+}
+
+// what one phase asks for each of its LPs
+struct PhaseLP {
+    int64_t id;        // index in the job
+    double reltol, time_limit;
+    int64_t max_passes, stall_passes;
+    const double* x0;  // warm start (original units) or null
+    const double* y0;
+};
+
+struct RunBase {
+    virtual ~RunBase() = default;
+    std::vector<PhaseLP> lps;
+    std::vector<int64_t> row_off, col_off;
+    // host copies of the results (written by copies queued after the kernel)
+    std::vector<BatchResult> res;
+    std::vector<double> ox, oy;
+    double setup = 0;
+    virtual void fetch(cudaStream_t s) = 0;
+    virtual void release_device() = 0;
+};
+
+// one persistent launch over a set of LPs, on stream h.stream
 template <class T>
-void batch_T(Handle& h, int64_t count, const cpdlp_lp* lps, const cpdlp_params* params,
-             double* const* x_out, double* const* y_out, cpdlp_stats* stats) {
-    cudaStream_t s = h.stream;
-    const double t0 = now_seconds();
-    // block-diagonal concatenation (1-based CSC)
-    std::vector<int64_t> row_off(count + 1, 0), col_off(count + 1, 0), nz_off(count + 1, 0);
-    for (int64_t k = 0; k < count; k++) {
-        const cpdlp_lp& L = lps[k];
-        if (L.m < 0 || L.n < 0 || L.nnz < 0) fail(CPDLP_ERR_DIMENSION, "negative LP size in batch");
-        row_off[k + 1] = row_off[k] + L.m;
-        col_off[k + 1] = col_off[k] + L.n;
-        nz_off[k + 1] = nz_off[k] + L.nnz;
-    }
-    const int64_t M = row_off[count], N = col_off[count], NZ = nz_off[count];
-    if (M >= INT32_MAX || N >= INT32_MAX || NZ >= INT32_MAX)
-        fail(CPDLP_ERR_UNSUPPORTED, "batch too large for int32 indices");
-    std::vector<int64_t> colptr((size_t)N + 1), rowval((size_t)std::max<int64_t>(NZ, 1));
-    std::vector<double> nzval((size_t)std::max<int64_t>(NZ, 1)), c((size_t)std::max<int64_t>(N, 1)),
-        lv(c.size()), uv(c.size()), lc((size_t)std::max<int64_t>(M, 1)), uc(lc.size());
-    colptr[0] = 1;
-    for (int64_t k = 0; k < count; k++) {
-        const cpdlp_lp& L = lps[k];
-        if (!L.colptr || (L.nnz > 0 && (!L.rowval || !L.nzval)))
-            fail(CPDLP_ERR_ARGUMENT, "null CSC array in batch");
-        if (L.colptr[0] != 1 || L.colptr[L.n] != L.nnz + 1)
-            fail(CPDLP_ERR_ARGUMENT, "invalid CSC column pointer in batch");
-        for (int64_t j = 0; j < L.n; j++) colptr[col_off[k] + j + 1] = nz_off[k] + L.colptr[j + 1];
-        for (int64_t q = 0; q < L.nnz; q++) {
-            if (L.rowval[q] < 1 || L.rowval[q] > L.m)
-                fail(CPDLP_ERR_ARGUMENT, "invalid CSC in batch: row index out of range");
-            rowval[nz_off[k] + q] = row_off[k] + L.rowval[q];
-            nzval[nz_off[k] + q] = L.nzval[q];
-        }
-        if (L.n > 0) {
-            std::copy(L.c, L.c + L.n, c.begin() + col_off[k]);
-            std::copy(L.lv, L.lv + L.n, lv.begin() + col_off[k]);
-            std::copy(L.uv, L.uv + L.n, uv.begin() + col_off[k]);
-        }
-        if (L.m > 0) {
-            std::copy(L.lc, L.lc + L.m, lc.begin() + row_off[k]);
-            std::copy(L.uc, L.uc + L.m, uc.begin() + row_off[k]);
-        }
-    }
-    cpdlp_lp big{M, N, NZ, colptr.data(), rowval.data(), nzval.data(), c.data(), lv.data(),
-                 uv.data(), lc.data(), uc.data()};
-    // rows were checked against each LP's own range above; monotone column
-    // pointers and row order are validated by problem_create
-    std::unique_ptr<ProblemBase> PB(problem_create(h, &big, params));
-    auto& P = static_cast<ProblemT<T>&>(*PB);
-    // tile plans with LP boundaries
-    const int items = (NZ / std::max<int64_t>(count, 1) > 32 * 1024) ? 8 : 4;
-    std::vector<int32_t> hpA((size_t)M + 1), hpAt((size_t)N + 1);
-    CK(cudaMemcpyAsync(hpA.data(), P.a_ptr.p, sizeof(int32_t) * (M + 1), cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(hpAt.data(), P.at_ptr.p, sizeof(int32_t) * (N + 1), cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
+struct Run : RunBase {
+    std::unique_ptr<ProblemBase> PB;
     TilePlan planA, planAt;
-    std::vector<int32_t> aT, aL, aI, atT, atL, atI;
-    build_tile_plan(hpA, (int32_t)M, items, planA, s, &row_off, &aT, &aL, &aI);
-    build_tile_plan(hpAt, (int32_t)N, items, planAt, s, &col_off, &atT, &atL, &atI);
-    DBuf<T> partA((size_t)std::max(planA.npieces, 1)), partAt((size_t)std::max(planAt.npieces, 1));
-    // per-LP descriptors
-    const bool f32 = std::is_same<T, float>::value;
-    std::vector<BatchLP> desc((size_t)count);
-    for (int64_t k = 0; k < count; k++) {
-        BatchLP& d = desc[(size_t)k];
-        d.m = (int32_t)lps[k].m; d.n = (int32_t)lps[k].n;
-        d.row_off = (int32_t)row_off[k]; d.col_off = (int32_t)col_off[k];
-        d.a_t0 = aT[k]; d.a_t1 = aT[k + 1]; d.a_l0 = aL[k]; d.a_l1 = aL[k + 1];
-        d.at_t0 = atT[k]; d.at_t1 = atT[k + 1]; d.at_l0 = atL[k]; d.at_l1 = atL[k + 1];
-        d.a_lid0 = aI[k]; d.a_lid1 = aI[k + 1]; d.at_lid0 = atI[k]; d.at_lid1 = atI[k + 1];
-        bool zc = true;
-        for (int64_t j = 0; j < lps[k].n; j++)
-            if (lps[k].c[j] != 0.0) { zc = false; break; }
-        d.zero_cost = zc ? 1 : 0;
-        d.power_tol = params->power_tol_override > 0 ? params->power_tol_override : powm_tol(d.n, f32);
-        d.power_maxiter = params->power_maxiter_override > 0 ? params->power_maxiter_override : d.n;
-    }
-    // power-method start vectors: the single-LP generator, per LP from counter 0
-    std::vector<double> xs((size_t)std::max<int64_t>(N, 1));
-    for (int64_t k = 0; k < count; k++) {
-        for (int64_t j = 0; j < lps[k].n; j++) {
-            const double u1 = (double)((splitmix64_at_host(params->power_seed, 2 * (uint64_t)j) >> 11) + 1) *
-                              (1.0 / 9007199254740992.0);
-            const double u2 = (double)((splitmix64_at_host(params->power_seed, 2 * (uint64_t)j + 1) >> 11) + 1) *
-                              (1.0 / 9007199254740992.0);
-            xs[(size_t)(col_off[k] + j)] = std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
+    DBuf<T> partA, partAt;
+    DBuf<T> bx[2], by[2], bxa[2], bya[2], bxr, byr, bxbar;
+    DBuf<double> d_x0, d_y0, d_outx, d_outy, longA, longAt, d_theta;
+    DBuf<int64_t> d_piters;
+    DBuf<BatchLP> d_desc;
+    DBuf<int32_t> d_order;
+    DBuf<BatchResult> d_res;
+    DBuf<int> d_next;
+
+    void launch(Handle& h, const std::vector<LPData>& all, const cpdlp_params& prm,
+                const int* cancel, int items) {
+        cudaStream_t s = h.stream;
+        const double t0 = now_seconds();
+        // occupancy first: it loads the kernels, which must not wait behind
+        // this job's own queued work
+        auto pk = (items == 8) ? k_batch_power<8, T> : k_batch_power<4, T>;
+        auto kern = (items == 8) ? k_batch_pdlp<8, T> : k_batch_pdlp<4, T>;
+        int per_sm_p = 0, per_sm = 0;
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_p, pk, BT, 0));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BT, 0));
+        const int64_t count = (int64_t)lps.size();
+        row_off.assign(count + 1, 0);
+        col_off.assign(count + 1, 0);
+        std::vector<int64_t> nz_off(count + 1, 0);
+        for (int64_t k = 0; k < count; k++) {
+            const cpdlp_lp& L = all[lps[k].id].v;
+            row_off[k + 1] = row_off[k] + L.m;
+            col_off[k + 1] = col_off[k] + L.n;
+            nz_off[k + 1] = nz_off[k] + L.nnz;
         }
-    }
-    // device buffers
-    const size_t nz = (size_t)std::max<int64_t>(N, 1), mz = (size_t)std::max<int64_t>(M, 1);
-    DBuf<T> bx[2], by[2], bxa[2], bya[2], bxr(nz), byr(mz), bxbar(nz);
-    for (int b = 0; b < 2; b++) { bx[b].alloc(nz); by[b].alloc(mz); bxa[b].alloc(nz); bya[b].alloc(mz); }
-    DBuf<double> d_xs(nz), d_outx(nz), d_outy(mz);
-    DBuf<BatchLP> d_desc((size_t)std::max<int64_t>(count, 1));
-    DBuf<BatchResult> d_res((size_t)std::max<int64_t>(count, 1));
-    DBuf<double> longA((size_t)std::max(planA.nlong, 1) * 2), longAt((size_t)std::max(planAt.nlong, 1) * 3);
-    DBuf<int> d_next(1);
-    CK(cudaMemcpyAsync(d_xs.p, xs.data(), sizeof(double) * nz, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(d_desc.p, desc.data(), sizeof(BatchLP) * desc.size(), cudaMemcpyHostToDevice, s));
-    CK(cudaMemsetAsync(d_next.p, 0, sizeof(int), s));
-    int per_sm = 0;
-    auto kern = (items == 8) ? k_batch_pdlp<8, T> : k_batch_pdlp<4, T>;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BT, 0));
-    const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(count, (int64_t)std::max(per_sm, 1) * h.num_sms));
-    DBuf<double> d_red((size_t)grid * 32);
-    DBuf<StepCoef<T>> d_coef((size_t)grid);
-    BatchArgs<T> g;
-    g.A = CsrView<T, T>{P.a_ptr.p, P.a_idx.p, P.a_val.p, planA.tasks.p, planA.ntasks,
-                        planA.ltasks.p, planA.nltasks, planA.counters.p, partA.p};
-    g.At = CsrView<T, T>{P.at_ptr.p, P.at_idx.p, P.at_val.p, planAt.tasks.p, planAt.ntasks,
-                         planAt.ltasks.p, planAt.nltasks, planAt.counters.p, partAt.p};
-    g.c = P.c.p; g.lv = P.lv.p; g.uv = P.uv.p; g.lc = P.lc.p; g.uc = P.uc.p;
-    g.invD1 = P.invD1.p; g.invD2 = P.invD2.p; g.D1 = P.D1.p; g.D2 = P.D2.p;
-    for (int b = 0; b < 2; b++) { g.x[b] = bx[b].p; g.y[b] = by[b].p; g.xa[b] = bxa[b].p; g.ya[b] = bya[b].p; }
-    g.xr = bxr.p; g.yr = byr.p; g.xbar = bxbar.p;
-    g.x_start = d_xs.p;
-    g.lps = d_desc.p; g.res = d_res.p; g.out_x = d_outx.p; g.out_y = d_outy.p;
-    g.red = d_red.p; g.longA = longA.p; g.longAt = longAt.p; g.coef = d_coef.p;
-    g.next = d_next.p; g.count = (int32_t)count;
-    g.prm = BatchParams{params->algorithm, params->check_every > 0 ? params->check_every : 100,
-                        params->max_kkt_passes, params->termination_reltol,
-                        params->time_limit - (now_seconds() - t0), params->invnorm_scaling,
-                        params->primal_weight_damping, params->zero_tol, params->sufficient_decay,
-                        params->necessary_decay, params->artificial_decay};
-    const double setup = now_seconds() - t0;
-    kern<<<(unsigned)grid, BT, 0, s>>>(g);
-    CK_LAUNCH();
-    std::vector<BatchResult> res((size_t)count);
-    std::vector<double> ox(nz), oy(mz);
-    CK(cudaMemcpyAsync(res.data(), d_res.p, sizeof(BatchResult) * count, cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(ox.data(), d_outx.p, sizeof(double) * nz, cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(oy.data(), d_outy.p, sizeof(double) * mz, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    for (int64_t k = 0; k < count; k++) {
-        if (x_out && x_out[k]) std::copy(ox.begin() + col_off[k], ox.begin() + col_off[k + 1], x_out[k]);
-        if (y_out && y_out[k]) std::copy(oy.begin() + row_off[k], oy.begin() + row_off[k + 1], y_out[k]);
-        if (stats) {
-            cpdlp_stats& st = stats[k];
-            const BatchResult& r = res[(size_t)k];
-            memset(&st, 0, sizeof(st));
-            st.err = r.err;
-            st.time_elapsed = r.time_elapsed;
-            st.kkt_passes = r.kkt_passes;
-            st.termination_status = r.status;
-            st.restart_from_avg = r.restart_from_avg;
-            st.outer = r.outer; st.inner = r.inner; st.total = r.total;
-            st.eta = r.eta; st.eta_sum = r.eta_sum; st.omega = r.omega;
-            st.power_iterations = r.power_iterations;
-            st.setup_seconds = setup;
-            st.kernel_launches = 1;
+        const int64_t M = row_off[count], N = col_off[count], NZ = nz_off[count];
+        if (M >= INT32_MAX || N >= INT32_MAX || NZ >= INT32_MAX)
+            fail(CPDLP_ERR_UNSUPPORTED, "batch too large for int32 indices");
+        // block-diagonal concatenation (1-based CSC)
+        std::vector<int64_t> colptr((size_t)N + 1), rowval((size_t)std::max<int64_t>(NZ, 1));
+        std::vector<double> nzval(rowval.size()), c((size_t)std::max<int64_t>(N, 1)),
+            lv(c.size()), uv(c.size()), lc((size_t)std::max<int64_t>(M, 1)), uc(lc.size());
+        colptr[0] = 1;
+        for (int64_t k = 0; k < count; k++) {
+            const cpdlp_lp& L = all[lps[k].id].v;
+            for (int64_t j = 0; j < L.n; j++) colptr[col_off[k] + j + 1] = nz_off[k] + L.colptr[j + 1];
+            for (int64_t q = 0; q < L.nnz; q++) {
+                rowval[nz_off[k] + q] = row_off[k] + L.rowval[q];
+                nzval[nz_off[k] + q] = L.nzval[q];
+            }
+            if (L.n > 0) {
+                std::copy(L.c, L.c + L.n, c.begin() + col_off[k]);
+                std::copy(L.lv, L.lv + L.n, lv.begin() + col_off[k]);
+                std::copy(L.uv, L.uv + L.n, uv.begin() + col_off[k]);
+            }
+            if (L.m > 0) {
+                std::copy(L.lc, L.lc + L.m, lc.begin() + row_off[k]);
+                std::copy(L.uc, L.uc + L.m, uc.begin() + row_off[k]);
+            }
         }
+        cpdlp_lp big{M, N, NZ, colptr.data(), rowval.data(), nzval.data(), c.data(), lv.data(),
+                     uv.data(), lc.data(), uc.data()};
+        PB.reset(problem_create(h, &big, &prm));
+        auto& P = static_cast<ProblemT<T>&>(*PB);
+        // tile plans with LP boundaries
+        std::vector<int32_t> hpA((size_t)M + 1), hpAt((size_t)N + 1);
+        CK(cudaMemcpyAsync(hpA.data(), P.a_ptr.p, sizeof(int32_t) * (M + 1), cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(hpAt.data(), P.at_ptr.p, sizeof(int32_t) * (N + 1), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        std::vector<int32_t> aT, aL, aI, atT, atL, atI;
+        build_tile_plan(hpA, (int32_t)M, items, planA, s, &row_off, &aT, &aL, &aI, 32 * BATCH_RPL);
+        build_tile_plan(hpAt, (int32_t)N, items, planAt, s, &col_off, &atT, &atL, &atI, 32 * BATCH_RPL);
+        partA.alloc((size_t)std::max(planA.npieces, 1));
+        partAt.alloc((size_t)std::max(planAt.npieces, 1));
+        // per-LP descriptors and the largest-first queue order
+        std::vector<BatchLP> desc((size_t)count);
+        bool any_warm = false;
+        for (int64_t k = 0; k < count; k++) {
+            const cpdlp_lp& L = all[lps[k].id].v;
+            BatchLP& d = desc[(size_t)k];
+            d.m = (int32_t)L.m; d.n = (int32_t)L.n;
+            d.row_off = (int32_t)row_off[k]; d.col_off = (int32_t)col_off[k];
+            d.a_t0 = aT[k]; d.a_t1 = aT[k + 1]; d.a_l0 = aL[k]; d.a_l1 = aL[k + 1];
+            d.at_t0 = atT[k]; d.at_t1 = atT[k + 1]; d.at_l0 = atL[k]; d.at_l1 = atL[k + 1];
+            d.a_lid0 = aI[k]; d.a_lid1 = aI[k + 1]; d.at_lid0 = atI[k]; d.at_lid1 = atI[k + 1];
+            bool zc = true;
+            for (int64_t j = 0; j < L.n; j++)
+                if (L.c[j] != 0.0) { zc = false; break; }
+            d.zero_cost = zc ? 1 : 0;
+            d.warm = (lps[k].x0 || lps[k].y0) ? 1 : 0;
+            any_warm = any_warm || d.warm;
+            // the power method runs in FP64 for either iterate type
+            d.power_tol = prm.power_tol_override > 0 ? prm.power_tol_override : powm_tol(d.n, false);
+            d.power_maxiter = prm.power_maxiter_override > 0 ? prm.power_maxiter_override : d.n;
+            d.reltol = lps[k].reltol;
+            d.time_limit = lps[k].time_limit;
+            d.max_passes = lps[k].max_passes;
+            d.stall_passes = lps[k].stall_passes;
+        }
+        std::vector<int32_t> order((size_t)count);
+        std::iota(order.begin(), order.end(), 0);
+        std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
+            return nz_off[a + 1] - nz_off[a] > nz_off[b + 1] - nz_off[b];
+        });
+        // power-method start vectors: the single-LP generator, per LP from counter 0
+        std::vector<double> xs((size_t)std::max<int64_t>(N, 1));
+        for (int64_t k = 0; k < count; k++) {
+            for (int64_t j = 0; j < col_off[k + 1] - col_off[k]; j++) {
+                const double u1 = (double)((splitmix64_at_host(prm.power_seed, 2 * (uint64_t)j) >> 11) + 1) *
+                                  (1.0 / 9007199254740992.0);
+                const double u2 = (double)((splitmix64_at_host(prm.power_seed, 2 * (uint64_t)j + 1) >> 11) + 1) *
+                                  (1.0 / 9007199254740992.0);
+                xs[(size_t)(col_off[k] + j)] = std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
+            }
+        }
+        const size_t nz = (size_t)std::max<int64_t>(N, 1), mz = (size_t)std::max<int64_t>(M, 1);
+        std::vector<double> hx0, hy0;
+        if (any_warm) {
+            hx0.assign(nz, 0.0);
+            hy0.assign(mz, 0.0);
+            for (int64_t k = 0; k < count; k++) {
+                if (lps[k].x0) std::copy(lps[k].x0, lps[k].x0 + (col_off[k + 1] - col_off[k]), hx0.begin() + col_off[k]);
+                if (lps[k].y0) std::copy(lps[k].y0, lps[k].y0 + (row_off[k + 1] - row_off[k]), hy0.begin() + row_off[k]);
+            }
+        }
+        // device buffers
+        for (int b = 0; b < 2; b++) { bx[b].alloc(nz); by[b].alloc(mz); bxa[b].alloc(nz); bya[b].alloc(mz); }
+        bxr.alloc(nz); byr.alloc(mz); bxbar.alloc(nz);
+        d_outx.alloc(nz); d_outy.alloc(mz);
+        d_desc.alloc((size_t)std::max<int64_t>(count, 1));
+        d_order.alloc((size_t)std::max<int64_t>(count, 1));
+        d_res.alloc((size_t)std::max<int64_t>(count, 1));
+        d_theta.alloc((size_t)std::max<int64_t>(count, 1));
+        d_piters.alloc((size_t)std::max<int64_t>(count, 1));
+        longA.alloc((size_t)std::max(planA.nlong, 1) * 2);
+        longAt.alloc((size_t)std::max(planAt.nlong, 1) * 3);
+        d_next.alloc(2);
+        if (any_warm) {
+            d_x0.alloc(nz);
+            d_y0.alloc(mz);
+            CK(cudaMemcpyAsync(d_x0.p, hx0.data(), sizeof(double) * nz, cudaMemcpyHostToDevice, s));
+            CK(cudaMemcpyAsync(d_y0.p, hy0.data(), sizeof(double) * mz, cudaMemcpyHostToDevice, s));
+        }
+        CK(cudaMemcpyAsync(d_desc.p, desc.data(), sizeof(BatchLP) * desc.size(), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(d_order.p, order.data(), sizeof(int32_t) * order.size(), cudaMemcpyHostToDevice, s));
+        CK(cudaMemsetAsync(d_next.p, 0, 2 * sizeof(int), s));
+        // power method (FP64 vectors, scratch released in stream order after it)
+        {
+            DBuf<double> px(nz), pAtx(nz), ps(mz), d_xs(nz);
+            DBuf<double> pA((size_t)std::max(planA.npieces, 1)), pAt((size_t)std::max(planAt.npieces, 1));
+            CK(cudaMemcpyAsync(d_xs.p, xs.data(), sizeof(double) * nz, cudaMemcpyHostToDevice, s));
+            PowerArgs<T> pg;
+            pg.A = CsrView<T, double>{P.a_ptr.p, P.a_idx.p, P.a_val.p, planA.tasks.p, planA.ntasks,
+                                      planA.ltasks.p, planA.nltasks, planA.counters.p, pA.p};
+            pg.At = CsrView<T, double>{P.at_ptr.p, P.at_idx.p, P.at_val.p, planAt.tasks.p,
+                                       planAt.ntasks, planAt.ltasks.p, planAt.nltasks,
+                                       planAt.counters.p, pAt.p};
+            pg.x = px.p; pg.Atx = pAtx.p; pg.s = ps.p; pg.x_start = d_xs.p;
+            pg.lps = d_desc.p; pg.order = d_order.p; pg.theta = d_theta.p; pg.iters = d_piters.p;
+            pg.longAt = longAt.p; pg.next = d_next.p + 1; pg.count = (int32_t)count;
+            const int64_t pgrid =
+                std::max<int64_t>(1, std::min<int64_t>(count, (int64_t)std::max(per_sm_p, 1) * h.num_sms));
+            pk<<<(unsigned)pgrid, BT, 0, s>>>(pg);
+            CK_LAUNCH();
+        }
+        const int64_t grid =
+            std::max<int64_t>(1, std::min<int64_t>(count, (int64_t)std::max(per_sm, 1) * h.num_sms));
+        BatchArgs<T> g;
+        g.A = CsrView<T, T>{P.a_ptr.p, P.a_idx.p, P.a_val.p, planA.tasks.p, planA.ntasks,
+                            planA.ltasks.p, planA.nltasks, planA.counters.p, partA.p};
+        g.At = CsrView<T, T>{P.at_ptr.p, P.at_idx.p, P.at_val.p, planAt.tasks.p, planAt.ntasks,
+                             planAt.ltasks.p, planAt.nltasks, planAt.counters.p, partAt.p};
+        g.c = P.c.p; g.lv = P.lv.p; g.uv = P.uv.p; g.lc = P.lc.p; g.uc = P.uc.p;
+        g.invD1 = P.invD1.p; g.invD2 = P.invD2.p; g.D1 = P.D1.p; g.D2 = P.D2.p;
+        for (int b = 0; b < 2; b++) { g.x[b] = bx[b].p; g.y[b] = by[b].p; g.xa[b] = bxa[b].p; g.ya[b] = bya[b].p; }
+        g.xr = bxr.p; g.yr = byr.p; g.xbar = bxbar.p;
+        g.theta = d_theta.p;
+        g.power_iters = d_piters.p;
+        g.x_init = any_warm ? d_x0.p : nullptr;
+        g.y_init = any_warm ? d_y0.p : nullptr;
+        g.lps = d_desc.p; g.order = d_order.p; g.res = d_res.p; g.out_x = d_outx.p; g.out_y = d_outy.p;
+        g.longA = longA.p; g.longAt = longAt.p;
+        g.next = d_next.p; g.cancel = cancel; g.count = (int32_t)count;
+        g.prm = BatchParams{prm.algorithm, prm.check_every > 0 ? prm.check_every : 100,
+                            prm.invnorm_scaling, prm.primal_weight_damping, prm.zero_tol,
+                            prm.sufficient_decay, prm.necessary_decay, prm.artificial_decay};
+        setup = now_seconds() - t0;
+        kern<<<(unsigned)grid, BT, 0, s>>>(g);
+        CK_LAUNCH();
+    }
+    // after the kernel: results to the host (the copies to pageable memory
+    // block, so they are issued only once the kernel has finished)
+    void fetch(cudaStream_t s) override {
+        const size_t count = lps.size();
+        res.resize(count);
+        ox.resize(d_outx.n);
+        oy.resize(d_outy.n);
+        CK(cudaMemcpyAsync(res.data(), d_res.p, sizeof(BatchResult) * count, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(ox.data(), d_outx.p, sizeof(double) * ox.size(), cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(oy.data(), d_outy.p, sizeof(double) * oy.size(), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+    }
+    void release_device() override {
+        PB.reset();
+        for (int b = 0; b < 2; b++) { bx[b].release(); by[b].release(); bxa[b].release(); bya[b].release(); }
+        bxr.release(); byr.release(); bxbar.release(); partA.release(); partAt.release();
+        d_x0.release(); d_y0.release(); d_outx.release(); d_outy.release();
+        longA.release(); longAt.release(); d_desc.release(); d_order.release(); d_res.release();
+        d_theta.release(); d_piters.release(); d_next.release();
+        planA = TilePlan();
+        planAt = TilePlan();
+    }
+};
+
+}  // namespace
+
+// ---- jobs ---------------------------------------------------------------------
+struct Job {
+    Handle jh;                 // the caller's device, this job's own stream
+    cudaEvent_t ev = nullptr;
+    cpdlp_params prm{};
+    int items = BATCH_ITEMS;
+    std::vector<LPData> lps;
+    std::vector<double> target;  // final relative KKT tolerance per LP
+    // results
+    std::vector<std::vector<double>> x, y;
+    std::vector<cpdlp_stats> st;
+    std::unique_ptr<RunBase> run;
+    int phase = 0;             // 1: first phase in flight, 2: refinement in flight, 3: done
+    bool cancelled = false;
+    DBuf<int> d_cancel;
+
+    ~Job() {
+        if (jh.stream) cudaStreamSynchronize(jh.stream);
+        if (run) run->release_device();
+        run.reset();
+        d_cancel.release();
+        if (ev) cudaEventDestroy(ev);
+        if (jh.stream) {
+            cudaStreamSynchronize(jh.stream);
+            cudaStreamDestroy(jh.stream);
+        }
+        if (jh.pinned) cudaFreeHost(jh.pinned);
+    }
+
+    template <class T>
+    void start(const std::vector<PhaseLP>& phase_lps, const cpdlp_params& p) {
+        AllocScope scope(jh.stream);
+        auto* r = new Run<T>();
+        run.reset(r);
+        r->lps = phase_lps;
+        r->launch(jh, lps, p, d_cancel.p, items);
+        CK(cudaEventRecord(ev, jh.stream));
+    }
+
+    void start_phase(const std::vector<PhaseLP>& phase_lps, int32_t float_type) {
+        cpdlp_params p = prm;
+        p.float_type = float_type;
+        if (float_type == CPDLP_VAL_F32) start<float>(phase_lps, p);
+        else start<double>(phase_lps, p);
+    }
+
+    // copies the finished run's results into x / y / st; returns the LPs
+    // that continue in the FP64 refinement phase
+    std::vector<PhaseLP> finish_run() {
+        RunBase& r = *run;
+        std::vector<PhaseLP> next;
+        const bool first = phase == 1;
+        for (size_t k = 0; k < r.lps.size(); k++) {
+            const int64_t id = r.lps[k].id;
+            const cpdlp_lp& L = lps[id].v;
+            const BatchResult& R = r.res[k];
+            x[id].assign(r.ox.begin() + r.col_off[k], r.ox.begin() + r.col_off[k + 1]);
+            y[id].assign(r.oy.begin() + r.row_off[k], r.oy.begin() + r.row_off[k + 1]);
+            cpdlp_stats& S = st[id];
+            const int64_t passes_before = first ? 0 : S.kkt_passes;
+            const double time_before = first ? 0.0 : S.time_elapsed;
+            const int64_t launches_before = first ? 0 : S.kernel_launches;
+            memset(&S, 0, sizeof(S));
+            S.err = R.err;
+            S.time_elapsed = time_before + R.time_elapsed;
+            S.kkt_passes = passes_before + R.kkt_passes;
+            S.refine_kkt_passes = first ? 0 : R.kkt_passes;
+            S.termination_status = R.status;
+            S.restart_from_avg = R.restart_from_avg;
+            S.outer = R.outer; S.inner = R.inner; S.total = R.total;
+            S.eta = R.eta; S.eta_sum = R.eta_sum; S.omega = R.omega;
+            S.power_iterations = R.power_iterations;
+            S.setup_seconds = r.setup;
+            S.kernel_launches = launches_before + 2;  // power method + solve
+            const bool early = L.m == 0 && R.status == CPDLP_OPTIMAL && R.kkt_passes == 0;
+            // FP64 phase: LPs that reached the FP32 tolerance but target a
+            // tighter one, and LPs whose FP32 iterates stalled
+            const bool refine = R.status == CPDLP_OPTIMAL && target[id] < r.lps[k].reltol;
+            const bool rescue = R.stalled && R.kkt_passes < prm.max_kkt_passes;
+            if (first && prm.float_type == CPDLP_VAL_F32 && !cancelled && !early &&
+                (refine || rescue)) {
+                PhaseLP q;
+                q.id = id;
+                q.reltol = target[id];
+                q.max_passes = std::max<int64_t>(prm.max_kkt_passes - R.kkt_passes, 1);
+                q.stall_passes = 0;
+                q.time_limit = prm.time_limit - R.time_elapsed;
+                q.x0 = nullptr;  // set below, once x / y hold this LP's result
+                q.y0 = nullptr;
+                next.push_back(q);
+            }
+        }
+        for (PhaseLP& q : next) {
+            q.x0 = x[q.id].data();
+            q.y0 = y[q.id].data();
+        }
+        return next;
+    }
+
+    bool poll() {
+        if (phase == 3) return true;
+        cudaError_t e = cudaEventQuery(ev);
+        if (e == cudaErrorNotReady) return false;
+        CK(e);
+        {
+            AllocScope scope(jh.stream);
+            run->fetch(jh.stream);
+            run->release_device();
+        }
+        std::vector<PhaseLP> next = finish_run();
+        run.reset();
+        if (phase == 1 && !next.empty()) {
+            phase = 2;
+            start_phase(next, CPDLP_VAL_F64);
+            return false;
+        }
+        phase = 3;
+        return true;
+    }
+};
+
+Job* job_submit(Handle& h, int64_t count, const cpdlp_lp* lps, const cpdlp_params* params,
+                const double* reltol, const double* const* x0, const double* const* y0) {
+    if (count < 0) fail(CPDLP_ERR_ARGUMENT, "negative batch size");
+    if (count > 0 && !lps) fail(CPDLP_ERR_ARGUMENT, "null LP array");
+    if (!params) fail(CPDLP_ERR_ARGUMENT, "null params");
+    if (params->check_every <= 0) fail(CPDLP_ERR_ARGUMENT, "check_every must be positive");
+    if (params->float_type != CPDLP_VAL_F64 && params->float_type != CPDLP_VAL_F32)
+        fail(CPDLP_ERR_ARGUMENT, "float_type must be CPDLP_VAL_F64 or CPDLP_VAL_F32");
+    if (params->tile_flags != 0) fail(CPDLP_ERR_ARGUMENT, "tile_flags is reserved and must be 0");
+    if (count > INT32_MAX) fail(CPDLP_ERR_UNSUPPORTED, "batch too large");
+    for (int64_t k = 0; k < count; k++) check_lp(lps[k]);
+    std::unique_ptr<Job> J(new Job());
+    J->prm = *params;
+    J->items = params->tile_nnz > 0 ? choose_items(0, 1, params->tile_nnz) : BATCH_ITEMS;
+    if (J->items != 4 && J->items != 8) J->items = 8;
+    J->jh.device = h.device;
+    J->jh.num_sms = h.num_sms;
+    CK(cudaStreamCreateWithFlags(&J->jh.stream, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&J->ev, cudaEventDisableTiming));
+    {
+        AllocScope scope(J->jh.stream);
+        J->d_cancel.alloc(1);
+        CK(cudaMemsetAsync(J->d_cancel.p, 0, sizeof(int), J->jh.stream));
+    }
+    J->lps.resize((size_t)count);
+    J->target.resize((size_t)count);
+    J->x.resize((size_t)count);
+    J->y.resize((size_t)count);
+    J->st.assign((size_t)count, cpdlp_stats{});
+    const bool f32 = params->float_type == CPDLP_VAL_F32;
+    std::vector<PhaseLP> first((size_t)count);
+    for (int64_t k = 0; k < count; k++) {
+        J->lps[k].v = lps[k];
+        J->lps[k].own();
+        double t = reltol ? reltol[k] : (f32 && params->refine_reltol > 0 ? params->refine_reltol
+                                                                         : params->termination_reltol);
+        if (!(t >= 0)) fail(CPDLP_ERR_ARGUMENT, "relative tolerance must be >= 0");
+        J->target[k] = t;
+        PhaseLP& q = first[k];
+        q.id = k;
+        // FP32 iterates stop at the FP32 phase's tolerance; tighter targets refine in FP64
+        q.reltol = f32 ? std::max(t, params->termination_reltol) : t;
+        q.max_passes = params->max_kkt_passes;
+        q.stall_passes = f32 ? FP32_STALL_CHECKS * (int64_t)params->check_every : 0;
+        q.time_limit = params->time_limit;
+        q.x0 = x0 ? x0[k] : nullptr;
+        q.y0 = y0 ? y0[k] : nullptr;
+    }
+    if (count == 0) {
+        J->phase = 3;
+        return J.release();
+    }
+    J->phase = 1;
+    J->start_phase(first, params->float_type);
+    return J.release();
+}
+
+bool job_poll(Job* j) { return j->poll(); }
+
+void job_wait(Job* j) {
+    while (!j->poll()) CK(cudaEventSynchronize(j->ev));
+}
+
+void job_cancel(Job* j) {
+    if (j->phase == 3) return;
+    j->cancelled = true;
+    // the job's stream is busy with the kernel: set the flag from a side stream
+    static const int one = 1;
+    cudaStream_t side;
+    CK(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+    cudaError_t e = cudaMemcpyAsync(j->d_cancel.p, &one, sizeof(int), cudaMemcpyHostToDevice, side);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(side);
+    cudaStreamDestroy(side);
+    CK(e);
+}
+
+void job_collect(Job* j, double* const* x_out, double* const* y_out, cpdlp_stats* stats) {
+    if (j->phase != 3) fail(CPDLP_ERR_ARGUMENT, "job not finished (poll until it reports done)");
+    for (size_t k = 0; k < j->lps.size(); k++) {
+        if (x_out && x_out[k]) std::copy(j->x[k].begin(), j->x[k].end(), x_out[k]);
+        if (y_out && y_out[k]) std::copy(j->y[k].begin(), j->y[k].end(), y_out[k]);
+        if (stats) stats[k] = j->st[k];
     }
 }
 
-}  // namespace
+int64_t job_count(const Job* j) { return (int64_t)j->lps.size(); }
+
+void job_destroy(Job* j) { delete j; }
+
+int64_t batch_footprint(int64_t count, const cpdlp_lp* lps, const cpdlp_params* params) {
+    const int64_t sv = params && params->float_type == CPDLP_VAL_F32 ? 4 : 8;
+    int64_t m = 0, n = 0, nnz = 0;
+    for (int64_t k = 0; k < count; k++) {
+        m += std::max<int64_t>(lps[k].m, 0);
+        n += std::max<int64_t>(lps[k].n, 0);
+        nnz += std::max<int64_t>(lps[k].nnz, 0);
+    }
+    // matrices: CSR of A and A' (index, value, padding) plus the preprocessing's
+    // FP64 CSC copies and sort buffers; vectors: 7 iterates of n and 5 of m,
+    // bounds and costs, FP64 scalings, start vectors and outputs
+    const int64_t mat = nnz * (2 * (4 + sv) + 40) + (m + n) * 16 + (1 << 16);
+    const int64_t vec = n * (10 * sv + 5 * 8) + m * (8 * sv + 5 * 8);
+    return mat + vec + count * 256 + (4 << 20);
+}
 
 void batch_solve(Handle& h, int64_t count, const cpdlp_lp* lps, const cpdlp_params* params,
                  double* const* x_out, double* const* y_out, cpdlp_stats* stats) {
     if (count == 0) return;
-    if (params->check_every <= 0) fail(CPDLP_ERR_ARGUMENT, "check_every must be positive");
-    if (params->float_type == CPDLP_VAL_F32) batch_T<float>(h, count, lps, params, x_out, y_out, stats);
-    else if (params->float_type == CPDLP_VAL_F64) batch_T<double>(h, count, lps, params, x_out, y_out, stats);
-    else fail(CPDLP_ERR_ARGUMENT, "float_type must be CPDLP_VAL_F64 or CPDLP_VAL_F32");
+    std::unique_ptr<Job> J(job_submit(h, count, lps, params, nullptr, nullptr, nullptr));
+    job_wait(J.get());
+    job_collect(J.get(), x_out, y_out, stats);
 }
 
 }  // namespace cpdlp

@@ -41,29 +41,48 @@ inline void cuda_check(cudaError_t e, const char* what, const char* file, int li
 #define CK_LAUNCH() ::cpdlp::cuda_check(cudaGetLastError(), "kernel launch", __FILE__, __LINE__)
 
 // ---------------------------------------------------------------------------
-// device buffer (owning, move-only)
+// device buffer (owning, move-only), stream-ordered: allocated with
+// cudaMallocAsync on the calling thread's current allocation stream and freed
+// with cudaFreeAsync on the same stream, so that creating or dropping buffers
+// never waits for kernels running on other streams (a plain cudaFree would
+// synchronise the device, stalling every batch in flight).  Buffers must be
+// released before the stream they were allocated on is destroyed.
 // ---------------------------------------------------------------------------
+inline cudaStream_t& alloc_stream() {
+    static thread_local cudaStream_t s = nullptr;
+    return s;
+}
+struct AllocScope {
+    cudaStream_t prev;
+    explicit AllocScope(cudaStream_t s) : prev(alloc_stream()) { alloc_stream() = s; }
+    ~AllocScope() { alloc_stream() = prev; }
+    AllocScope(const AllocScope&) = delete;
+    AllocScope& operator=(const AllocScope&) = delete;
+};
+
 template <class T>
 struct DBuf {
     T* p = nullptr;
     size_t n = 0;
+    cudaStream_t s = nullptr;
     DBuf() = default;
     explicit DBuf(size_t count) { alloc(count); }
     DBuf(const DBuf&) = delete;
     DBuf& operator=(const DBuf&) = delete;
-    DBuf(DBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+    DBuf(DBuf&& o) noexcept : p(o.p), n(o.n), s(o.s) { o.p = nullptr; o.n = 0; }
     DBuf& operator=(DBuf&& o) noexcept {
-        if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+        if (this != &o) { release(); p = o.p; n = o.n; s = o.s; o.p = nullptr; o.n = 0; }
         return *this;
     }
     ~DBuf() { release(); }
     void alloc(size_t count) {
         release();
         n = count;
-        if (count) CK(cudaMalloc((void**)&p, sizeof(T) * count));
+        s = alloc_stream();
+        if (count) CK(cudaMallocAsync((void**)&p, sizeof(T) * count, s));
     }
     void release() {
-        if (p) cudaFree(p);
+        if (p) cudaFreeAsync(p, s);
         p = nullptr;
         n = 0;
     }

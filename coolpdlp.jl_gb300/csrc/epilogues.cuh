@@ -1,6 +1,15 @@
 // epilogues.cuh -- the fused per-row epilogues of the tile SpMV engine:
 // PDHG steps (pdlp.jl:108-117, :126-136), KKT error terms (errors.jl:65-109),
 // the power method (linalg.jl:60-96) and a plain store.
+//
+// Epilogue interface (per row r, per input vector p):
+//   struct Pre;                      inputs of one row, loaded before the gathers
+//   Pre pre_global(int r) const;     loads them
+//   void row(int p, int r, T s, const Pre&, Acc&)   rows of short tiles
+//   void row_long(int p, int r, T s, int lid, Acc&)  long rows (one lane)
+//   void init(Acc&); void finish(Acc&);             block reductions
+// Every load of a vector that a kernel may itself have written earlier (the
+// in-kernel step loop of the batched solver) is a coherent load.
 #pragma once
 
 #include "cpdlp_common.cuh"
@@ -15,20 +24,32 @@ template <class T>
 struct StoreEpi {  // out = s (mul! with alpha = true, beta = false)
     T* out;
     using Acc = NoAcc;
-    StoreEpi shifted(unsigned) const { return *this; }
     struct Pre {};
-    static constexpr int NPRE = 0;
-    static constexpr int pre_esz(int) { return (int)sizeof(T); }
-    __device__ const void* pre_src(int) const { return nullptr; }
     __device__ Pre pre_global(int) const { return Pre{}; }
-    __device__ Pre pre_staged(const Staged<NPRE>&, int) const { return Pre{}; }
     __device__ void init(Acc&) {}
     __device__ void row(int, int r, T s, const Pre&, Acc&) { out[r] = s; }
     __device__ void row_long(int, int r, T s, int, Acc&) { out[r] = s; }
     __device__ void finish(Acc&) {}
 };
 
+// Step coefficients tau, sigma, 1/sigma and the averaging weights: read from
+// device memory written before the launch (graph-captured step kernels), or
+// carried by value (the batched kernel, which changes them between steps
+// inside one launch).
+template <class T, bool BYVAL>
+struct CoefSrc;
 template <class T>
+struct CoefSrc<T, false> {
+    const StepCoef<T>* __restrict__ coef;
+    __device__ __forceinline__ const StepCoef<T>& get() const { return *coef; }
+};
+template <class T>
+struct CoefSrc<T, true> {
+    StepCoef<T> k;
+    __device__ __forceinline__ const StepCoef<T>& get() const { return k; }
+};
+
+template <class T, bool BYVAL = false>
 struct PrimalEpi {
     const T* __restrict__ x;
     const T* __restrict__ c;
@@ -38,38 +59,27 @@ struct PrimalEpi {
     T* __restrict__ xbar;
     const T* __restrict__ xa_old;
     T* __restrict__ xa_new;
-    const StepCoef<T>* __restrict__ coef;
+    CoefSrc<T, BYVAL> coef;
     int avg;
     using Acc = NoAcc;
-    PrimalEpi shifted(unsigned) const { return *this; }
     struct Pre { T x, c, lv, uv, xa; };
-    static constexpr int NPRE = 5;
-    static constexpr int pre_esz(int) { return (int)sizeof(T); }
-    __device__ const void* pre_src(int k) const {
-        return k == 0 ? (const void*)x : k == 1 ? (const void*)c : k == 2 ? (const void*)lv
-             : k == 3 ? (const void*)uv : (avg ? (const void*)xa_old : nullptr);
-    }
     __device__ __forceinline__ Pre pre_global(int j) const {
         return Pre{ld_stream(x + j), ld_stream(c + j), ld_stream(lv + j), ld_stream(uv + j),
                    avg ? ld_stream(xa_old + j) : T(0)};
     }
-    __device__ __forceinline__ Pre pre_staged(const Staged<NPRE>& st, int j) const {
-        return Pre{st.template get<T>(0, j), st.template get<T>(1, j), st.template get<T>(2, j), st.template get<T>(3, j),
-                   avg ? st.template get<T>(4, j) : T(0)};
-    }
     __device__ void init(Acc&) {}
     __device__ __forceinline__ void row(int, int j, T s, const Pre& q, Acc&) {
-        const T tau = coef->tau;
-        const T xp = proj_box(sub_rn(q.x, mul_rn(tau, sub_rn(q.c, s))), q.lv, q.uv);
+        const StepCoef<T>& k = coef.get();
+        const T xp = proj_box(sub_rn(q.x, mul_rn(k.tau, sub_rn(q.c, s))), q.lv, q.uv);
         __stcs(xn + j, xp);
         xbar[j] = sub_rn(mul_rn(T(2), xp), q.x);
-        if (avg) __stcs(xa_new + j, add_rn(mul_rn(xp, coef->a), mul_rn(q.xa, coef->b)));
+        if (avg) __stcs(xa_new + j, add_rn(mul_rn(xp, k.a), mul_rn(q.xa, k.b)));
     }
     __device__ void row_long(int p, int j, T s, int, Acc& a) { row(p, j, s, pre_global(j), a); }
     __device__ void finish(Acc&) {}
 };
 
-template <class T>
+template <class T, bool BYVAL = false>
 struct DualEpi {
     const T* __restrict__ y;
     const T* __restrict__ lc;
@@ -77,33 +87,24 @@ struct DualEpi {
     T* __restrict__ yn;
     const T* __restrict__ ya_old;
     T* __restrict__ ya_new;
-    const StepCoef<T>* __restrict__ coef;
+    CoefSrc<T, BYVAL> coef;
     int avg;
     using Acc = NoAcc;
-    DualEpi shifted(unsigned) const { return *this; }
     struct Pre { T y, lc, uc, ya; };
-    static constexpr int NPRE = 4;
-    static constexpr int pre_esz(int) { return (int)sizeof(T); }
-    __device__ const void* pre_src(int k) const {
-        return k == 0 ? (const void*)y : k == 1 ? (const void*)lc : k == 2 ? (const void*)uc
-             : (avg ? (const void*)ya_old : nullptr);
-    }
     __device__ __forceinline__ Pre pre_global(int i) const {
         return Pre{ld_stream(y + i), ld_stream(lc + i), ld_stream(uc + i),
                    avg ? ld_stream(ya_old + i) : T(0)};
     }
-    __device__ __forceinline__ Pre pre_staged(const Staged<NPRE>& st, int i) const {
-        return Pre{st.template get<T>(0, i), st.template get<T>(1, i), st.template get<T>(2, i), avg ? st.template get<T>(3, i) : T(0)};
-    }
     __device__ void init(Acc&) {}
     __device__ __forceinline__ void row(int, int i, T s, const Pre& q, Acc&) {
-        const T sigma = coef->sigma;
+        const StepCoef<T>& k = coef.get();
+        const T sigma = k.sigma;
         const T t2 = sub_rn(q.y, mul_rn(sigma, s));
-        const T t4 = sub_rn(mul_rn(coef->inv_sigma, q.y), s);
+        const T t4 = sub_rn(mul_rn(k.inv_sigma, q.y), s);
         const T pr = proj_box(t4, -q.uc, -q.lc);
         const T yp = sub_rn(t2, mul_rn(sigma, pr));
         yn[i] = yp;
-        if (avg) __stcs(ya_new + i, add_rn(mul_rn(yp, coef->a), mul_rn(q.ya, coef->b)));
+        if (avg) __stcs(ya_new + i, add_rn(mul_rn(yp, k.a), mul_rn(q.ya, k.b)));
     }
     __device__ void row_long(int p, int i, T s, int, Acc& a) { row(p, i, s, pre_global(i), a); }
     __device__ void finish(Acc&) {}
@@ -119,20 +120,9 @@ struct KktRowEpi {
     double* block_out;
     double* long_out;
     struct Acc { double v[2 * NV]; };
-    KktRowEpi shifted(unsigned blocks) const {
-        KktRowEpi e = *this;
-        e.block_out += (size_t)blocks * 2 * NV;
-        return e;
-    }
     // inputs are read when the row is reduced (no prefetch): four iterates
     // per row would cost too many registers
     struct Pre {};
-    static constexpr int NPRE = 3 + NV;
-    static constexpr int pre_esz(int k) { return k == 2 ? 8 : (int)sizeof(T); }
-    __device__ const void* pre_src(int k) const {
-        return k == 0 ? (const void*)lc : k == 1 ? (const void*)uc : k == 2 ? (const void*)invD1
-                                                                           : (const void*)y[k - 3];
-    }
     __device__ void init(Acc& a) {
 #pragma unroll
         for (int q = 0; q < 2 * NV; q++) a.v[q] = 0.0;
@@ -143,7 +133,7 @@ struct KktRowEpi {
         const double sd = (double)s;
         const double d = __dmul_rn(invD1[i], __dsub_rn(sd, proj_box(sd, l, u)));
         pr2 = __dmul_rn(d, d);
-        const double yy = (double)y[p][i];
+        const double yy = (double)y[p][i];  // y[] is not restrict: a coherent load
         pc = __dsub_rn(safeprod_left(u, pos_part(-yy)), safeprod_left(l, neg_part(-yy)));
     }
     __device__ __forceinline__ void row(int p, int i, T s, const Pre&, Acc& a) {
@@ -172,18 +162,7 @@ struct KktColEpi {
     double* block_out;
     double* long_out;
     struct Acc { double v[3 * NV]; };
-    KktColEpi shifted(unsigned blocks) const {
-        KktColEpi e = *this;
-        e.block_out += (size_t)blocks * 3 * NV;
-        return e;
-    }
     struct Pre {};
-    static constexpr int NPRE = 4 + NV;
-    static constexpr int pre_esz(int k) { return k == 3 ? 8 : (int)sizeof(T); }
-    __device__ const void* pre_src(int k) const {
-        return k == 0 ? (const void*)c : k == 1 ? (const void*)lv : k == 2 ? (const void*)uv
-             : k == 3 ? (const void*)invD2 : (const void*)x[k - 4];
-    }
     __device__ void init(Acc& a) {
 #pragma unroll
         for (int q = 0; q < 3 * NV; q++) a.v[q] = 0.0;
@@ -225,17 +204,8 @@ struct PowerEpi {
     double* block_out;
     double* long_out;
     struct Acc { double v[2]; };
-    PowerEpi shifted(unsigned blocks) const {
-        PowerEpi e = *this;
-        e.block_out += (size_t)blocks * 2;
-        return e;
-    }
     struct Pre { T x; };
-    static constexpr int NPRE = 1;
-    static constexpr int pre_esz(int) { return (int)sizeof(T); }
-    __device__ const void* pre_src(int) const { return x; }
     __device__ Pre pre_global(int j) const { return Pre{ld_stream(x + j)}; }
-    __device__ Pre pre_staged(const Staged<NPRE>& st, int j) const { return Pre{st.template get<T>(0, j)}; }
     __device__ void init(Acc& a) { a.v[0] = a.v[1] = 0.0; }
     __device__ __forceinline__ void row(int, int j, T s, const Pre& q, Acc& a) {
         out[j] = s;
@@ -244,11 +214,10 @@ struct PowerEpi {
     }
     __device__ void row_long(int, int j, T s, int lid, Acc&) {
         out[j] = s;
-        long_out[(size_t)lid * 2] = (double)x[j] * (double)s;
+        long_out[(size_t)lid * 2] = (double)ld_stream(x + j) * (double)s;
         long_out[(size_t)lid * 2 + 1] = (double)s * (double)s;
     }
     __device__ void finish(Acc& a) { block_reduce_store<2>(a.v, block_out); }
 };
-
 
 }  // namespace cpdlp

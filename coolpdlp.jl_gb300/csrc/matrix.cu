@@ -16,15 +16,8 @@ struct MulEpi {  // c[i] = alpha*s + beta*c[i]; beta == 0 does not read c (mat_c
     T alpha, beta;
     int use_beta;
     struct Acc {};
-    MulEpi shifted(unsigned) const { return *this; }
     struct Pre { T c; };
-    static constexpr int NPRE = 1;
-    static constexpr int pre_esz(int) { return (int)sizeof(T); }
-    __device__ const void* pre_src(int) const { return use_beta ? (const void*)out : nullptr; }
     __device__ Pre pre_global(int r) const { return Pre{use_beta ? out[r] : T(0)}; }
-    __device__ Pre pre_staged(const Staged<NPRE>& st, int r) const {
-        return Pre{use_beta ? st.template get<T>(0, r) : T(0)};
-    }
     __device__ void init(Acc&) {}
     __device__ __forceinline__ void row(int, int r, T s, const Pre& q, Acc&) {
         T v = mul_rn(alpha, s);

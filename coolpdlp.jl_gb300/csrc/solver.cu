@@ -597,7 +597,6 @@ struct StateT : StateBase {
         }
         while (count-- > 0) run_single();
         CK(cudaStreamSynchronize(h->stream));
-        check_tile_error(h->stream);
     }
 
     // KKT errors (errors.jl:65-109) of NV (x, y) pairs: one row-side and one
@@ -633,7 +632,6 @@ struct StateT : StateBase {
         double* pin = h->pinned_area(sizeof(double) * 64);
         CK(cudaMemcpyAsync(pin, P.red_out.p, sizeof(double) * 5 * NV, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
-        check_tile_error(s);
         for (int p = 0; p < NV; p++) {
             const double pr2 = pin[2 * p], pc = pin[2 * p + 1];
             const double du2 = pin[2 * NV + 3 * p], pv = pin[2 * NV + 3 * p + 1],

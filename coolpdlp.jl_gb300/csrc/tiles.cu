@@ -22,7 +22,9 @@ int choose_items(int64_t nnz, int64_t rows, int requested_tile_nnz) {
 void build_tile_plan(const std::vector<int32_t>& ptr, int32_t rows, int items, TilePlan& plan,
                      cudaStream_t s, const std::vector<int64_t>* seg_rows,
                      std::vector<int32_t>* seg_tasks, std::vector<int32_t>* seg_ltasks,
-                     std::vector<int32_t>* seg_lids) {
+                     std::vector<int32_t>* seg_lids, int max_rows) {
+    if (max_rows < 32 || max_rows > MAX_TILE_ROWS || max_rows % 32 != 0)
+        fail(CPDLP_ERR_ARGUMENT, "tile row cap must be a multiple of 32 up to 128");
     plan.rows = rows;
     plan.items = items;
     const int tile = 32 * items;
@@ -54,7 +56,7 @@ void build_tile_plan(const std::vector<int32_t>& ptr, int32_t rows, int items, T
                 continue;
             }
             int32_t r0 = r, nz = 0;
-            while (r < end && r - r0 < MAX_TILE_ROWS) {
+            while (r < end && r - r0 < max_rows) {
                 int32_t l = ptr[r + 1] - ptr[r];
                 if (l > LONG_ROW || nz + l > tile) break;
                 nz += l;
@@ -82,31 +84,6 @@ void build_tile_plan(const std::vector<int32_t>& ptr, int32_t rows, int items, T
     plan.counters.alloc(plan.nlong ? (size_t)plan.nlong : 1);
     CK(cudaMemsetAsync(plan.counters.p, 0, sizeof(int32_t) * plan.counters.n, s));
     CK(cudaStreamSynchronize(s));
-}
-
-namespace {
-__device__ int g_tile_error = 0;
-}  // namespace
-
-int* tile_error_word() {
-    int dev = 0;
-    CK(cudaGetDevice(&dev));
-    static int* addr[64] = {nullptr};
-    if (dev < 0 || dev >= 64) fail(CPDLP_ERR_UNSUPPORTED, "device ordinal above 63");
-    if (!addr[dev]) CK(cudaGetSymbolAddress((void**)&addr[dev], g_tile_error));
-    return addr[dev];
-}
-
-void check_tile_error(cudaStream_t s) {
-    int* w = tile_error_word();
-    int h = 0;
-    CK(cudaMemcpyAsync(&h, w, sizeof(int), cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    if (h) {
-        CK(cudaMemsetAsync(w, 0, sizeof(int), s));
-        CK(cudaStreamSynchronize(s));
-        fail(CPDLP_ERR_TIMEOUT, "a tile kernel timed out waiting for its staged data");
-    }
 }
 
 namespace {

@@ -52,11 +52,13 @@ struct TilePlan {
 // With seg_rows (segment start rows, last = rows) no tile crosses a segment
 // start, and seg_tasks / seg_ltasks / seg_lids receive, per segment, the first
 // short task, long task and long-row id (one extra final entry = totals).
+// max_rows caps the rows of a short tile (a multiple of 32, at most
+// MAX_TILE_ROWS): kernels built for max_rows / 32 rows per lane.
 void build_tile_plan(const std::vector<int32_t>& ptr, int32_t rows, int items, TilePlan& plan,
                      cudaStream_t s, const std::vector<int64_t>* seg_rows = nullptr,
                      std::vector<int32_t>* seg_tasks = nullptr,
                      std::vector<int32_t>* seg_ltasks = nullptr,
-                     std::vector<int32_t>* seg_lids = nullptr);
+                     std::vector<int32_t>* seg_lids = nullptr, int max_rows = MAX_TILE_ROWS);
 
 // Picks nonzeros-per-lane from the size and mean row length (autotuner default).
 int choose_items(int64_t nnz, int64_t rows, int requested_tile_nnz);
@@ -74,7 +76,11 @@ struct CsrView {
     T* partials;   // npieces * NVEC
 };
 
-template <class T, int NVEC>
+// The input vectors of one product.  COH = false gathers them through the
+// non-coherent read-only path, valid when nothing in the same launch writes
+// them (one product per launch).  COH = true uses coherent loads, for kernels
+// that rewrite the vectors between products (the batched solver's step loop).
+template <class T, int NVEC, bool COH = false>
 struct VecSet {
     const T* v[NVEC];
 };
@@ -111,16 +117,20 @@ __device__ __forceinline__ void load4v(const int8_t* p, T (&o)[4]) {
     o[0] = (T)(int8_t)(v & 0xff); o[1] = (T)(int8_t)((v >> 8) & 0xff);
     o[2] = (T)(int8_t)((v >> 16) & 0xff); o[3] = (T)(int8_t)((v >> 24) & 0xff);
 }
-// gathers of x[col] through the read-only path; same ordering property as
-// the loads above
+// gathers of x[col]: through the read-only path (COH = false) or with a
+// coherent load (COH = true); same ordering property as the loads above
+template <bool COH>
 __device__ __forceinline__ float gather(const float* p) {
     float v;
-    asm volatile("ld.global.nc.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    if (COH) asm volatile("ld.global.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    else asm volatile("ld.global.nc.f32 %0, [%1];" : "=f"(v) : "l"(p));
     return v;
 }
+template <bool COH>
 __device__ __forceinline__ double gather(const double* p) {
     double v;
-    asm volatile("ld.global.nc.f64 %0, [%1];" : "=d"(v) : "l"(p));
+    if (COH) asm volatile("ld.global.f64 %0, [%1];" : "=d"(v) : "l"(p));
+    else asm volatile("ld.global.nc.f64 %0, [%1];" : "=d"(v) : "l"(p));
     return v;
 }
 template <class V, class T>
@@ -143,94 +153,29 @@ __device__ __forceinline__ T warp_sum_tree(T v) {
     return v;
 }
 
-// ---- TMA bulk copies and mbarriers (PTX) -------------------------------------
-__device__ __forceinline__ uint32_t smem_addr(const void* p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void mbar_init(uint64_t* m, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(m)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void fence_mbar_init() {
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* m, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(m)),
-                 "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* m, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_addr(m)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// 1-D bulk copy global -> shared (TMA engine), completion counted on `m`.
-// src, dst and bytes must be multiples of 16.
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* m) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-            smem_addr(dst)),
-        "l"(src), "r"(bytes), "r"(smem_addr(m))
-        : "memory");
-}
+// GPU wall clock in nanoseconds
 __device__ __forceinline__ uint64_t global_ns() {
     uint64_t t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
 }
-// Waits for phase `parity` of `m` for at most ~1 s (wall clock on the GPU) and
-// at most 2^30 polls; returns false on timeout.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* m, uint32_t parity) {
-    if (mbar_try_wait(m, parity)) return true;
-    const uint64_t t0 = global_ns();
-    for (uint32_t it = 0; it < (1u << 30); it++) {
-        if (mbar_try_wait(m, parity)) return true;
-        if ((it & 255u) == 0 && global_ns() - t0 > 1000000000ull) break;
-    }
-    return false;
-}
-
-// Epilogue interface (per row r, per input vector p):
-//   static constexpr int NPRE;               number of per-row input vectors
-//   const void* pre_src(int k) const;       global base of input k (nullptr: skip)
-//   static constexpr int pre_esz(int k);    its element size (4 or 8 bytes)
-//   struct Pre;                              the inputs of one row
-//   Pre pre_global(int r) const;            read from global memory
-//   Pre pre_staged(Staged<NPRE>, int r);    read from the staged shared copy
-//   void row(int p, int r, T s, const Pre&, Acc&)   short-tile rows
-//   void row_long(int p, int r, T s, int lid, Acc&)  long rows (one lane)
-//   void init(Acc&); void finish(Acc&);             block reductions
-template <int NPRE>
-struct Staged {
-    const unsigned char* base[NPRE > 0 ? NPRE : 1];
-    int first[NPRE > 0 ? NPRE : 1];
-    template <class E>
-    __device__ __forceinline__ E get(int k, int r) const {
-        return reinterpret_cast<const E*>(base[k])[r - first[k]];
-    }
-};
 
 // One warp, one short tile.  All loads of a phase are volatile PTX issued back
 // to back, so they are in flight together: (1) the tile's indices and values
 // with 128-bit loads over the 4-element-aligned window plus the row pointers
 // and epilogue inputs of this lane's rows, (2) one batch of gathers.  Then
 // products go to shared memory and every lane reduces whole rows in column
-// order before the fused epilogue.
-template <int ITEMS, int NVEC, class V, class T, class Epi>
-__device__ __forceinline__ void short_tile(const CsrView<V, T>& A, const VecSet<T, NVEC>& xs,
+// order before the fused epilogue.  RPL: rows per lane, the plan's row cap / 32.
+template <int ITEMS, int NVEC, class V, class T, class Epi, bool COH, int RPL = ROWS_PER_LANE>
+__device__ __forceinline__ void short_tile(const CsrView<V, T>& A, const VecSet<T, NVEC, COH>& xs,
                                            Epi& epi, typename Epi::Acc& acc, int r0, int r1,
                                            int nz0, int nz1, int lane, T* prod) {
     constexpr int NV4 = ITEMS / 4 + 1;  // 4-element chunks per lane (+1: alignment slack)
     const int base = nz0 & ~3;
-    int ra[ROWS_PER_LANE], rb[ROWS_PER_LANE];
-    typename Epi::Pre pre[ROWS_PER_LANE];
+    int ra[RPL], rb[RPL];
+    typename Epi::Pre pre[RPL];
 #pragma unroll
-    for (int k = 0; k < ROWS_PER_LANE; k++) {
+    for (int k = 0; k < RPL; k++) {
         const int r = r0 + lane + 32 * k;
         if (r < r1) {
             ra[k] = ld_keep(A.ptr + r);
@@ -263,7 +208,7 @@ __device__ __forceinline__ void short_tile(const CsrView<V, T>& A, const VecSet<
             const int e = base + 4 * (lane + 32 * j);
 #pragma unroll
             for (int q = 0; q < 4; q++)
-                xg[j][q] = (e + q >= nz0 && e + q < nz1) ? gather(xs.v[p] + cc[j][q])
+                xg[j][q] = (e + q >= nz0 && e + q < nz1) ? gather<COH>(xs.v[p] + cc[j][q])
                                                          : T(0);
         }
 #pragma unroll
@@ -275,7 +220,7 @@ __device__ __forceinline__ void short_tile(const CsrView<V, T>& A, const VecSet<
         }
         __syncwarp();
 #pragma unroll
-        for (int k = 0; k < ROWS_PER_LANE; k++) {
+        for (int k = 0; k < RPL; k++) {
             const int r = r0 + lane + 32 * k;
             if (r < r1) {
                 T sum = T(0);
@@ -292,8 +237,8 @@ __device__ __forceinline__ void short_tile(const CsrView<V, T>& A, const VecSet<
 // combine through scratch slots: the warp that completes the row (atomic
 // counter, no waiting) adds the partials in piece order and applies the
 // epilogue.
-template <int ITEMS, int NVEC, class V, class T, class Epi>
-__device__ __forceinline__ void long_piece(const CsrView<V, T>& A, const VecSet<T, NVEC>& xs,
+template <int ITEMS, int NVEC, class V, class T, class Epi, bool COH>
+__device__ __forceinline__ void long_piece(const CsrView<V, T>& A, const VecSet<T, NVEC, COH>& xs,
                                            Epi& epi, typename Epi::Acc& acc, int4 t, int lane) {
     constexpr int TILE = 32 * ITEMS;
     const int row = t.x, piece = -t.y - 1, lid = t.z, base_slot = t.w;
@@ -308,7 +253,7 @@ __device__ __forceinline__ void long_piece(const CsrView<V, T>& A, const VecSet<
         const T vv = load1v<V, T>(A.val + e);
         const int cc = __ldcs(A.idx + e);
 #pragma unroll
-        for (int p = 0; p < NVEC; p++) s[p] = add_rn(s[p], mul_rn(vv, __ldg(xs.v[p] + cc)));
+        for (int p = 0; p < NVEC; p++) s[p] = add_rn(s[p], mul_rn(vv, gather<COH>(xs.v[p] + cc)));
     }
 #pragma unroll
     for (int p = 0; p < NVEC; p++) s[p] = warp_sum_tree(s[p]);
@@ -362,12 +307,6 @@ __global__ void __launch_bounds__(WARPS * 32)
 }
 
 constexpr int TILE_WARPS = 8;
-
-// The device error word that bounded waits in this library report into.
-int* tile_error_word();
-// Reads (and clears) the error word on `s`; throws Error(CPDLP_ERR_TIMEOUT)
-// if a kernel gave up a bounded wait.
-void check_tile_error(cudaStream_t s);
 
 // Launches the tile kernel on `s`.  Reducing epilogues write one row of
 // block partials per block.

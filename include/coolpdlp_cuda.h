@@ -170,6 +170,7 @@ typedef struct cpdlp_handle cpdlp_handle;
 typedef struct cpdlp_matrix cpdlp_matrix;
 typedef struct cpdlp_problem cpdlp_problem;
 typedef struct cpdlp_state cpdlp_state;
+typedef struct cpdlp_job cpdlp_job;
 
 /* ---- library & handle ----------------------------------------------------- */
 int cpdlp_abi_version(void);
@@ -316,10 +317,44 @@ int cpdlp_spmv_csr_noalloc(cpdlp_handle* h, int64_t m, int64_t n, int64_t nnz,
  * No counterpart in the reference, which solves one LP per call: this is the
  * batched form of solve(milp, algo) (common.jl:203-209) over `count` LPs.
  * x_out[k] / y_out[k] receive LP k's solution (NULL pointers skip the copy);
- * stats[k] its ConvergenceStats.  All LPs share `params`. */
+ * stats[k] its ConvergenceStats.  All LPs share `params`.  One CTA solves
+ * one LP, so an LP's result does not depend on the other LPs of the call.
+ * With float_type CPDLP_VAL_F32 and refine_reltol > 0, every LP that reaches
+ * termination_reltol continues in FP64 to refine_reltol, warm-started from
+ * its FP32 solution (as cpdlp_solve does for one LP). */
 int cpdlp_batch_solve(cpdlp_handle* h, int64_t count, const cpdlp_lp* lps,
                       const cpdlp_params* params, double* const* x_out,
                       double* const* y_out, cpdlp_stats* stats);
+
+/* ---- asynchronous jobs (continuous batching) -------------------------------
+ * No counterpart in the reference.  cpdlp_submit copies the LPs (the caller
+ * may free them on return), preprocesses them on the job's own CUDA stream,
+ * launches the persistent solve kernel and returns without waiting for it;
+ * jobs submitted while others run share the GPU (the CTAs of a finishing job
+ * hand their SMs to the others).  reltol: `count` target relative KKT
+ * errors, or NULL for params->termination_reltol (refine_reltol for FP32 with
+ * refine_reltol > 0).  With FP32 iterates, LPs whose target is below
+ * termination_reltol stop there in FP32 and finish in an FP64 phase
+ * warm-started from the FP32 solution.  x0 / y0: `count` warm starts in
+ * original units (NULL, or NULL entries, for a cold start).
+ * cpdlp_poll never blocks: *done = 1 once every LP is finished (it also
+ * launches the FP64 phase when the first one ends).  cpdlp_cancel makes the
+ * job's kernels stop at their next termination check: unfinished LPs report
+ * CPDLP_STILL_RUNNING.  cpdlp_collect (after done) copies x / y / stats per
+ * LP like cpdlp_batch_solve.  cpdlp_job_destroy waits for the job's GPU work.
+ * cpdlp_batch_footprint: upper bound of the device bytes a job over these LPs
+ * holds (admission control); -1 on invalid arguments. */
+int cpdlp_submit(cpdlp_handle* h, int64_t count, const cpdlp_lp* lps,
+                 const cpdlp_params* params, const double* reltol,
+                 const double* const* x0, const double* const* y0, cpdlp_job** out);
+int cpdlp_poll(cpdlp_handle* h, cpdlp_job* job, int32_t* done);
+int cpdlp_wait(cpdlp_handle* h, cpdlp_job* job);
+int cpdlp_cancel(cpdlp_handle* h, cpdlp_job* job);
+int cpdlp_collect(cpdlp_handle* h, cpdlp_job* job, double* const* x_out,
+                  double* const* y_out, cpdlp_stats* stats);
+int64_t cpdlp_job_count(const cpdlp_job* job);
+int cpdlp_job_destroy(cpdlp_job* job);
+int64_t cpdlp_batch_footprint(int64_t count, const cpdlp_lp* lps, const cpdlp_params* params);
 
 #ifdef __cplusplus
 }
