@@ -50,6 +50,13 @@ def parse_args():
                     help="shrink the workload (testing only; 1.0 = the named workload)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--batch-lps", type=int, default=4096,
+                    help="LPs of the batched workload (0 skips the batch measurement)")
+    ap.add_argument("--sequential-sample", type=int, default=32,
+                    help="LPs of the batch solved one at a time by the FP64 path")
+    ap.add_argument("--serve-requests", type=int, default=240,
+                    help="requests of the served stream (0 skips the serving measurement)")
+    ap.add_argument("--serve-rate", type=float, default=60.0, help="Poisson arrivals per second")
     return ap.parse_args()
 
 
@@ -161,6 +168,85 @@ def cpu_baseline(lp, budget_s: float = 20.0) -> dict:
             "kind": "port",
             "sample": (f"{iters} PDLP iterations (FP64) of the same LP after "
                        f"{t_setup:.1f} s of untimed preprocessing"), "seconds": t}
+
+
+def measure_batch(h, count: int, sample: int) -> dict:
+    """LPs/s to 1e-4 relative KKT on `count` random sparse LPs (m log-U[50,5000],
+    n = 2m, 3-8 nonzeros per column, seed 1000 + i): the batched solver with
+    FP32 iterates (stalled FP32 LPs finish in its FP64 phase) and with FP64
+    iterates, against the plain FP64 one-LP-at-a-time path (cpdlp_solve) on an
+    evenly spaced sample of the same LPs.  Every result's relative KKT error
+    is read back and checked; objectives are compared with the FP64 batch."""
+    import numpy as np
+    from coolpdlp import _abi as A
+    from coolpdlp import generators as G
+    from coolpdlp import native
+    lps = G.batch_lps(count)
+    S = [native.LPStruct(lp.m, lp.n, lp.colptr, lp.rowval, lp.nzval, lp.c, lp.lv, lp.uv, lp.lc,
+                         lp.uc) for lp in lps]
+    warm = native.default_params()
+    native.batch_solve(h, S[:4], warm)          # loads the kernels
+    out = {"lps": count, "nnz_total": int(sum(lp.nnz for lp in lps))}
+    res = {}
+    for name, ft in (("fp32_refined", A.VAL_F32), ("fp64_batched", A.VAL_F64)):
+        p = native.default_params()
+        p.float_type = ft
+        t0 = time.perf_counter()
+        xs, ys, st = native.batch_solve(h, S, p)
+        dt = time.perf_counter() - t0
+        rel = np.array([max(s.err.primal / s.err.primal_scale, s.err.dual / s.err.dual_scale,
+                            s.err.gap / s.err.gap_scale) for s in st])
+        res[name] = xs
+        out[name] = {"lps_per_s": count / dt, "seconds": dt,
+                     "optimal": int(sum(s.termination_status == 0 for s in st)),
+                     "max_rel_kkt": float(np.nanmax(rel)),
+                     "fp64_phase_lps": int(sum(s.refine_kkt_passes > 0 for s in st)),
+                     "mean_passes": float(np.mean([s.kkt_passes for s in st]))}
+    obj = lambda k, x: float(np.dot(lps[k].c, x))
+    out["max_obj_rel_diff_fp32_vs_fp64"] = float(max(
+        abs(obj(k, res["fp32_refined"][k]) - obj(k, res["fp64_batched"][k]))
+        / max(1.0, abs(obj(k, res["fp64_batched"][k]))) for k in range(count)))
+    idx = list(range(0, count, max(1, count // max(sample, 1))))[:sample]
+    p = native.default_params()
+    t0 = time.perf_counter()
+    passes = 0
+    for k in idx:
+        _, _, s1 = native.solve_lp(h, S[k], p)
+        passes += s1.kkt_passes
+    dt = time.perf_counter() - t0
+    seq = len(idx) / dt
+    out["fp64_sequential"] = {"lps_per_s": seq, "sample": len(idx), "seconds": dt,
+                              "mean_passes": passes / len(idx)}
+    out["speedup_fp32_refined_vs_sequential"] = out["fp32_refined"]["lps_per_s"] / seq
+    out["speedup_fp64_batched_vs_sequential"] = out["fp64_batched"]["lps_per_s"] / seq
+    out["workload"] = (f"{count} random sparse LPs, m log-U[50,5000], n=2m, 3-8 nnz/column, "
+                       "seed 1000+i, 1e-4 relative KKT")
+    return out
+
+
+def measure_serving(requests: int, rate: float) -> dict:
+    """The served stream: Poisson arrivals, 80% random sparse LPs (m log-U[100,
+    20000]) and 20% grid multicommodity flows (side U{32..128}, K U{2..8}),
+    tolerance 1e-4 or 1e-8; replayed in real time through the continuous-
+    batching server with FP32+FP64-refined and with plain FP64 iterates."""
+    from coolpdlp import _abi as A
+    from coolpdlp import generators as G
+    from coolpdlp import serving
+    reqs = G.served_stream(requests, rate, seed=7)
+    t0 = time.perf_counter()
+    lps = [G.request_lp(r) for r in reqs]
+    gen_s = time.perf_counter() - t0
+    out = {"requests": requests, "rate_per_s": rate, "generation_s": gen_s,
+           "workload": (f"{requests} Poisson arrivals at {rate}/s: 80% random sparse LPs "
+                        "m log-U[100,20000] n=2m 5 nnz/col, 20% grid multicommodity flows "
+                        "side U{32..128} K U{2..8}; tolerance 1e-4 or 1e-8; "
+                        "150 GB admission budget")}
+    for name, ft in (("fp32_refined", A.VAL_F32), ("fp64", A.VAL_F64)):
+        srv = serving.Server(float_type=ft, hbm_budget=150e9)
+        r = serving.replay(srv, [q.arrival for q in reqs], lps, [q.reltol for q in reqs])
+        srv.close()
+        out[name] = r
+    return out
 
 
 def run_reference(args):
@@ -336,6 +422,10 @@ def run_ours(args):
         }
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(lp)
+        if args.batch_lps > 0:
+            line["batch"] = measure_batch(h, args.batch_lps, args.sequential_sample)
+        if args.serve_requests > 0:
+            line["serving"] = measure_serving(args.serve_requests, args.serve_rate)
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.barrier()

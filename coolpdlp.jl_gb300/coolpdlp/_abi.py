@@ -162,7 +162,8 @@ EXPORTED_SYMBOLS = (
     "cpdlp_batch_solve", "cpdlp_state_solve_blocks", "cpdlp_state_profile",
     "cpdlp_state_kernel_bytes", "cpdlp_spmv_csr_noalloc",
     "cpdlp_submit", "cpdlp_poll", "cpdlp_wait", "cpdlp_cancel", "cpdlp_collect",
-    "cpdlp_job_count", "cpdlp_job_destroy", "cpdlp_batch_footprint",
+    "cpdlp_job_count", "cpdlp_job_destroy", "cpdlp_batch_footprint", "cpdlp_job_ready",
+    "cpdlp_collect_lp",
 )
 
 _LIB = None
@@ -210,12 +211,14 @@ def _declare(lib):
                                              c_void_p, c_int32, c_void_p, c_void_p, c_double,
                                              c_double]),
         "cpdlp_submit": (c_int32, [H, c_int64, POINTER(LPC), POINTER(ParamsC), PD,
-                                   POINTER(PD), POINTER(PD), POINTER(H)]),
+                                   POINTER(PD), POINTER(PD), c_int64, POINTER(H)]),
         "cpdlp_poll": (c_int32, [H, H, POINTER(c_int32)]),
         "cpdlp_wait": (c_int32, [H, H]),
         "cpdlp_cancel": (c_int32, [H, H]),
         "cpdlp_collect": (c_int32, [H, H, POINTER(PD), POINTER(PD), POINTER(StatsC)]),
         "cpdlp_job_count": (c_int64, [H]),
+        "cpdlp_job_ready": (c_int32, [H, H, POINTER(c_int32)]),
+        "cpdlp_collect_lp": (c_int32, [H, H, c_int64, PD, PD, POINTER(StatsC)]),
         "cpdlp_job_destroy": (c_int32, [H]),
         "cpdlp_batch_footprint": (c_int64, [c_int64, POINTER(LPC), POINTER(ParamsC)]),
     }

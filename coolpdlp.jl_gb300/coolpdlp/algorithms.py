@@ -31,6 +31,10 @@ TIME_LIMIT = TerminationStatus.TIME_LIMIT
 ITERATION_LIMIT = TerminationStatus.ITERATION_LIMIT
 STILL_RUNNING = TerminationStatus.STILL_RUNNING
 
+# FP32 iterates whose relative KKT error has not halved over this many checks
+# continue in FP64 when refine_reltol > 0 (the library's rule, solver.cuh)
+STALL_CHECKS = 30
+
 
 @dataclasses.dataclass(frozen=True)
 class KKTErrors:
@@ -241,13 +245,30 @@ def solve(milp: MILP, *args):
         return PrimalDualSolution(x, y), _stats_from(st, [], t0)
     dmilp, sol = preprocess(milp, sol, algo)
     state = initialize(dmilp, sol, algo, starting_time=t0)
-    solve_inplace(state)
+    p = algo.params
+    mixed = p.float_type == A.VAL_F32 and p.refine_reltol > 0
+    stalled = False
+    if mixed:
+        # FP32 phase one check at a time: iterates whose relative KKT error has
+        # not halved over STALL_CHECKS checks continue in FP64 (as cpdlp_solve)
+        best, mark = math.inf, 0
+        while True:
+            s_now = state.native.solve_blocks(1)
+            if s_now.termination_status != A.STILL_RUNNING:
+                break
+            rel = relative(KKTErrors.from_c(s_now.err))
+            if rel < 0.5 * best:
+                best, mark = rel, s_now.kkt_passes
+            elif s_now.kkt_passes - mark >= STALL_CHECKS * p.check_every:
+                stalled = True
+                break
+    else:
+        solve_inplace(state)
     stats = state.stats()
     sol_out = state.solution()
-    p = algo.params
-    if (p.float_type == A.VAL_F32 and p.refine_reltol > 0
-            and stats.termination_status == OPTIMAL):
-        # FP64 refinement: continue from the FP32 solution in Float64 until
+    if mixed and ((stats.termination_status == OPTIMAL
+                   and p.refine_reltol < p.termination_reltol) or stalled):
+        # FP64 phase: continue from the FP32 solution in Float64 until
         # refine_reltol (same scaling, recomputed in FP64)
         kw = algo.kwargs()
         kw.update(termination_reltol=p.refine_reltol,

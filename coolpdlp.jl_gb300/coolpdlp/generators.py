@@ -356,3 +356,49 @@ def random_milp_and_sol(m: int, n: int, p: float, seed: int = 0):
     lp = LPData(m, n, colptr, rowval, nzval, c, lv, uv, lc, uc,
                 name=f"random_milp(m={m},n={n},p={p},seed={seed})")
     return lp, x, y
+
+
+@dataclasses.dataclass
+class ServedRequest:
+    rid: int
+    arrival: float          # seconds from the start of the stream
+    reltol: float
+    kind: str               # "sparse" (m) or "flow" (side, K)
+    seed: int
+    m: int = 0
+    side: int = 0
+    K: int = 0
+
+
+def served_stream(count: int, rate: float, seed: int = 7, m_lo: int = 100, m_hi: int = 20000,
+                  side_lo: int = 32, side_hi: int = 128, k_lo: int = 2, k_hi: int = 8,
+                  flow_frac: float = 0.2, tols=(1e-4, 1e-8)) -> list[ServedRequest]:
+    """A served stream of LPs: Poisson arrivals at `rate` per second; each
+    request is, with probability 1 - flow_frac, a random sparse LP (m
+    log-uniform in [m_lo, m_hi], n = 2m, 5 nonzeros per column) and otherwise
+    a grid multicommodity flow LP (side uniform in {side_lo..side_hi}, K uniform
+    in {k_lo..k_hi}); its tolerance is drawn uniformly from `tols`.  LPs are
+    built lazily by the caller through ``request_lp`` to bound memory."""
+    st = Stream(seed, 21)
+    gaps = -np.log(st.uniform_open0(count)) / rate
+    arrivals = np.cumsum(gaps) - gaps[0]
+    kind = st.uniform(count) < flow_frac
+    out = []
+    for i in range(count):
+        s = seed * 1_000_003 + i
+        tol = tols[int(st.integers(1, 0, len(tols))[0])]
+        if kind[i]:
+            side = int(st.integers(1, side_lo, side_hi + 1)[0])
+            K = int(st.integers(1, k_lo, k_hi + 1)[0])
+            out.append(ServedRequest(i, float(arrivals[i]), tol, "flow", s, side=side, K=K))
+        else:
+            m = int(round(np.exp(st.uniform(1, np.log(m_lo), np.log(m_hi))[0])))
+            out.append(ServedRequest(i, float(arrivals[i]), tol, "sparse", s, m=m))
+    return out
+
+
+def request_lp(req: ServedRequest) -> LPData:
+    """Builds the LP a served request names (see ``served_stream``)."""
+    if req.kind == "flow":
+        return multicommodity_flow_lp(side=req.side, K=req.K, seed=req.seed)
+    return random_sparse_lp(req.m, 2 * req.m, 5, seed=req.seed)

@@ -86,6 +86,12 @@ def default_params(algorithm: int = A.ALGO_PDLP) -> A.ParamsC:
     return p
 
 
+def copy_params(p: A.ParamsC) -> A.ParamsC:
+    q = A.ParamsC()
+    ctypes.memmove(ctypes.addressof(q), ctypes.addressof(p), ctypes.sizeof(A.ParamsC))
+    return q
+
+
 class LPStruct:
     """A cpdlp_lp pointing at numpy arrays that it keeps alive."""
 
@@ -254,7 +260,7 @@ class Job:
     caller continues.  poll() never blocks; result() waits and collects."""
 
     def __init__(self, handle: Handle, lps: list, params: A.ParamsC, reltol=None,
-                 x0=None, y0=None):
+                 x0=None, y0=None, max_ctas: int = 0):
         self.handle = handle
         self.j = None
         self.k = len(lps)
@@ -274,7 +280,8 @@ class Job:
             y0p = (_PD * max(self.k, 1))(*[_pd(v) for v in ys])
         out = c_void_p()
         handle.check(handle.lib.cpdlp_submit(handle.h, self.k, arr, byref(params), _pd(rt),
-                                             x0p, y0p, byref(out)), "cpdlp_submit")
+                                             x0p, y0p, int(max_ctas), byref(out)),
+                     "cpdlp_submit")
         self.j = out.value
         self._keep = None
 
@@ -301,6 +308,21 @@ class Job:
         self.handle.check(self.handle.lib.cpdlp_collect(self.handle.h, self.j, xp, yp, st),
                           "cpdlp_collect")
         return xs, ys, [st[i] for i in range(self.k)]
+
+    def ready(self) -> np.ndarray:
+        """per LP: finished as of the last poll()"""
+        r = np.zeros(max(self.k, 1), dtype=np.int32)
+        self.handle.check(self.handle.lib.cpdlp_job_ready(
+            self.handle.h, self.j, r.ctypes.data_as(POINTER(c_int32))), "cpdlp_job_ready")
+        return r[:self.k].astype(bool)
+
+    def collect_lp(self, k: int):
+        """x, y, StatsC of finished LP k"""
+        m, n = self.shapes[k]
+        x, y, st = np.empty(n), np.empty(m), A.StatsC()
+        self.handle.check(self.handle.lib.cpdlp_collect_lp(self.handle.h, self.j, int(k), _pd(x),
+                                                           _pd(y), byref(st)), "cpdlp_collect_lp")
+        return x, y, st
 
     def close(self):
         if getattr(self, "j", None):

@@ -110,6 +110,7 @@ int cpdlp_destroy(cpdlp_handle* h) {
         cudaStreamDestroy(h->stream);
     }
     if (h->pinned) cudaFreeHost(h->pinned);
+    h->host_release_all();
     delete h;
     return CPDLP_OK;
 }
@@ -344,12 +345,13 @@ int cpdlp_batch_solve(cpdlp_handle* h, int64_t count, const cpdlp_lp* lps,
 
 int cpdlp_submit(cpdlp_handle* h, int64_t count, const cpdlp_lp* lps, const cpdlp_params* params,
                  const double* reltol, const double* const* x0, const double* const* y0,
-                 cpdlp_job** out) {
+                 int64_t max_ctas, cpdlp_job** out) {
     NEED(h);
     if (!out) return CPDLP_ERR_ARGUMENT;
     *out = nullptr;
     return guarded(h, [&] {
-        *out = reinterpret_cast<cpdlp_job*>(job_submit(*H(h), count, lps, params, reltol, x0, y0));
+        *out = reinterpret_cast<cpdlp_job*>(
+            job_submit(*H(h), count, lps, params, reltol, x0, y0, max_ctas));
     });
 }
 
@@ -376,6 +378,19 @@ int cpdlp_collect(cpdlp_handle* h, cpdlp_job* job, double* const* x_out, double*
     NEED(h);
     if (!job) return CPDLP_ERR_ARGUMENT;
     return guarded(h, [&] { job_collect(reinterpret_cast<Job*>(job), x_out, y_out, stats); });
+}
+
+int cpdlp_job_ready(cpdlp_handle* h, const cpdlp_job* job, int32_t* ready) {
+    NEED(h);
+    if (!job || !ready) return CPDLP_ERR_ARGUMENT;
+    return guarded(h, [&] { job_ready(reinterpret_cast<const Job*>(job), ready); });
+}
+
+int cpdlp_collect_lp(cpdlp_handle* h, cpdlp_job* job, int64_t k, double* x_out, double* y_out,
+                     cpdlp_stats* stats) {
+    NEED(h);
+    if (!job) return CPDLP_ERR_ARGUMENT;
+    return guarded(h, [&] { job_collect_lp(reinterpret_cast<Job*>(job), k, x_out, y_out, stats); });
 }
 
 int64_t cpdlp_job_count(const cpdlp_job* job) {

@@ -40,9 +40,6 @@ constexpr int BW = TILE_WARPS;  // warps per CTA
 constexpr int BT = BW * 32;
 constexpr int BATCH_ITEMS = 4;  // default nonzeros per lane of a short tile (128-nonzero tiles)
 constexpr int BATCH_RPL = 1;    // rows per lane: short tiles of at most 32 rows
-// FP32 iterates whose relative KKT error has not halved over this many checks
-// hand the LP to the FP64 phase (warm-started from where they stopped)
-constexpr int64_t FP32_STALL_CHECKS = 30;
 #ifndef CPDLP_BATCH_MINB
 #define CPDLP_BATCH_MINB 2      // resident CTAs per SM the solve kernel is compiled for
 #endif
@@ -83,9 +80,12 @@ struct BatchArgs {
     const double* y_init;
     const BatchLP* lps;
     const int32_t* order;    // queue order of the LPs
+    // results, in mapped host memory: each LP's result and solution are
+    // visible to the host once its done flag is set
     BatchResult* res;
     double* out_x;
     double* out_y;
+    int* done;
     double* longA;    // row-side long-row terms (2 per long row of A)
     double* longAt;   // column-side long-row terms (3 per long row of A')
     int* next;
@@ -429,6 +429,8 @@ __device__ __forceinline__ void solve_one(const BatchArgs<T>& g, BatchCtl& C, T*
     // ---- get_solution (common.jl:233-235): unscaled, double
     for (int j = c0 + tid; j < c1; j += BT) g.out_x[j] = g.D2[j] * (double)g.x[cur][j];
     for (int i = r0 + tid; i < r1; i += BT) g.out_y[i] = g.D1[i] * (double)g.y[cur][i];
+    __threadfence_system();
+    __syncthreads();
     if (tid == 0) {
         BatchResult R;
         R.err = C.e_sol;
@@ -446,6 +448,8 @@ __device__ __forceinline__ void solve_one(const BatchArgs<T>& g, BatchCtl& C, T*
         R.stalled = C.stalled;
         R.pad = 0;
         g.res[C.lp] = R;
+        __threadfence_system();
+        *(volatile int*)(g.done + C.lp) = 1;
     }
 }
 
@@ -455,6 +459,8 @@ __device__ __forceinline__ void skip_one(const BatchArgs<T>& g, const BatchCtl& 
     const int tid = threadIdx.x;
     for (int j = C.L.col_off + tid; j < C.L.col_off + C.L.n; j += BT) g.out_x[j] = 0.0;
     for (int i = C.L.row_off + tid; i < C.L.row_off + C.L.m; i += BT) g.out_y[i] = 0.0;
+    __threadfence_system();
+    __syncthreads();
     if (tid == 0) {
         BatchResult R;
         memset(&R, 0, sizeof(R));
@@ -462,6 +468,8 @@ __device__ __forceinline__ void skip_one(const BatchArgs<T>& g, const BatchCtl& 
         R.err = cpdlp_kkt_errors{nan, nan, nan, nan, nan, nan};
         R.status = CPDLP_STILL_RUNNING;
         g.res[C.lp] = R;
+        __threadfence_system();
+        *(volatile int*)(g.done + C.lp) = 1;
     }
 }
 
@@ -602,43 +610,90 @@ struct PhaseLP {
     const double* y0;
 };
 
+// One launch pair (power method, then the solve kernel) over a set of LPs on
+// its own stream.  Results land in a mapped host block taken from the parent
+// handle's pool: res[count] | done[count] | x[N] | y[M].
 struct RunBase {
     virtual ~RunBase() = default;
     std::vector<PhaseLP> lps;
     std::vector<int64_t> row_off, col_off;
-    // host copies of the results (written by copies queued after the kernel)
-    std::vector<BatchResult> res;
-    std::vector<double> ox, oy;
+    int phase = 1;             // 1: first phase, 2: FP64 phase
+    Handle rh;                 // the device, this run's stream
+    Handle* parent = nullptr;  // owner of the host block pool
+    cudaEvent_t ev = nullptr;  // recorded after the solve kernel
+    void* block = nullptr;
+    BatchResult* h_res = nullptr;
+    int* h_done = nullptr;
+    double* h_x = nullptr;
+    double* h_y = nullptr;
+    std::vector<char> taken;   // per LP: result already taken by the job
+    int64_t ntaken = 0;
     double setup = 0;
-    virtual void fetch(cudaStream_t s) = 0;
+    bool done(int64_t k) const { return __atomic_load_n(h_done + k, __ATOMIC_ACQUIRE) != 0; }
+    bool kernel_finished() {
+        cudaError_t e = cudaEventQuery(ev);
+        if (e == cudaErrorNotReady) return false;
+        CK(e);
+        return true;
+    }
+    void open(Handle& h, int64_t count, int64_t N, int64_t M) {
+        parent = &h;
+        rh.device = h.device;
+        rh.num_sms = h.num_sms;
+        rh.pinned = h.pinned_area(sizeof(double) * 64);   // shared: runs start one at a time
+        rh.pinned_bytes = sizeof(double) * 64;
+        CK(cudaStreamCreateWithFlags(&rh.stream, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        const size_t a = ((size_t)count * sizeof(BatchResult) + 255) & ~(size_t)255;
+        const size_t b = ((size_t)count * sizeof(int) + 255) & ~(size_t)255;
+        const size_t bytes = a + b + sizeof(double) * (size_t)(std::max<int64_t>(N, 1) + std::max<int64_t>(M, 1));
+        block = h.host_get(bytes);
+        char* base = static_cast<char*>(block);
+        h_res = reinterpret_cast<BatchResult*>(base);
+        h_done = reinterpret_cast<int*>(base + a);
+        h_x = reinterpret_cast<double*>(base + a + b);
+        h_y = h_x + std::max<int64_t>(N, 1);
+        memset(h_done, 0, sizeof(int) * (size_t)count);
+        taken.assign((size_t)count, 0);
+    }
+    template <class P>
+    P* dev(P* host) {
+        void* d = nullptr;
+        CK(cudaHostGetDevicePointer(&d, host, 0));
+        return static_cast<P*>(d);
+    }
+    // waits for the kernels (a run is dropped early only when its job is)
+    void close() {
+        if (ev) cudaEventSynchronize(ev);
+        if (rh.stream) cudaStreamSynchronize(rh.stream);
+        release_device();
+        if (ev) cudaEventDestroy(ev);
+        ev = nullptr;
+        if (rh.stream) cudaStreamDestroy(rh.stream);
+        rh.stream = nullptr;
+        if (block && parent) parent->host_put(block);
+        block = nullptr;
+    }
     virtual void release_device() = 0;
 };
 
-// one persistent launch over a set of LPs, on stream h.stream
 template <class T>
 struct Run : RunBase {
     std::unique_ptr<ProblemBase> PB;
     TilePlan planA, planAt;
     DBuf<T> partA, partAt;
     DBuf<T> bx[2], by[2], bxa[2], bya[2], bxr, byr, bxbar;
-    DBuf<double> d_x0, d_y0, d_outx, d_outy, longA, longAt, d_theta;
+    DBuf<double> d_x0, d_y0, longA, longAt, d_theta;
     DBuf<int64_t> d_piters;
     DBuf<BatchLP> d_desc;
     DBuf<int32_t> d_order;
-    DBuf<BatchResult> d_res;
     DBuf<int> d_next;
 
+    ~Run() override { close(); }
+
     void launch(Handle& h, const std::vector<LPData>& all, const cpdlp_params& prm,
-                const int* cancel, int items) {
-        cudaStream_t s = h.stream;
+                const int* cancel, int items, int64_t max_ctas) {
         const double t0 = now_seconds();
-        // occupancy first: it loads the kernels, which must not wait behind
-        // this job's own queued work
-        auto pk = (items == 8) ? k_batch_power<8, T> : k_batch_power<4, T>;
-        auto kern = (items == 8) ? k_batch_pdlp<8, T> : k_batch_pdlp<4, T>;
-        int per_sm_p = 0, per_sm = 0;
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_p, pk, BT, 0));
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BT, 0));
         const int64_t count = (int64_t)lps.size();
         row_off.assign(count + 1, 0);
         col_off.assign(count + 1, 0);
@@ -652,6 +707,16 @@ struct Run : RunBase {
         const int64_t M = row_off[count], N = col_off[count], NZ = nz_off[count];
         if (M >= INT32_MAX || N >= INT32_MAX || NZ >= INT32_MAX)
             fail(CPDLP_ERR_UNSUPPORTED, "batch too large for int32 indices");
+        open(h, count, N, M);
+        cudaStream_t s = rh.stream;
+        AllocScope scope(s);
+        // occupancy first: it loads the kernels, which must not wait behind
+        // this run's own queued work
+        auto pk = (items == 8) ? k_batch_power<8, T> : k_batch_power<4, T>;
+        auto kern = (items == 8) ? k_batch_pdlp<8, T> : k_batch_pdlp<4, T>;
+        int per_sm_p = 0, per_sm = 0;
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_p, pk, BT, 0));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BT, 0));
         // block-diagonal concatenation (1-based CSC)
         std::vector<int64_t> colptr((size_t)N + 1), rowval((size_t)std::max<int64_t>(NZ, 1));
         std::vector<double> nzval(rowval.size()), c((size_t)std::max<int64_t>(N, 1)),
@@ -676,7 +741,7 @@ struct Run : RunBase {
         }
         cpdlp_lp big{M, N, NZ, colptr.data(), rowval.data(), nzval.data(), c.data(), lv.data(),
                      uv.data(), lc.data(), uc.data()};
-        PB.reset(problem_create(h, &big, &prm));
+        PB.reset(problem_create(rh, &big, &prm));
         auto& P = static_cast<ProblemT<T>&>(*PB);
         // tile plans with LP boundaries
         std::vector<int32_t> hpA((size_t)M + 1), hpAt((size_t)N + 1);
@@ -742,10 +807,8 @@ struct Run : RunBase {
         // device buffers
         for (int b = 0; b < 2; b++) { bx[b].alloc(nz); by[b].alloc(mz); bxa[b].alloc(nz); bya[b].alloc(mz); }
         bxr.alloc(nz); byr.alloc(mz); bxbar.alloc(nz);
-        d_outx.alloc(nz); d_outy.alloc(mz);
         d_desc.alloc((size_t)std::max<int64_t>(count, 1));
         d_order.alloc((size_t)std::max<int64_t>(count, 1));
-        d_res.alloc((size_t)std::max<int64_t>(count, 1));
         d_theta.alloc((size_t)std::max<int64_t>(count, 1));
         d_piters.alloc((size_t)std::max<int64_t>(count, 1));
         longA.alloc((size_t)std::max(planA.nlong, 1) * 2);
@@ -774,13 +837,15 @@ struct Run : RunBase {
             pg.x = px.p; pg.Atx = pAtx.p; pg.s = ps.p; pg.x_start = d_xs.p;
             pg.lps = d_desc.p; pg.order = d_order.p; pg.theta = d_theta.p; pg.iters = d_piters.p;
             pg.longAt = longAt.p; pg.next = d_next.p + 1; pg.count = (int32_t)count;
-            const int64_t pgrid =
-                std::max<int64_t>(1, std::min<int64_t>(count, (int64_t)std::max(per_sm_p, 1) * h.num_sms));
+            int64_t pgrid = std::min<int64_t>(count, (int64_t)std::max(per_sm_p, 1) * rh.num_sms);
+            if (max_ctas > 0) pgrid = std::min(pgrid, max_ctas);
+            pgrid = std::max<int64_t>(pgrid, 1);
             pk<<<(unsigned)pgrid, BT, 0, s>>>(pg);
             CK_LAUNCH();
         }
-        const int64_t grid =
-            std::max<int64_t>(1, std::min<int64_t>(count, (int64_t)std::max(per_sm, 1) * h.num_sms));
+        int64_t grid = std::min<int64_t>(count, (int64_t)std::max(per_sm, 1) * rh.num_sms);
+        if (max_ctas > 0) grid = std::min(grid, max_ctas);
+        grid = std::max<int64_t>(grid, 1);
         BatchArgs<T> g;
         g.A = CsrView<T, T>{P.a_ptr.p, P.a_idx.p, P.a_val.p, planA.tasks.p, planA.ntasks,
                             planA.ltasks.p, planA.nltasks, planA.counters.p, partA.p};
@@ -794,7 +859,8 @@ struct Run : RunBase {
         g.power_iters = d_piters.p;
         g.x_init = any_warm ? d_x0.p : nullptr;
         g.y_init = any_warm ? d_y0.p : nullptr;
-        g.lps = d_desc.p; g.order = d_order.p; g.res = d_res.p; g.out_x = d_outx.p; g.out_y = d_outy.p;
+        g.lps = d_desc.p; g.order = d_order.p;
+        g.res = dev(h_res); g.out_x = dev(h_x); g.out_y = dev(h_y); g.done = dev(h_done);
         g.longA = longA.p; g.longAt = longAt.p;
         g.next = d_next.p; g.cancel = cancel; g.count = (int32_t)count;
         g.prm = BatchParams{prm.algorithm, prm.check_every > 0 ? prm.check_every : 100,
@@ -803,26 +869,15 @@ struct Run : RunBase {
         setup = now_seconds() - t0;
         kern<<<(unsigned)grid, BT, 0, s>>>(g);
         CK_LAUNCH();
-    }
-    // after the kernel: results to the host (the copies to pageable memory
-    // block, so they are issued only once the kernel has finished)
-    void fetch(cudaStream_t s) override {
-        const size_t count = lps.size();
-        res.resize(count);
-        ox.resize(d_outx.n);
-        oy.resize(d_outy.n);
-        CK(cudaMemcpyAsync(res.data(), d_res.p, sizeof(BatchResult) * count, cudaMemcpyDeviceToHost, s));
-        CK(cudaMemcpyAsync(ox.data(), d_outx.p, sizeof(double) * ox.size(), cudaMemcpyDeviceToHost, s));
-        CK(cudaMemcpyAsync(oy.data(), d_outy.p, sizeof(double) * oy.size(), cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
+        CK(cudaEventRecord(ev, s));
     }
     void release_device() override {
+        AllocScope scope(rh.stream);
         PB.reset();
         for (int b = 0; b < 2; b++) { bx[b].release(); by[b].release(); bxa[b].release(); bya[b].release(); }
         bxr.release(); byr.release(); bxbar.release(); partA.release(); partAt.release();
-        d_x0.release(); d_y0.release(); d_outx.release(); d_outy.release();
-        longA.release(); longAt.release(); d_desc.release(); d_order.release(); d_res.release();
-        d_theta.release(); d_piters.release(); d_next.release();
+        d_x0.release(); d_y0.release(); longA.release(); longAt.release(); d_desc.release();
+        d_order.release(); d_theta.release(); d_piters.release(); d_next.release();
         planA = TilePlan();
         planAt = TilePlan();
     }
@@ -831,128 +886,124 @@ struct Run : RunBase {
 }  // namespace
 
 // ---- jobs ---------------------------------------------------------------------
+// A job owns copies of its LPs and the runs in flight.  poll() takes every LP
+// whose done flag is set (so an LP is available as soon as its CTA finishes,
+// not when the whole launch does), starts an FP64 run for the LPs that need
+// one, and drops runs whose kernels have finished.
 struct Job {
-    Handle jh;                 // the caller's device, this job's own stream
-    cudaEvent_t ev = nullptr;
+    Handle* parent = nullptr;
+    Handle jh;                 // device and a stream for the cancel flag
     cpdlp_params prm{};
     int items = BATCH_ITEMS;
+    int64_t max_ctas = 0;      // > 0: at most this many CTAs per launch
     std::vector<LPData> lps;
     std::vector<double> target;  // final relative KKT tolerance per LP
-    // results
     std::vector<std::vector<double>> x, y;
     std::vector<cpdlp_stats> st;
-    std::unique_ptr<RunBase> run;
-    int phase = 0;             // 1: first phase in flight, 2: refinement in flight, 3: done
+    std::vector<char> final_;  // LP finished for good
+    int64_t remaining = 0;
+    std::vector<std::unique_ptr<RunBase>> runs;
     bool cancelled = false;
     DBuf<int> d_cancel;
 
     ~Job() {
-        if (jh.stream) cudaStreamSynchronize(jh.stream);
-        if (run) run->release_device();
-        run.reset();
+        runs.clear();          // each run waits for its kernels
         d_cancel.release();
-        if (ev) cudaEventDestroy(ev);
         if (jh.stream) {
             cudaStreamSynchronize(jh.stream);
             cudaStreamDestroy(jh.stream);
         }
-        if (jh.pinned) cudaFreeHost(jh.pinned);
     }
 
-    template <class T>
-    void start(const std::vector<PhaseLP>& phase_lps, const cpdlp_params& p) {
-        AllocScope scope(jh.stream);
-        auto* r = new Run<T>();
-        run.reset(r);
-        r->lps = phase_lps;
-        r->launch(jh, lps, p, d_cancel.p, items);
-        CK(cudaEventRecord(ev, jh.stream));
-    }
-
-    void start_phase(const std::vector<PhaseLP>& phase_lps, int32_t float_type) {
+    void start(const std::vector<PhaseLP>& phase_lps, int32_t float_type, int phase) {
         cpdlp_params p = prm;
         p.float_type = float_type;
-        if (float_type == CPDLP_VAL_F32) start<float>(phase_lps, p);
-        else start<double>(phase_lps, p);
+        std::unique_ptr<RunBase> r;
+        if (float_type == CPDLP_VAL_F32) r.reset(new Run<float>());
+        else r.reset(new Run<double>());
+        r->lps = phase_lps;
+        r->phase = phase;
+        if (float_type == CPDLP_VAL_F32)
+            static_cast<Run<float>&>(*r).launch(*parent, lps, p, d_cancel.p, items, max_ctas);
+        else
+            static_cast<Run<double>&>(*r).launch(*parent, lps, p, d_cancel.p, items, max_ctas);
+        runs.push_back(std::move(r));
     }
 
-    // copies the finished run's results into x / y / st; returns the LPs
-    // that continue in the FP64 refinement phase
-    std::vector<PhaseLP> finish_run() {
-        RunBase& r = *run;
-        std::vector<PhaseLP> next;
-        const bool first = phase == 1;
-        for (size_t k = 0; k < r.lps.size(); k++) {
-            const int64_t id = r.lps[k].id;
-            const cpdlp_lp& L = lps[id].v;
-            const BatchResult& R = r.res[k];
-            x[id].assign(r.ox.begin() + r.col_off[k], r.ox.begin() + r.col_off[k + 1]);
-            y[id].assign(r.oy.begin() + r.row_off[k], r.oy.begin() + r.row_off[k + 1]);
-            cpdlp_stats& S = st[id];
-            const int64_t passes_before = first ? 0 : S.kkt_passes;
-            const double time_before = first ? 0.0 : S.time_elapsed;
-            const int64_t launches_before = first ? 0 : S.kernel_launches;
-            memset(&S, 0, sizeof(S));
-            S.err = R.err;
-            S.time_elapsed = time_before + R.time_elapsed;
-            S.kkt_passes = passes_before + R.kkt_passes;
-            S.refine_kkt_passes = first ? 0 : R.kkt_passes;
-            S.termination_status = R.status;
-            S.restart_from_avg = R.restart_from_avg;
-            S.outer = R.outer; S.inner = R.inner; S.total = R.total;
-            S.eta = R.eta; S.eta_sum = R.eta_sum; S.omega = R.omega;
-            S.power_iterations = R.power_iterations;
-            S.setup_seconds = r.setup;
-            S.kernel_launches = launches_before + 2;  // power method + solve
-            const bool early = L.m == 0 && R.status == CPDLP_OPTIMAL && R.kkt_passes == 0;
-            // FP64 phase: LPs that reached the FP32 tolerance but target a
-            // tighter one, and LPs whose FP32 iterates stalled
-            const bool refine = R.status == CPDLP_OPTIMAL && target[id] < r.lps[k].reltol;
-            const bool rescue = R.stalled && R.kkt_passes < prm.max_kkt_passes;
-            if (first && prm.float_type == CPDLP_VAL_F32 && !cancelled && !early &&
-                (refine || rescue)) {
-                PhaseLP q;
-                q.id = id;
-                q.reltol = target[id];
-                q.max_passes = std::max<int64_t>(prm.max_kkt_passes - R.kkt_passes, 1);
-                q.stall_passes = 0;
-                q.time_limit = prm.time_limit - R.time_elapsed;
-                q.x0 = nullptr;  // set below, once x / y hold this LP's result
-                q.y0 = nullptr;
-                next.push_back(q);
-            }
+    // takes LP k of run r; returns true if it continues in the FP64 phase
+    bool take(RunBase& r, size_t k, PhaseLP& next) {
+        const int64_t id = r.lps[k].id;
+        const cpdlp_lp& L = lps[id].v;
+        const BatchResult R = r.h_res[k];
+        const bool first = r.phase == 1;
+        x[id].assign(r.h_x + r.col_off[k], r.h_x + r.col_off[k + 1]);
+        y[id].assign(r.h_y + r.row_off[k], r.h_y + r.row_off[k + 1]);
+        cpdlp_stats& S = st[id];
+        const int64_t passes_before = first ? 0 : S.kkt_passes;
+        const double time_before = first ? 0.0 : S.time_elapsed;
+        const int64_t launches_before = first ? 0 : S.kernel_launches;
+        memset(&S, 0, sizeof(S));
+        S.err = R.err;
+        S.time_elapsed = time_before + R.time_elapsed;
+        S.kkt_passes = passes_before + R.kkt_passes;
+        S.refine_kkt_passes = first ? 0 : R.kkt_passes;
+        S.termination_status = R.status;
+        S.restart_from_avg = R.restart_from_avg;
+        S.outer = R.outer; S.inner = R.inner; S.total = R.total;
+        S.eta = R.eta; S.eta_sum = R.eta_sum; S.omega = R.omega;
+        S.power_iterations = R.power_iterations;
+        S.setup_seconds = r.setup;
+        S.kernel_launches = launches_before + 2;  // power method + solve
+        const bool early = L.m == 0 && R.status == CPDLP_OPTIMAL && R.kkt_passes == 0;
+        // FP64 phase: LPs that reached the FP32 tolerance but target a tighter
+        // one, and LPs whose FP32 iterates stalled
+        const bool refine = R.status == CPDLP_OPTIMAL && target[id] < r.lps[k].reltol;
+        const bool rescue = R.stalled && R.kkt_passes < prm.max_kkt_passes;
+        if (first && prm.float_type == CPDLP_VAL_F32 && !cancelled && !early && (refine || rescue)) {
+            next.id = id;
+            next.reltol = target[id];
+            next.max_passes = std::max<int64_t>(prm.max_kkt_passes - R.kkt_passes, 1);
+            next.stall_passes = 0;
+            next.time_limit = prm.time_limit - R.time_elapsed;
+            next.x0 = x[id].data();
+            next.y0 = y[id].data();
+            return true;
         }
-        for (PhaseLP& q : next) {
-            q.x0 = x[q.id].data();
-            q.y0 = y[q.id].data();
-        }
-        return next;
+        final_[id] = 1;
+        remaining--;
+        return false;
     }
 
     bool poll() {
-        if (phase == 3) return true;
-        cudaError_t e = cudaEventQuery(ev);
-        if (e == cudaErrorNotReady) return false;
-        CK(e);
-        {
-            AllocScope scope(jh.stream);
-            run->fetch(jh.stream);
-            run->release_device();
+        std::vector<PhaseLP> next;
+        for (auto& rp : runs) {
+            RunBase& r = *rp;
+            if (r.ntaken == (int64_t)r.lps.size()) continue;
+            // the kernel's state is read before the flags, so that a finished
+            // kernel with an unset flag (an error) is seen
+            const bool kdone = r.kernel_finished();
+            for (size_t k = 0; k < r.lps.size(); k++) {
+                if (r.taken[k] || !r.done((int64_t)k)) continue;
+                r.taken[k] = 1;
+                r.ntaken++;
+                PhaseLP q;
+                if (take(r, k, q)) next.push_back(q);
+            }
+            if (kdone && r.ntaken != (int64_t)r.lps.size())
+                fail(CPDLP_ERR_CUDA, "batched solve kernel ended without finishing every LP");
         }
-        std::vector<PhaseLP> next = finish_run();
-        run.reset();
-        if (phase == 1 && !next.empty()) {
-            phase = 2;
-            start_phase(next, CPDLP_VAL_F64);
-            return false;
-        }
-        phase = 3;
-        return true;
+        // drop runs that are complete
+        for (auto& rp : runs)
+            if (rp && rp->ntaken == (int64_t)rp->lps.size() && rp->kernel_finished()) rp.reset();
+        runs.erase(std::remove(runs.begin(), runs.end(), nullptr), runs.end());
+        if (!next.empty()) start(next, CPDLP_VAL_F64, 2);
+        return remaining == 0 && runs.empty();
     }
 };
 
 Job* job_submit(Handle& h, int64_t count, const cpdlp_lp* lps, const cpdlp_params* params,
-                const double* reltol, const double* const* x0, const double* const* y0) {
+                const double* reltol, const double* const* x0, const double* const* y0,
+                int64_t max_ctas) {
     if (count < 0) fail(CPDLP_ERR_ARGUMENT, "negative batch size");
     if (count > 0 && !lps) fail(CPDLP_ERR_ARGUMENT, "null LP array");
     if (!params) fail(CPDLP_ERR_ARGUMENT, "null params");
@@ -961,25 +1012,30 @@ Job* job_submit(Handle& h, int64_t count, const cpdlp_lp* lps, const cpdlp_param
         fail(CPDLP_ERR_ARGUMENT, "float_type must be CPDLP_VAL_F64 or CPDLP_VAL_F32");
     if (params->tile_flags != 0) fail(CPDLP_ERR_ARGUMENT, "tile_flags is reserved and must be 0");
     if (count > INT32_MAX) fail(CPDLP_ERR_UNSUPPORTED, "batch too large");
+    if (max_ctas < 0) fail(CPDLP_ERR_ARGUMENT, "max_ctas must be >= 0");
     for (int64_t k = 0; k < count; k++) check_lp(lps[k]);
     std::unique_ptr<Job> J(new Job());
+    J->parent = &h;
     J->prm = *params;
+    J->max_ctas = max_ctas;
     J->items = params->tile_nnz > 0 ? choose_items(0, 1, params->tile_nnz) : BATCH_ITEMS;
     if (J->items != 4 && J->items != 8) J->items = 8;
     J->jh.device = h.device;
     J->jh.num_sms = h.num_sms;
     CK(cudaStreamCreateWithFlags(&J->jh.stream, cudaStreamNonBlocking));
-    CK(cudaEventCreateWithFlags(&J->ev, cudaEventDisableTiming));
     {
         AllocScope scope(J->jh.stream);
         J->d_cancel.alloc(1);
         CK(cudaMemsetAsync(J->d_cancel.p, 0, sizeof(int), J->jh.stream));
+        CK(cudaStreamSynchronize(J->jh.stream));
     }
     J->lps.resize((size_t)count);
     J->target.resize((size_t)count);
     J->x.resize((size_t)count);
     J->y.resize((size_t)count);
     J->st.assign((size_t)count, cpdlp_stats{});
+    J->final_.assign((size_t)count, 0);
+    J->remaining = count;
     const bool f32 = params->float_type == CPDLP_VAL_F32;
     std::vector<PhaseLP> first((size_t)count);
     for (int64_t k = 0; k < count; k++) {
@@ -999,41 +1055,45 @@ Job* job_submit(Handle& h, int64_t count, const cpdlp_lp* lps, const cpdlp_param
         q.x0 = x0 ? x0[k] : nullptr;
         q.y0 = y0 ? y0[k] : nullptr;
     }
-    if (count == 0) {
-        J->phase = 3;
-        return J.release();
-    }
-    J->phase = 1;
-    J->start_phase(first, params->float_type);
+    if (count > 0) J->start(first, params->float_type, 1);
     return J.release();
 }
 
 bool job_poll(Job* j) { return j->poll(); }
 
 void job_wait(Job* j) {
-    while (!j->poll()) CK(cudaEventSynchronize(j->ev));
+    while (!j->poll()) {
+        // sleep on the oldest run's kernel; its LPs are taken by the next poll
+        if (!j->runs.empty()) CK(cudaEventSynchronize(j->runs.front()->ev));
+    }
 }
 
 void job_cancel(Job* j) {
-    if (j->phase == 3) return;
+    if (j->remaining == 0) return;
     j->cancelled = true;
-    // the job's stream is busy with the kernel: set the flag from a side stream
+    // the runs' streams are busy with their kernels: set the flag from the job's stream
     static const int one = 1;
-    cudaStream_t side;
-    CK(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
-    cudaError_t e = cudaMemcpyAsync(j->d_cancel.p, &one, sizeof(int), cudaMemcpyHostToDevice, side);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(side);
-    cudaStreamDestroy(side);
-    CK(e);
+    CK(cudaMemcpyAsync(j->d_cancel.p, &one, sizeof(int), cudaMemcpyHostToDevice, j->jh.stream));
+    CK(cudaStreamSynchronize(j->jh.stream));
+}
+
+void job_ready(const Job* j, int32_t* ready) {
+    for (size_t k = 0; k < j->final_.size(); k++) ready[k] = j->final_[k] ? 1 : 0;
+}
+
+void job_collect_lp(Job* j, int64_t k, double* x_out, double* y_out, cpdlp_stats* stats) {
+    if (k < 0 || k >= (int64_t)j->lps.size()) fail(CPDLP_ERR_ARGUMENT, "LP index out of range");
+    if (!j->final_[(size_t)k]) fail(CPDLP_ERR_ARGUMENT, "LP not finished (poll until it is ready)");
+    if (x_out) std::copy(j->x[k].begin(), j->x[k].end(), x_out);
+    if (y_out) std::copy(j->y[k].begin(), j->y[k].end(), y_out);
+    if (stats) *stats = j->st[k];
 }
 
 void job_collect(Job* j, double* const* x_out, double* const* y_out, cpdlp_stats* stats) {
-    if (j->phase != 3) fail(CPDLP_ERR_ARGUMENT, "job not finished (poll until it reports done)");
-    for (size_t k = 0; k < j->lps.size(); k++) {
-        if (x_out && x_out[k]) std::copy(j->x[k].begin(), j->x[k].end(), x_out[k]);
-        if (y_out && y_out[k]) std::copy(j->y[k].begin(), j->y[k].end(), y_out[k]);
-        if (stats) stats[k] = j->st[k];
-    }
+    if (j->remaining != 0) fail(CPDLP_ERR_ARGUMENT, "job not finished (poll until it reports done)");
+    for (size_t k = 0; k < j->lps.size(); k++)
+        job_collect_lp(j, (int64_t)k, x_out ? x_out[k] : nullptr, y_out ? y_out[k] : nullptr,
+                       stats ? stats + k : nullptr);
 }
 
 int64_t job_count(const Job* j) { return (int64_t)j->lps.size(); }
@@ -1050,18 +1110,19 @@ int64_t batch_footprint(int64_t count, const cpdlp_lp* lps, const cpdlp_params* 
     }
     // matrices: CSR of A and A' (index, value, padding) plus the preprocessing's
     // FP64 CSC copies and sort buffers; vectors: 7 iterates of n and 5 of m,
-    // bounds and costs, FP64 scalings, start vectors and outputs
+    // bounds and costs, FP64 scalings, power-method vectors
     const int64_t mat = nnz * (2 * (4 + sv) + 40) + (m + n) * 16 + (1 << 16);
-    const int64_t vec = n * (10 * sv + 5 * 8) + m * (8 * sv + 5 * 8);
+    const int64_t vec = n * (10 * sv + 6 * 8) + m * (8 * sv + 5 * 8);
     return mat + vec + count * 256 + (4 << 20);
 }
 
 void batch_solve(Handle& h, int64_t count, const cpdlp_lp* lps, const cpdlp_params* params,
                  double* const* x_out, double* const* y_out, cpdlp_stats* stats) {
     if (count == 0) return;
-    std::unique_ptr<Job> J(job_submit(h, count, lps, params, nullptr, nullptr, nullptr));
+    std::unique_ptr<Job> J(job_submit(h, count, lps, params, nullptr, nullptr, nullptr, 0));
     job_wait(J.get());
     job_collect(J.get(), x_out, y_out, stats);
 }
 
 }  // namespace cpdlp
+

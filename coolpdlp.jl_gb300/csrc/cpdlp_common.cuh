@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -187,6 +188,40 @@ struct Handle {
             pinned_bytes = bytes;
         }
         return pinned;
+    }
+    // Reusable blocks of mapped, page-locked host memory that kernels write
+    // results into while they run.  Blocks are returned to the pool instead of
+    // freed, because freeing page-locked memory waits for the whole device.
+    struct HostBlock {
+        void* p;
+        size_t bytes;
+        bool used;
+    };
+    std::vector<HostBlock> host_blocks;
+    void* host_get(size_t bytes) {
+        int best = -1;
+        for (size_t i = 0; i < host_blocks.size(); i++) {
+            const HostBlock& b = host_blocks[i];
+            if (!b.used && b.bytes >= bytes && (best < 0 || b.bytes < host_blocks[best].bytes))
+                best = (int)i;
+        }
+        if (best >= 0) {
+            host_blocks[best].used = true;
+            return host_blocks[best].p;
+        }
+        void* p = nullptr;
+        const size_t sz = std::max<size_t>(bytes, 1 << 16);
+        CK(cudaHostAlloc(&p, sz, cudaHostAllocMapped | cudaHostAllocPortable));
+        host_blocks.push_back(HostBlock{p, sz, true});
+        return p;
+    }
+    void host_put(void* p) {
+        for (HostBlock& b : host_blocks)
+            if (b.p == p) b.used = false;
+    }
+    void host_release_all() {
+        for (HostBlock& b : host_blocks) cudaFreeHost(b.p);
+        host_blocks.clear();
     }
 };
 

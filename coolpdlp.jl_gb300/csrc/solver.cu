@@ -446,37 +446,45 @@ double powm_default_tol(int64_t n, bool f32) {
     return eps * (double)n3;
 }
 
-template <class T>
-double spectral_norm_T(Handle& h, ProblemT<T>& P, const cpdlp_params* prm, int64_t* iters_out) {
+// powm! on A'A (linalg.jl:86-96).  The vectors and every product are FP64 for
+// both value types (FP32 matrix values promote exactly), and the stopping rule
+// is IterativeSolvers' default for Float64 (eps * n^3): with eps(Float32) that
+// rule stops large FP32 problems after one iteration, and the step size
+// eta = 0.9 / |A| then overshoots.
+template <class V>
+double spectral_norm_T(Handle& h, ProblemT<V>& P, const cpdlp_params* prm, int64_t* iters_out) {
     cudaStream_t s = h.stream;
     const int64_t m = P.m, n = P.n;
-    const bool f32 = std::is_same<T, float>::value;
-    double tol = prm->power_tol_override > 0 ? prm->power_tol_override : powm_default_tol(n, f32);
+    double tol = prm->power_tol_override > 0 ? prm->power_tol_override : powm_default_tol(n, false);
     int64_t maxiter = prm->power_maxiter_override > 0 ? prm->power_maxiter_override : n;
     std::vector<double> x0;
     gaussian_vector(prm->power_seed, n, x0);
-    std::vector<T> x0t(x0.begin(), x0.end());
-    DBuf<T> x((size_t)(n > 0 ? n : 1)), Ax((size_t)(n > 0 ? n : 1)), sv((size_t)(m > 0 ? m : 1));
-    if (n > 0) CK(cudaMemcpyAsync(x.p, x0t.data(), sizeof(T) * n, cudaMemcpyHostToDevice, s));
-    CsrView<T, T> A = view_A(P), At = view_At(P);
+    DBuf<double> x((size_t)(n > 0 ? n : 1)), Ax((size_t)(n > 0 ? n : 1)), sv((size_t)(m > 0 ? m : 1));
+    DBuf<double> pA((size_t)std::max(P.planA.npieces, 1)), pAt((size_t)std::max(P.planAt.npieces, 1));
+    if (n > 0) CK(cudaMemcpyAsync(x.p, x0.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    const CsrView<V, double> A{P.a_ptr.p, P.a_idx.p, P.a_val.p, P.planA.tasks.p, P.planA.ntasks,
+                               P.planA.ltasks.p, P.planA.nltasks, P.planA.counters.p, pA.p};
+    const CsrView<V, double> At{P.at_ptr.p, P.at_idx.p, P.at_val.p, P.planAt.tasks.p,
+                                P.planAt.ntasks, P.planAt.ltasks.p, P.planAt.nltasks,
+                                P.planAt.counters.p, pAt.p};
     double theta_d = 0.0, residual = INFINITY;
     int64_t it = 0;
     const unsigned gr = red_grid(h, n);
     while (!(it > maxiter || residual <= tol)) {
-        launch_tiles<1>(P.planA, A, VecSet<T, 1>{{x.p}}, StoreEpi<T>{sv.p}, s);
-        PowerEpi<T> pe{x.p, Ax.p, P.red_cols.p, P.red_cols.p + (size_t)tiles_grid(P.planAt) * 2};
-        launch_tiles<1>(P.planAt, At, VecSet<T, 1>{{sv.p}}, pe, s);
+        launch_tiles<1>(P.planA, A, VecSet<double, 1>{{x.p}}, StoreEpi<double>{sv.p}, s);
+        PowerEpi<double> pe{x.p, Ax.p, P.red_cols.p, P.red_cols.p + (size_t)tiles_grid(P.planAt) * 2};
+        launch_tiles<1>(P.planAt, At, VecSet<double, 1>{{sv.p}}, pe, s);
         double q[2];
         fetch_reduced(h, P.red_cols.p, P.rows_At_partials, 2, P.red_out.p, q);
-        const T theta = (T)q[0];
-        const T nrm = (T)std::sqrt(q[1]);
-        const T inv = T(1) / nrm;
-        k_power_residual<T><<<gr, RED_THREADS, 0, s>>>(x.p, Ax.p, theta, inv, n, P.red_rows.p);
+        const double theta = q[0];
+        const double nrm = std::sqrt(q[1]);
+        const double inv = 1.0 / nrm;
+        k_power_residual<double><<<gr, RED_THREADS, 0, s>>>(x.p, Ax.p, theta, inv, n, P.red_rows.p);
         CK_LAUNCH();
         double r2;
         fetch_reduced(h, P.red_rows.p, gr, 1, P.red_out.p, &r2);
         residual = std::sqrt(r2);
-        theta_d = (double)theta;
+        theta_d = theta;
         it++;
     }
     if (iters_out) *iters_out = it;
@@ -1000,13 +1008,35 @@ void solve_full(Handle& h, const cpdlp_lp* lp, const cpdlp_params* params, const
     std::unique_ptr<ProblemBase> P(problem_create(h, lp, params));
     std::unique_ptr<StateBase> S(state_create(h, P.get(), params, x0, y0));
     S->starting_time = t0;
+    const bool mixed = params->float_type == CPDLP_VAL_F32 && params->refine_reltol > 0;
+    bool stalled = false;
     if (P->m == 0 && P->zero_cost) {
         S->early_exit_zero_problem();  // common.jl:194-198
+    } else if (mixed) {
+        // FP32 phase, one check at a time: iterates whose relative KKT error has
+        // not halved over FP32_STALL_CHECKS checks continue in FP64
+        double best = INFINITY;
+        int64_t mark = 0;
+        while (S->solve_blocks(1) == CPDLP_STILL_RUNNING) {
+            const cpdlp_kkt_errors& e = S->err;
+            const double rel = std::max(std::max(e.primal / e.primal_scale, e.dual / e.dual_scale),
+                                        e.gap / e.gap_scale);
+            if (rel < 0.5 * best) {
+                best = rel;
+                mark = S->kkt_passes;
+            } else if (S->kkt_passes - mark >= FP32_STALL_CHECKS * (int64_t)params->check_every) {
+                stalled = true;
+                break;
+            }
+        }
     } else {
         S->solve();
     }
-    const bool refine = params->float_type == CPDLP_VAL_F32 && params->refine_reltol > 0 &&
-                        S->status == CPDLP_OPTIMAL && !(P->m == 0 && P->zero_cost);
+    // FP64 phase: the FP32 solution reached termination_reltol and a tighter
+    // refine_reltol is asked for, or the FP32 iterates stalled
+    const bool refine = mixed && !(P->m == 0 && P->zero_cost) &&
+                        ((S->status == CPDLP_OPTIMAL &&
+                          params->refine_reltol < params->termination_reltol) || stalled);
     if (!refine) {
         S->solution(x_out, y_out);
         if (stats) S->stats(stats);

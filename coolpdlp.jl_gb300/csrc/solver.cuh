@@ -8,6 +8,10 @@
 namespace cpdlp {
 
 // Scalars of one step, in the iterate type T (pdlp.jl:108, :126-136).
+// FP32 iterates whose relative KKT error has not halved over this many checks
+// continue in FP64 (cpdlp_solve with refine_reltol > 0, and the batched solver)
+constexpr int64_t FP32_STALL_CHECKS = 30;
+
 template <class T>
 struct StepCoef {
     T tau, sigma, inv_sigma, a, b;

@@ -118,8 +118,11 @@ typedef struct cpdlp_params {
     double power_tol_override;      /* 0 = reference default */
     int64_t power_maxiter_override; /* 0 = reference default */
     uint64_t power_seed;            /* start vector seed (EXT; the reference uses StableRNG(0)) */
-    /* EXT: final FP64 refinement after an FP32 solve reaches termination_reltol:
-     * continue in FP64 from the FP32 iterate until refine_reltol (0 = off). */
+    /* EXT: mixed precision for float_type CPDLP_VAL_F32 (0 = off): when the
+     * FP32 solve reaches termination_reltol and refine_reltol is smaller, or
+     * when the FP32 iterates stall (the relative KKT error does not halve over
+     * 30 checks), the solve continues in FP64 from the FP32 iterate until
+     * refine_reltol. */
     double refine_reltol;
     /* EXT: CSR tile size in nonzeros for the SpMV work partition (0 = autotune). */
     int32_t tile_nnz;
@@ -319,9 +322,11 @@ int cpdlp_spmv_csr_noalloc(cpdlp_handle* h, int64_t m, int64_t n, int64_t nnz,
  * x_out[k] / y_out[k] receive LP k's solution (NULL pointers skip the copy);
  * stats[k] its ConvergenceStats.  All LPs share `params`.  One CTA solves
  * one LP, so an LP's result does not depend on the other LPs of the call.
- * With float_type CPDLP_VAL_F32 and refine_reltol > 0, every LP that reaches
- * termination_reltol continues in FP64 to refine_reltol, warm-started from
- * its FP32 solution (as cpdlp_solve does for one LP). */
+ * With float_type CPDLP_VAL_F32, an LP that reaches termination_reltol and
+ * targets a smaller refine_reltol, or whose FP32 iterates stall (error not
+ * halved over 30 checks), continues in FP64 warm-started from its FP32
+ * solution (as cpdlp_solve does for one LP).  The power method runs in FP64
+ * for both iterate types. */
 int cpdlp_batch_solve(cpdlp_handle* h, int64_t count, const cpdlp_lp* lps,
                       const cpdlp_params* params, double* const* x_out,
                       double* const* y_out, cpdlp_stats* stats);
@@ -336,22 +341,33 @@ int cpdlp_batch_solve(cpdlp_handle* h, int64_t count, const cpdlp_lp* lps,
  * refine_reltol > 0).  With FP32 iterates, LPs whose target is below
  * termination_reltol stop there in FP32 and finish in an FP64 phase
  * warm-started from the FP32 solution.  x0 / y0: `count` warm starts in
- * original units (NULL, or NULL entries, for a cold start).
- * cpdlp_poll never blocks: *done = 1 once every LP is finished (it also
- * launches the FP64 phase when the first one ends).  cpdlp_cancel makes the
- * job's kernels stop at their next termination check: unfinished LPs report
- * CPDLP_STILL_RUNNING.  cpdlp_collect (after done) copies x / y / stats per
- * LP like cpdlp_batch_solve.  cpdlp_job_destroy waits for the job's GPU work.
+ * original units (NULL, or NULL entries, for a cold start).  max_ctas > 0
+ * caps the CTAs (concurrent LPs) of the job's launches, leaving SMs to jobs
+ * submitted later; 0 fills the GPU.
+ * Each LP is available as soon as its CTA finishes it: the kernel writes the
+ * LP's result into mapped host memory and sets its done flag.
+ * cpdlp_poll never blocks: it takes every LP finished so far, launches the
+ * FP64 phase (on a new stream) for those that need it, and sets *done = 1
+ * once every LP is finished.  cpdlp_job_ready fills ready[count] with 1 for
+ * the LPs finished as of the last poll; cpdlp_collect_lp copies one of them.
+ * cpdlp_cancel makes the job's kernels stop at their next termination check:
+ * unfinished LPs report CPDLP_STILL_RUNNING.  cpdlp_collect (after done)
+ * copies x / y / stats per LP like cpdlp_batch_solve.  cpdlp_job_destroy
+ * waits for the job's GPU work.  A job must be destroyed before its handle.
  * cpdlp_batch_footprint: upper bound of the device bytes a job over these LPs
  * holds (admission control); -1 on invalid arguments. */
 int cpdlp_submit(cpdlp_handle* h, int64_t count, const cpdlp_lp* lps,
                  const cpdlp_params* params, const double* reltol,
-                 const double* const* x0, const double* const* y0, cpdlp_job** out);
+                 const double* const* x0, const double* const* y0, int64_t max_ctas,
+                 cpdlp_job** out);
 int cpdlp_poll(cpdlp_handle* h, cpdlp_job* job, int32_t* done);
 int cpdlp_wait(cpdlp_handle* h, cpdlp_job* job);
 int cpdlp_cancel(cpdlp_handle* h, cpdlp_job* job);
 int cpdlp_collect(cpdlp_handle* h, cpdlp_job* job, double* const* x_out,
                   double* const* y_out, cpdlp_stats* stats);
+int cpdlp_job_ready(cpdlp_handle* h, const cpdlp_job* job, int32_t* ready);
+int cpdlp_collect_lp(cpdlp_handle* h, cpdlp_job* job, int64_t k, double* x_out,
+                     double* y_out, cpdlp_stats* stats);
 int64_t cpdlp_job_count(const cpdlp_job* job);
 int cpdlp_job_destroy(cpdlp_job* job);
 int64_t cpdlp_batch_footprint(int64_t count, const cpdlp_lp* lps, const cpdlp_params* params);

@@ -173,6 +173,39 @@ def test_job_cancel(handle):
         assert np.all(np.isfinite(x[k]))
 
 
+def test_job_lps_retire_individually(handle):
+    """An LP's result is available as soon as its CTA finishes it, while a
+    slower LP of the same job is still running."""
+    from coolpdlp import native, _abi as A
+    from coolpdlp import generators as G
+    slow = G.batch_lps(1, m_lo=300, m_hi=300, seed0=6100)
+    fast = G.batch_lps(6, m_lo=40, m_hi=80, seed0=6200)
+    S = _structs(slow + fast)
+    prm = A.default_params_py(A.ALGO_PDLP)
+    prm.max_kkt_passes = 10_000_000
+    prm.time_limit = 20.0
+    tol = [1e-300] + [1e-4] * len(fast)       # the first LP cannot converge
+    job = native.Job(handle, S, prm, reltol=tol)
+    t0 = time.time()
+    seen_early = False
+    while time.time() - t0 < 15.0:
+        done = job.poll()
+        r = job.ready()
+        if r[1:].all() and not r[0]:
+            seen_early = not done
+            break
+        time.sleep(0.01)
+    assert seen_early
+    for k in range(1, len(S)):
+        x, y, st = job.collect_lp(k)
+        assert st.termination_status == 0 and _rel(st) <= 1e-4
+    with pytest.raises(A.ArgumentError):
+        job.collect_lp(0)
+    job.cancel()
+    xs, ys, st = job.result()
+    assert st[0].termination_status == A.STILL_RUNNING
+
+
 def test_batch_pdhg_limits_and_errors(handle):
     from coolpdlp import native, _abi as A
     lps = _set(6, seed0=77)

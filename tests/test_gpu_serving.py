@@ -1,0 +1,72 @@
+"""The continuous-batching server (coolpdlp.serving): requests that arrive
+while others run are admitted as slots and HBM budget free up, their work
+overlaps on the GPU, and every result equals the result of the same request
+solved alone (bit-identical: an LP's arithmetic does not depend on the mix)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _stream(count=36, rate=400.0, seed=11):
+    from coolpdlp import generators as G
+    reqs = G.served_stream(count, rate, seed=seed, m_lo=60, m_hi=1500, side_lo=6, side_hi=14,
+                           k_lo=2, k_hi=4)
+    lps = [G.request_lp(r) for r in reqs]
+    return reqs, lps
+
+
+def _rel(st):
+    e = st.err
+    return max(e.primal / e.primal_scale, e.dual / e.dual_scale, e.gap / e.gap_scale)
+
+
+@pytest.mark.parametrize("float_type", [1, 0])
+def test_served_stream_equals_alone(float_type):
+    from coolpdlp import native, serving, _abi as A
+    reqs, lps = _stream()
+    server = serving.Server(float_type=float_type, big_nnz=4000, max_ctas=16,
+                            max_inflight_lps=24)
+    out = serving.replay(server, [r.arrival for r in reqs], lps, [r.reltol for r in reqs])
+    assert out["requests"] == len(reqs)
+    assert out["status_counts"][0] == len(reqs), out
+    assert out["jobs"] >= 2 and out["single_route"] >= 1, out
+    assert out["p99_ms"] >= out["p50_ms"] > 0
+    overlapped = 0
+    h = native.Handle(0)
+    for r in reqs:
+        res = server.results[r.rid]
+        assert _rel(res.stats) <= r.reltol, (r.rid, _rel(res.stats), r.reltol)
+        lp = lps[r.rid]
+        S = native.LPStruct(lp.m, lp.n, lp.colptr, lp.rowval, lp.nzval, lp.c, lp.lv, lp.uv,
+                            lp.lc, lp.uc)
+        if res.route == "batch":
+            x1, y1, s1 = native.Job(h, [S], server.params, reltol=[r.reltol]).result()
+            x1, y1, s1 = x1[0], y1[0], s1[0]
+        else:
+            x1, y1, s1 = server._solve_single(serving._Waiting(r.rid, S, r.reltol, 0.0, 0,
+                                                                int(S.s.nnz)))
+        assert np.array_equal(x1, res.x) and np.array_equal(y1, res.y), (r.rid, res.route)
+        assert s1.kkt_passes == res.stats.kkt_passes
+        overlapped += int(any(o.admitted < res.finished and o.finished > res.admitted
+                              for o in server.results.values() if o.rid != r.rid))
+    assert overlapped >= len(reqs) // 2   # requests really ran while others were in flight
+    server.close()
+
+
+def test_admission_respects_hbm_budget():
+    from coolpdlp import native, serving, _abi as A
+    reqs, lps = _stream(count=12, rate=1000.0, seed=5)
+    probe = serving.Server(float_type=A.VAL_F32)
+    sizes = []
+    for i, lp in enumerate(lps):
+        probe.offer(i, lp, 1e-4)
+        sizes.append(probe.waiting[-1].nbytes)
+    probe.close()
+    budget = 2.5 * max(sizes)
+    server = serving.Server(float_type=A.VAL_F32, hbm_budget=budget, big_nnz=10**9)
+    out = serving.replay(server, [r.arrival for r in reqs], lps, [1e-4] * len(reqs))
+    assert out["status_counts"][0] == len(reqs)
+    assert 0 < out["peak_admitted_bytes"] <= budget
+    assert out["jobs"] >= 3
+    server.close()
