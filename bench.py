@@ -246,6 +246,21 @@ def measure_serving(requests: int, rate: float) -> dict:
         r = serving.replay(srv, [q.arrival for q in reqs], lps, [q.reltol for q in reqs])
         srv.close()
         out[name] = r
+    # the plain FP64 one-LP-at-a-time path (cpdlp_solve) on an evenly spaced sample
+    from coolpdlp import native
+    h = native.Handle(0)
+    idx = list(range(0, requests, max(1, requests // 40)))[:40]
+    t0 = time.perf_counter()
+    for i in idx:
+        lp = lps[i]
+        p = native.default_params()
+        p.termination_reltol = reqs[i].reltol
+        native.solve_lp(h, native.LPStruct(lp.m, lp.n, lp.colptr, lp.rowval, lp.nzval, lp.c,
+                                           lp.lv, lp.uv, lp.lc, lp.uc), p)
+    seq = len(idx) / (time.perf_counter() - t0)
+    out["fp64_sequential"] = {"lps_per_s": seq, "sample": len(idx)}
+    for name in ("fp32_refined", "fp64"):
+        out[name]["throughput_vs_sequential"] = out[name]["throughput_lps_per_s"] / seq
     return out
 
 

@@ -53,6 +53,8 @@ struct BatchLP {
     double power_tol, reltol, time_limit;
     int64_t power_maxiter, max_passes;
     int64_t stall_passes;  // > 0: stop when the error has not halved for this many passes
+    double theta0;         // >= 0: |A|^2 estimate carried over (the power method is skipped)
+    double omega0;         // > 0: primal weight carried over
 };
 
 struct BatchResult {
@@ -60,6 +62,7 @@ struct BatchResult {
     int64_t kkt_passes, outer, inner, total, power_iterations;
     double eta, omega, eta_sum, time_elapsed;
     int32_t status, restart_from_avg, stalled, pad;
+    double theta;
 };
 
 struct BatchParams {
@@ -254,6 +257,7 @@ __device__ __forceinline__ void solve_one(const BatchArgs<T>& g, BatchCtl& C, T*
         block_sum<4>(q, sh);
         const double cn = sqrt(q[3]), bn = sqrt(q[1]);
         omega = !pdlp ? 1.0 : (cn > g.prm.zero_tol && bn > g.prm.zero_tol) ? cn / bn : 1.0;
+        if (pdlp && C.L.omega0 > 0) omega = C.L.omega0;
         if (tid == 0) {
             C.pscale = 1.0 + sqrt(q[0]);
             C.dscale = 1.0 + sqrt(q[2]);
@@ -440,6 +444,7 @@ __device__ __forceinline__ void solve_one(const BatchArgs<T>& g, BatchCtl& C, T*
         R.total = C.total;
         R.power_iterations = C.power_it;
         R.eta = eta;
+        R.theta = g.theta[C.lp];
         R.omega = omega;
         R.eta_sum = eta_sum;
         R.time_elapsed = (double)(global_ns() - C.t_start) * 1e-9;
@@ -490,6 +495,14 @@ __global__ void __launch_bounds__(BT) k_batch_power(PowerArgs<V> g) {
         }
         __syncthreads();
         if (s_lp < 0) break;
+        if (L.theta0 >= 0) {  // carried over from an earlier run of the same LP
+            if (tid == 0) {
+                g.theta[s_lp] = L.theta0;
+                g.iters[s_lp] = 0;
+            }
+            __syncthreads();
+            continue;
+        }
         const int c0 = L.col_off, c1 = c0 + L.n;
         for (int j = c0 + tid; j < c1; j += BT) g.x[j] = g.x_start[j];
         __syncthreads();
@@ -608,6 +621,8 @@ struct PhaseLP {
     int64_t max_passes, stall_passes;
     const double* x0;  // warm start (original units) or null
     const double* y0;
+    double theta0 = -1.0;  // >= 0: skip the power method with this |A|^2 estimate
+    double omega0 = 0.0;   // > 0: start from this primal weight
 };
 
 // One launch pair (power method, then the solve kernel) over a set of LPs on
@@ -777,6 +792,8 @@ struct Run : RunBase {
             d.time_limit = lps[k].time_limit;
             d.max_passes = lps[k].max_passes;
             d.stall_passes = lps[k].stall_passes;
+            d.theta0 = lps[k].theta0;
+            d.omega0 = lps[k].omega0;
         }
         std::vector<int32_t> order((size_t)count);
         std::iota(order.begin(), order.end(), 0);
@@ -967,6 +984,10 @@ struct Job {
             next.time_limit = prm.time_limit - R.time_elapsed;
             next.x0 = x[id].data();
             next.y0 = y[id].data();
+            // continuation: the FP64 run keeps the FP32 run's |A|^2 estimate (an FP64
+            // power method over the same values up to FP32 rounding) and primal weight
+            next.theta0 = R.theta;
+            next.omega0 = R.omega;
             return true;
         }
         final_[id] = 1;

@@ -896,7 +896,7 @@ struct StateT : StateBase {
 
 template <class T>
 StateBase* make_state(Handle& h, ProblemT<T>* P, const cpdlp_params* prm, const double* x0,
-                      const double* y0) {
+                      const double* y0, double eta0, double omega0) {
     double t0 = now_seconds();
     auto* S = new StateT<T>();
     std::unique_ptr<StateT<T>> guard(S);
@@ -933,8 +933,13 @@ StateBase* make_state(Handle& h, ProblemT<T>* P, const cpdlp_params* prm, const 
     CK(cudaMemsetAsync(S->xbar.p, 0, sizeof(T) * nz, s));
     S->cur = 0;
     // fixed_stepsize (step_size.jl:22-27)
-    double sn = spectral_norm_T(h, *P, prm, &S->power_iterations);
-    S->eta = prm->invnorm_scaling * (1.0 / sn);
+    if (eta0 > 0) {  // continuation of an earlier solve of the same LP
+        S->eta = eta0;
+        S->power_iterations = 0;
+    } else {
+        double sn = spectral_norm_T(h, *P, prm, &S->power_iterations);
+        S->eta = prm->invnorm_scaling * (1.0 / sn);
+    }
     // primal_weight_init (step_size.jl:29-40); PDHG: omega = 1 (pdhg.jl:48)
     if (prm->algorithm == CPDLP_ALGO_PDHG) {
         S->omega = 1.0;
@@ -947,6 +952,7 @@ StateBase* make_state(Handle& h, ProblemT<T>* P, const cpdlp_params* prm, const 
         fetch_reduced(h, P->red_rows.p, g, 4, P->red_out.p, q);
         const double c_norm = std::sqrt(q[3]), cb_norm = std::sqrt(q[1]);
         S->omega = (c_norm > prm->zero_tol && cb_norm > prm->zero_tol) ? c_norm / cb_norm : 1.0;
+        if (omega0 > 0) S->omega = omega0;
     }
     S->eta_sum = 0.0;
     for (auto* e : {&S->err, &S->err_cand, &S->err_cand_last, &S->err_restart})
@@ -988,12 +994,12 @@ ProblemBase* problem_create(Handle& h, const cpdlp_lp* lp, const cpdlp_params* p
 }
 
 StateBase* state_create(Handle& h, ProblemBase* P, const cpdlp_params* prm, const double* x0,
-                        const double* y0) {
+                        const double* y0, double eta0, double omega0) {
     if (!P || !prm) fail(CPDLP_ERR_ARGUMENT, "null problem or params");
     if (prm->check_every <= 0) fail(CPDLP_ERR_ARGUMENT, "check_every must be positive");
     if (P->vt == CPDLP_VAL_F32)
-        return make_state<float>(h, static_cast<ProblemT<float>*>(P), prm, x0, y0);
-    return make_state<double>(h, static_cast<ProblemT<double>*>(P), prm, x0, y0);
+        return make_state<float>(h, static_cast<ProblemT<float>*>(P), prm, x0, y0, eta0, omega0);
+    return make_state<double>(h, static_cast<ProblemT<double>*>(P), prm, x0, y0, eta0, omega0);
 }
 
 double problem_spectral_norm(Handle& h, ProblemBase* P, const cpdlp_params* prm, int64_t* iters) {
@@ -1052,10 +1058,14 @@ void solve_full(Handle& h, const cpdlp_lp* lp, const cpdlp_params* params, const
     p64.time_limit = params->time_limit - (now_seconds() - t0);
     const int64_t passes32 = S->kkt_passes;
     const int64_t launches32 = S->launches;
+    // continuation: the FP64 phase keeps the step size (an FP64 power method over
+    // the same values up to FP32 rounding) and the adapted primal weight
+    const double eta32 = S->eta, omega32 = S->omega;
     S.reset();
     P.reset();
     std::unique_ptr<ProblemBase> P64(problem_create(h, lp, &p64));
-    std::unique_ptr<StateBase> S64(state_create(h, P64.get(), &p64, xs.data(), ys.data()));
+    std::unique_ptr<StateBase> S64(
+        state_create(h, P64.get(), &p64, xs.data(), ys.data(), eta32, omega32));
     S64->starting_time = t0;
     S64->solve();
     S64->solution(x_out, y_out);

@@ -78,8 +78,10 @@ struct StateBase {
 };
 
 ProblemBase* problem_create(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm);
+// eta0 > 0 / omega0 > 0 continue an earlier solve of the same LP: the step size
+// (no power method) and the primal weight start from these values
 StateBase* state_create(Handle& h, ProblemBase* P, const cpdlp_params* prm, const double* x0,
-                        const double* y0);
+                        const double* y0, double eta0 = 0.0, double omega0 = 0.0);
 double problem_spectral_norm(Handle& h, ProblemBase* P, const cpdlp_params* prm, int64_t* iters);
 
 // solve(milp, sol, algo) (common.jl:186-209) on the device, plus the FP64
