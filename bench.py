@@ -54,9 +54,9 @@ def parse_args():
                     help="LPs of the batched workload (0 skips the batch measurement)")
     ap.add_argument("--sequential-sample", type=int, default=32,
                     help="LPs of the batch solved one at a time by the FP64 path")
-    ap.add_argument("--serve-requests", type=int, default=240,
+    ap.add_argument("--serve-requests", type=int, default=160,
                     help="requests of the served stream (0 skips the serving measurement)")
-    ap.add_argument("--serve-rate", type=float, default=60.0, help="Poisson arrivals per second")
+    ap.add_argument("--serve-rate", type=float, default=8.0, help="Poisson arrivals per second")
     return ap.parse_args()
 
 

@@ -985,9 +985,10 @@ struct Job {
             next.x0 = x[id].data();
             next.y0 = y[id].data();
             // continuation: the FP64 run keeps the FP32 run's |A|^2 estimate (an FP64
-            // power method over the same values up to FP32 rounding) and primal weight
+            // power method over the same values up to FP32 rounding) and, after a
+            // converged FP32 run, its primal weight
             next.theta0 = R.theta;
-            next.omega0 = R.omega;
+            next.omega0 = refine ? R.omega : 0.0;  // a stalled run's weight is not kept
             return true;
         }
         final_[id] = 1;

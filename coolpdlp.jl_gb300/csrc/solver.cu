@@ -17,6 +17,9 @@
 // FP64 exactly as restart.jl:40-57, termination.jl:89-101 state them.
 #include <algorithm>
 #include <chrono>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <memory>
 #include <type_traits>
 
@@ -180,19 +183,46 @@ __global__ void k_scales(const T* __restrict__ lc, const T* __restrict__ uc,
 // ---------------------------------------------------------------------------
 // epilogues of the tile engine
 // ---------------------------------------------------------------------------
-// powm! residual and normalisation: r = Ax - theta*x, x = Ax * (1/||Ax||)
-template <class T>
+// One power-method iteration is captured as a graph and runs without the host:
+//   k_power_theta:    theta = x.Ax, inv = 1/||Ax|| from the reduced partials
+//   k_power_residual: r = Ax - theta*x, x = Ax * inv (block partials of ||r||^2)
+//   k_power_finish:   ||r||, then the iteration's (theta, ||r||) go to slot it % depth
+//                     of a mapped host ring and the device iteration counter advances
+// so the host can queue several iterations ahead and check each one's stopping
+// rule when its slot is written (powm!, linalg.jl:86-96, IterativeSolvers 0.9.4).
+struct PowerSlot {
+    double theta, residual;
+};
+__global__ void k_power_theta(const double* __restrict__ q, double* __restrict__ scal,
+                              const int* __restrict__ it, PowerSlot* ring, int depth) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        const double theta = q[0];
+        const double nrm = sqrt(q[1]);
+        scal[0] = theta;
+        scal[1] = 1.0 / nrm;
+        ring[*it % depth].theta = theta;
+    }
+}
 __global__ void __launch_bounds__(RED_THREADS)
-    k_power_residual(T* __restrict__ x, const T* __restrict__ Ax, T theta, T inv, int64_t n,
-                     double* __restrict__ part) {
+    k_power_residual(double* __restrict__ x, const double* __restrict__ Ax,
+                     const double* __restrict__ scal, int64_t n, double* __restrict__ part) {
+    const double theta = scal[0], inv = scal[1];
     double acc[1] = {0.0};
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
-        const T r = add_rn(mul_rn(-theta, x[j]), Ax[j]);
-        acc[0] += (double)r * (double)r;
+        const double r = add_rn(mul_rn(-theta, x[j]), Ax[j]);
+        acc[0] += r * r;
         x[j] = mul_rn(Ax[j], inv);
     }
     block_reduce_store<1>(acc, part);
+}
+__global__ void k_power_finish(const double* __restrict__ r2, int* it, PowerSlot* ring,
+                               int depth) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        ring[*it % depth].residual = sqrt(r2[0]);
+        __threadfence_system();
+        *it += 1;
+    }
 }
 
 // ||a - b||^2 over x (n) and y (m): primal_weight_update! (step_size.jl:58-75)
@@ -254,6 +284,61 @@ template <class T>
 CsrView<T, T> view_At(ProblemT<T>& P) {
     return CsrView<T, T>{P.at_ptr.p, P.at_idx.p, P.at_val.p, P.planAt.tasks.p, P.planAt.ntasks,
                          P.planAt.ltasks.p, P.planAt.nltasks, P.planAt.counters.p, P.partAt.p};
+}
+
+// Autotuner of the tile shape (nonzeros per lane) of one CSR matrix: each
+// candidate's plan is built and the fused step kernel that uses the matrix (the
+// primal step for A', the dual step for A) is timed with CUDA events on the
+// handle's stream, on scratch vectors.  The heuristic's choice is kept unless
+// another candidate is at least 3% faster.  Decisions are cached per matrix
+// shape for the process.
+constexpr int64_t AUTOTUNE_MIN_NNZ = 1 << 21;
+
+template <class T, class Launch>
+int tune_items(Handle& h, const std::vector<int32_t>& hp, int32_t rows, int64_t cols, int64_t nnz,
+               int heuristic, int which, Launch&& launch) {
+    static std::mutex mu;
+    static std::map<std::tuple<int64_t, int64_t, int64_t, int, int, int>, int> cache;
+    const auto key = std::make_tuple((int64_t)rows, cols, nnz, (int)sizeof(T), h.device, which);
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        auto it = cache.find(key);
+        if (it != cache.end()) return it->second;
+    }
+    cudaStream_t s = h.stream;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    int best = heuristic;
+    float best_ms = INFINITY;
+    const int cands[3] = {heuristic, heuristic == 4 ? 8 : 4, heuristic == 16 ? 8 : 16};
+    try {
+        for (int items : cands) {
+            TilePlan plan;
+            build_tile_plan(hp, rows, items, plan, s);
+            DBuf<T> part((size_t)std::max(plan.npieces, 1));
+            launch(plan, part.p);
+            CK(cudaEventRecord(e0, s));
+            for (int r = 0; r < 4; r++) launch(plan, part.p);
+            CK(cudaEventRecord(e1, s));
+            CK(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, e0, e1));
+            if (items == heuristic ? ms < best_ms : ms < 0.97f * best_ms) {
+                best_ms = ms;
+                best = items;
+            }
+        }
+    } catch (...) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        throw;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    std::lock_guard<std::mutex> lock(mu);
+    cache[key] = best;
+    return best;
 }
 
 // device reduction of (rows x q) partials into host doubles
@@ -387,8 +472,30 @@ ProblemBase* make_problem(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm
     CK(cudaMemcpyAsync(hp2.data(), P->a_ptr.p, sizeof(int32_t) * (m + 1), cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(hp1.data(), P->at_ptr.p, sizeof(int32_t) * (n + 1), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    build_tile_plan(hp2, (int32_t)m, choose_items(nnz, m, prm->tile_nnz), P->planA, s);
-    build_tile_plan(hp1, (int32_t)n, choose_items(nnz, n, prm->tile_nnz), P->planAt, s);
+    int items_A = choose_items(nnz, m, prm->tile_nnz), items_At = choose_items(nnz, n, prm->tile_nnz);
+    if (prm->tile_nnz == 0 && nnz >= AUTOTUNE_MIN_NNZ) {
+        // scratch iterates (zeros) for the fused step kernels being timed
+        DBuf<T> vx(nzv), vxn(nzv), vxb(nzv), vxa(nzv), vxa2(nzv), vy(mz), vyn(mz), vya(mz), vya2(mz);
+        for (DBuf<T>* b : {&vx, &vxn, &vxb, &vxa, &vxa2, &vy, &vyn, &vya, &vya2})
+            CK(cudaMemsetAsync(b->p, 0, sizeof(T) * b->n, s));
+        DBuf<StepCoef<T>> cf(1);
+        CK(cudaMemsetAsync(cf.p, 0, sizeof(StepCoef<T>), s));
+        ProblemT<T>* Q = P;
+        items_At = tune_items<T>(h, hp1, (int32_t)n, m, nnz, items_At, 1, [&](TilePlan& pl, T* part) {
+            const CsrView<T, T> V{Q->at_ptr.p, Q->at_idx.p, Q->at_val.p, pl.tasks.p, pl.ntasks,
+                                  pl.ltasks.p, pl.nltasks, pl.counters.p, part};
+            PrimalEpi<T> pe{vx.p, Q->c.p, Q->lv.p, Q->uv.p, vxn.p, vxb.p, vxa.p, vxa2.p, {cf.p}, 1};
+            launch_tiles<1>(pl, V, VecSet<T, 1>{{vy.p}}, pe, s);
+        });
+        items_A = tune_items<T>(h, hp2, (int32_t)m, n, nnz, items_A, 0, [&](TilePlan& pl, T* part) {
+            const CsrView<T, T> V{Q->a_ptr.p, Q->a_idx.p, Q->a_val.p, pl.tasks.p, pl.ntasks,
+                                  pl.ltasks.p, pl.nltasks, pl.counters.p, part};
+            DualEpi<T> de{vy.p, Q->lc.p, Q->uc.p, vyn.p, vya.p, vya2.p, {cf.p}, 1};
+            launch_tiles<1>(pl, V, VecSet<T, 1>{{vxb.p}}, de, s);
+        });
+    }
+    build_tile_plan(hp2, (int32_t)m, items_A, P->planA, s);
+    build_tile_plan(hp1, (int32_t)n, items_At, P->planAt, s);
     P->partA.alloc((size_t)(P->planA.npieces > 0 ? P->planA.npieces : 1) * 4);
     P->partAt.alloc((size_t)(P->planAt.npieces > 0 ? P->planAt.npieces : 1) * 4);
     P->rows_A_partials = (int64_t)tiles_grid(P->planA) + P->planA.nlong;
@@ -461,31 +568,67 @@ double spectral_norm_T(Handle& h, ProblemT<V>& P, const cpdlp_params* prm, int64
     gaussian_vector(prm->power_seed, n, x0);
     DBuf<double> x((size_t)(n > 0 ? n : 1)), Ax((size_t)(n > 0 ? n : 1)), sv((size_t)(m > 0 ? m : 1));
     DBuf<double> pA((size_t)std::max(P.planA.npieces, 1)), pAt((size_t)std::max(P.planAt.npieces, 1));
+    DBuf<double> scal(4);
+    DBuf<int> d_it(1);
     if (n > 0) CK(cudaMemcpyAsync(x.p, x0.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(d_it.p, 0, sizeof(int), s));
     const CsrView<V, double> A{P.a_ptr.p, P.a_idx.p, P.a_val.p, P.planA.tasks.p, P.planA.ntasks,
                                P.planA.ltasks.p, P.planA.nltasks, P.planA.counters.p, pA.p};
     const CsrView<V, double> At{P.at_ptr.p, P.at_idx.p, P.at_val.p, P.planAt.tasks.p,
                                 P.planAt.ntasks, P.planAt.ltasks.p, P.planAt.nltasks,
                                 P.planAt.counters.p, pAt.p};
-    double theta_d = 0.0, residual = INFINITY;
-    int64_t it = 0;
+    constexpr int DEPTH = 8;  // iterations queued ahead of the host's stopping check
+    void* block = h.host_get(sizeof(PowerSlot) * DEPTH);
+    PowerSlot* ring = static_cast<PowerSlot*>(block);
+    PowerSlot* dring = nullptr;
+    CK(cudaHostGetDevicePointer((void**)&dring, ring, 0));
+    struct Cleanup {
+        Handle& h; void* block; cudaStream_t s; cudaGraphExec_t exec = nullptr;
+        cudaEvent_t ev[DEPTH] = {};
+        ~Cleanup() {
+            cudaStreamSynchronize(s);  // speculative iterations finish before buffers go
+            if (exec) cudaGraphExecDestroy(exec);
+            for (cudaEvent_t e : ev)
+                if (e) cudaEventDestroy(e);
+            h.host_put(block);
+        }
+    } cleanup{h, block, s};
+    for (int k = 0; k < DEPTH; k++)
+        CK(cudaEventCreateWithFlags(&cleanup.ev[k], cudaEventDisableTiming));
     const unsigned gr = red_grid(h, n);
-    while (!(it > maxiter || residual <= tol)) {
+    {
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         launch_tiles<1>(P.planA, A, VecSet<double, 1>{{x.p}}, StoreEpi<double>{sv.p}, s);
         PowerEpi<double> pe{x.p, Ax.p, P.red_cols.p, P.red_cols.p + (size_t)tiles_grid(P.planAt) * 2};
         launch_tiles<1>(P.planAt, At, VecSet<double, 1>{{sv.p}}, pe, s);
-        double q[2];
-        fetch_reduced(h, P.red_cols.p, P.rows_At_partials, 2, P.red_out.p, q);
-        const double theta = q[0];
-        const double nrm = std::sqrt(q[1]);
-        const double inv = 1.0 / nrm;
-        k_power_residual<double><<<gr, RED_THREADS, 0, s>>>(x.p, Ax.p, theta, inv, n, P.red_rows.p);
-        CK_LAUNCH();
-        double r2;
-        fetch_reduced(h, P.red_rows.p, gr, 1, P.red_out.p, &r2);
-        residual = std::sqrt(r2);
-        theta_d = theta;
+        reduce_partials(P.red_cols.p, P.rows_At_partials, 2, P.red_out.p, s);
+        k_power_theta<<<1, 32, 0, s>>>(P.red_out.p, scal.p, d_it.p, dring, DEPTH);
+        k_power_residual<<<gr, RED_THREADS, 0, s>>>(x.p, Ax.p, scal.p, n, P.red_rows.p);
+        reduce_partials(P.red_rows.p, gr, 1, P.red_out.p + 2, s);
+        k_power_finish<<<1, 32, 0, s>>>(P.red_out.p + 2, d_it.p, dring, DEPTH);
+        const cudaError_t launch_err = cudaGetLastError();
+        const cudaError_t end_err = cudaStreamEndCapture(s, &g);
+        CK(launch_err);
+        CK(end_err);
+        const cudaError_t inst = cudaGraphInstantiate(&cleanup.exec, g, 0);
+        cudaGraphDestroy(g);
+        CK(inst);
+    }
+    // powm!: iterate while !(it > maxiter || residual <= tol); it counts iterations run
+    double theta_d = 0.0;
+    int64_t launched = 0, it = 0;
+    for (;;) {
+        while (launched - it < DEPTH && launched <= maxiter) {
+            CK(cudaGraphLaunch(cleanup.exec, s));
+            CK(cudaEventRecord(cleanup.ev[launched % DEPTH], s));
+            launched++;
+        }
+        CK(cudaEventSynchronize(cleanup.ev[it % DEPTH]));
+        const PowerSlot slot = ring[it % DEPTH];
         it++;
+        theta_d = slot.theta;
+        if (it > maxiter || slot.residual <= tol) break;
     }
     if (iters_out) *iters_out = it;
     return std::sqrt(theta_d);
@@ -1059,13 +1202,14 @@ void solve_full(Handle& h, const cpdlp_lp* lp, const cpdlp_params* params, const
     const int64_t passes32 = S->kkt_passes;
     const int64_t launches32 = S->launches;
     // continuation: the FP64 phase keeps the step size (an FP64 power method over
-    // the same values up to FP32 rounding) and the adapted primal weight
+    // the same values up to FP32 rounding) and, after a converged FP32 phase, the
+    // adapted primal weight
     const double eta32 = S->eta, omega32 = S->omega;
     S.reset();
     P.reset();
     std::unique_ptr<ProblemBase> P64(problem_create(h, lp, &p64));
     std::unique_ptr<StateBase> S64(
-        state_create(h, P64.get(), &p64, xs.data(), ys.data(), eta32, omega32));
+        state_create(h, P64.get(), &p64, xs.data(), ys.data(), eta32, stalled ? 0.0 : omega32));
     S64->starting_time = t0;
     S64->solve();
     S64->solution(x_out, y_out);
