@@ -57,6 +57,10 @@ def parse_args():
     ap.add_argument("--serve-requests", type=int, default=160,
                     help="requests of the served stream (0 skips the serving measurement)")
     ap.add_argument("--serve-rate", type=float, default=8.0, help="Poisson arrivals per second")
+    ap.add_argument("--batch-m-hi", type=int, default=5000,
+                    help="largest m of the batched LPs (5000 = the named workload)")
+    ap.add_argument("--only-batch", action="store_true",
+                    help="run only the batched measurement (profiling small cases)")
     return ap.parse_args()
 
 
@@ -170,7 +174,7 @@ def cpu_baseline(lp, budget_s: float = 20.0) -> dict:
                        f"{t_setup:.1f} s of untimed preprocessing"), "seconds": t}
 
 
-def measure_batch(h, count: int, sample: int) -> dict:
+def measure_batch(h, count: int, sample: int, m_hi: int = 5000) -> dict:
     """LPs/s to 1e-4 relative KKT on `count` random sparse LPs (m log-U[50,5000],
     n = 2m, 3-8 nonzeros per column, seed 1000 + i): the batched solver with
     FP32 iterates (stalled FP32 LPs finish in its FP64 phase) and with FP64
@@ -181,7 +185,7 @@ def measure_batch(h, count: int, sample: int) -> dict:
     from coolpdlp import _abi as A
     from coolpdlp import generators as G
     from coolpdlp import native
-    lps = G.batch_lps(count)
+    lps = G.batch_lps(count, m_hi=m_hi)
     S = [native.LPStruct(lp.m, lp.n, lp.colptr, lp.rowval, lp.nzval, lp.c, lp.lv, lp.uv, lp.lc,
                          lp.uc) for lp in lps]
     warm = native.default_params()
@@ -197,7 +201,10 @@ def measure_batch(h, count: int, sample: int) -> dict:
         rel = np.array([max(s.err.primal / s.err.primal_scale, s.err.dual / s.err.dual_scale,
                             s.err.gap / s.err.gap_scale) for s in st])
         res[name] = xs
+        te = np.array([s.time_elapsed for s in st])
         out[name] = {"lps_per_s": count / dt, "seconds": dt,
+                     "lp_seconds_sum": float(te.sum()), "lp_seconds_max": float(te.max()),
+                     "setup_seconds": float(st[0].setup_seconds),
                      "optimal": int(sum(s.termination_status == 0 for s in st)),
                      "max_rel_kkt": float(np.nanmax(rel)),
                      "fp64_phase_lps": int(sum(s.refine_kkt_passes > 0 for s in st)),
@@ -219,7 +226,7 @@ def measure_batch(h, count: int, sample: int) -> dict:
                               "mean_passes": passes / len(idx)}
     out["speedup_fp32_refined_vs_sequential"] = out["fp32_refined"]["lps_per_s"] / seq
     out["speedup_fp64_batched_vs_sequential"] = out["fp64_batched"]["lps_per_s"] / seq
-    out["workload"] = (f"{count} random sparse LPs, m log-U[50,5000], n=2m, 3-8 nnz/column, "
+    out["workload"] = (f"{count} random sparse LPs, m log-U[50,{m_hi}], n=2m, 3-8 nnz/column, "
                        "seed 1000+i, 1e-4 relative KKT")
     return out
 
@@ -308,6 +315,15 @@ def run_ours(args):
     from coolpdlp import _abi as A
     from coolpdlp import native
 
+    if args.only_batch:
+        # the batched workload alone (small cases for profilers); no headline value
+        if rank == 0:
+            h = native.Handle(local)
+            print(json.dumps({"metric": METRIC, "impl": "ours", "value": None,
+                              "batch": measure_batch(h, args.batch_lps, args.sequential_sample,
+                                                     args.batch_m_hi)}),
+                  flush=True)
+        return
     lp = workload(args.scale)
     h = native.Handle(local)
     prm = A.default_params_py(A.ALGO_PDLP)
@@ -438,7 +454,8 @@ def run_ours(args):
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(lp)
         if args.batch_lps > 0:
-            line["batch"] = measure_batch(h, args.batch_lps, args.sequential_sample)
+            line["batch"] = measure_batch(h, args.batch_lps, args.sequential_sample,
+                                          args.batch_m_hi)
         if args.serve_requests > 0:
             line["serving"] = measure_serving(args.serve_requests, args.serve_rate)
         print(json.dumps(line), flush=True)

@@ -28,6 +28,8 @@
 #include <numeric>
 #include <type_traits>
 
+#include <cooperative_groups.h>
+
 #include "batch.cuh"
 #include "epilogues.cuh"
 #include "solver.cuh"
@@ -36,10 +38,17 @@ namespace cpdlp {
 
 namespace {
 
+namespace cg = cooperative_groups;
+
 constexpr int BW = TILE_WARPS;  // warps per CTA
 constexpr int BT = BW * 32;
 constexpr int BATCH_ITEMS = 4;  // default nonzeros per lane of a short tile (128-nonzero tiles)
 constexpr int BATCH_RPL = 1;    // rows per lane: short tiles of at most 32 rows
+// LPs with at least CLUSTER_MIN_NNZ nonzeros are solved by a thread-block
+// cluster of CLUSTER_CTAS CTAs instead of one CTA
+constexpr int CLUSTER_CTAS = 8;
+constexpr int64_t CLUSTER_MIN_NNZ = 24000;
+
 #ifndef CPDLP_BATCH_MINB
 #define CPDLP_BATCH_MINB 2      // resident CTAs per SM the solve kernel is compiled for
 #endif
@@ -50,7 +59,7 @@ struct BatchLP {
     int32_t at_t0, at_t1, at_l0, at_l1;
     int32_t a_lid0, a_lid1, at_lid0, at_lid1;
     int32_t zero_cost, warm;
-    double power_tol, reltol, time_limit;
+    double power_tol, power_rtol, reltol, time_limit;
     int64_t power_maxiter, max_passes;
     int64_t stall_passes;  // > 0: stop when the error has not halved for this many passes
     double theta0;         // >= 0: |A|^2 estimate carried over (the power method is skipped)
@@ -125,14 +134,41 @@ struct BatchCtl {
     int64_t passes, outer, inner, total, power_it;
     double best_rel;       // smallest relative error at a halving mark
     int64_t mark;          // passes at that mark
-    int32_t lp, status, flag, from_avg, restart_valid, cancelled, stop, stalled;
+    double eta_sum;        // the averaging weight sum (thread 0)
+    double kd[2][5];       // step coefficients of this step and the next, rounded to T
+    int32_t lp, status, flag, from_avg, restart_valid, cancelled, stop, stalled, tl_hit;
 };
 
-// -- block-wide helpers ---------------------------------------------------------
-// Sums Q per-thread values over the CTA in a fixed order (warp trees, then the
-// warps in order); every thread receives the sums.
-template <int Q>
-__device__ __forceinline__ void block_sum(double (&v)[Q], double* sh) {
+// -- the CTA group that solves one LP ------------------------------------------
+// One CTA (CS = 1) or a thread-block cluster of CS CTAs on as many SMs, joined
+// by the hardware cluster barrier and distributed shared memory.  Every branch
+// that encloses a group barrier depends only on values that are identical in
+// all CTAs of the group: the LP's descriptor, group sums (computed in the same
+// order by every CTA), and the few clock- or flag-derived values that rank 0
+// reads and the other CTAs copy from it.
+template <int CS>
+struct Grp {
+    static __device__ __forceinline__ void sync() {
+        if constexpr (CS == 1) __syncthreads();
+        else cg::this_cluster().sync();
+    }
+    static __device__ __forceinline__ int rank() {
+        if constexpr (CS == 1) return 0;
+        else return (int)cg::this_cluster().block_rank();
+    }
+    // the copy of the shared variable *p held by CTA r of the group
+    template <class P>
+    static __device__ __forceinline__ P* at(P* p, int r) {
+        if constexpr (CS == 1) return p;
+        else return cg::this_cluster().map_shared_rank(p, r);
+    }
+};
+
+// Sums Q per-thread values over the group in a fixed order (warp trees, the
+// warps of each CTA in order, then the CTAs in rank order); every thread of
+// every CTA receives the same sums.  sh: BW*Q + Q doubles of shared memory.
+template <int Q, int CS>
+__device__ __forceinline__ void grp_sum(double (&v)[Q], double* sh) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
     for (int q = 0; q < Q; q++) {
@@ -147,22 +183,28 @@ __device__ __forceinline__ void block_sum(double (&v)[Q], double* sh) {
         for (int ww = 0; ww < BW; ww++) s += sh[ww * Q + threadIdx.x];
         sh[BW * Q + threadIdx.x] = s;
     }
-    __syncthreads();
+    Grp<CS>::sync();
 #pragma unroll
-    for (int q = 0; q < Q; q++) v[q] = sh[BW * Q + q];
-    __syncthreads();
+    for (int q = 0; q < Q; q++) {
+        double s = Grp<CS>::at(sh, 0)[BW * Q + q];
+        for (int r = 1; r < CS; r++) s += Grp<CS>::at(sh, r)[BW * Q + q];
+        v[q] = s;
+    }
+    Grp<CS>::sync();
 }
 
-// the LP's tiles of one matrix, warps striding over its tasks; the vectors are
-// gathered with coherent loads (this kernel rewrites them between products)
-template <int ITEMS, class V, class T, class Epi>
+// the LP's tiles of one matrix, the group's warps striding over its tasks; the
+// vectors are gathered with coherent loads (this kernel rewrites them between
+// products)
+template <int ITEMS, int CS, class V, class T, class Epi>
 __device__ __forceinline__ void lp_tiles(const CsrView<V, T>& A, int t0, int t1, int l0, int l1,
                                          const T* xin, Epi& epi, typename Epi::Acc& acc,
                                          T* prod) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int gw = Grp<CS>::rank() * BW + w;
     const VecSet<T, 1, true> xs{{xin}};
-    for (int t = l0 + w; t < l1; t += BW) long_piece<ITEMS, 1>(A, xs, epi, acc, A.ltasks[t], lane);
-    for (int t = t0 + w; t < t1; t += BW) {
+    for (int t = l0 + gw; t < l1; t += BW * CS) long_piece<ITEMS, 1>(A, xs, epi, acc, A.ltasks[t], lane);
+    for (int t = t0 + gw; t < t1; t += BW * CS) {
         const int4 tk = A.tasks[t];
         short_tile<ITEMS, 1, V, T, Epi, true, BATCH_RPL>(A, xs, epi, acc, tk.x, tk.y, tk.z, tk.w,
                                                        lane, prod + w * 32 * ITEMS);
@@ -182,9 +224,22 @@ __device__ __forceinline__ bool should_restart(const BatchParams& p, double ac, 
            ((double)inner >= p.artificial_decay * (double)total);
 }
 
-// KKT errors of (xv, yv) (errors.jl:65-109) into *out (thread 0); all threads
-// take part; ends with a barrier
-template <int ITEMS, class T>
+// step coefficients (pdlp.jl:108-117, averaging :126-136): tau = eta/omega,
+// sigma = eta*omega, 1/sigma, and the averaging weights eta/(eta+S), S/(eta+S)
+template <class T>
+__device__ __forceinline__ void fill_coef(BatchCtl& C, int slot, double eta, double omega,
+                                          double es) {
+    const double sigma = eta * omega;
+    C.kd[slot][0] = (double)(T)(eta / omega);
+    C.kd[slot][1] = (double)(T)sigma;
+    C.kd[slot][2] = (double)(T)(1.0 / sigma);
+    C.kd[slot][3] = (double)(T)(eta / (eta + es));
+    C.kd[slot][4] = (double)(T)(es / (eta + es));
+}
+
+// KKT errors of (xv, yv) (errors.jl:65-109) into *out (thread 0 of every CTA,
+// identical values); the whole group takes part; ends with a group barrier
+template <int ITEMS, int CS, class T>
 __device__ __forceinline__ void lp_kkt(const BatchArgs<T>& g, const BatchCtl& C, const T* xv,
                                        const T* yv, cpdlp_kkt_errors* out, T* prod, double* sh) {
     const BatchLP& L = C.L;
@@ -195,8 +250,8 @@ __device__ __forceinline__ void lp_kkt(const BatchArgs<T>& g, const BatchCtl& C,
         re.block_out = nullptr; re.long_out = g.longA;
         typename KktRowEpi<T, 1>::Acc a;
         re.init(a);
-        lp_tiles<ITEMS, T>(g.A, L.a_t0, L.a_t1, L.a_l0, L.a_l1, xv, re, a, prod);
-        block_sum<2>(a.v, sh);
+        lp_tiles<ITEMS, CS>(g.A, L.a_t0, L.a_t1, L.a_l0, L.a_l1, xv, re, a, prod);
+        grp_sum<2, CS>(a.v, sh);
         rs[0] = a.v[0]; rs[1] = a.v[1];
     }
     {
@@ -205,8 +260,8 @@ __device__ __forceinline__ void lp_kkt(const BatchArgs<T>& g, const BatchCtl& C,
         ce.block_out = nullptr; ce.long_out = g.longAt;
         typename KktColEpi<T, 1>::Acc a;
         ce.init(a);
-        lp_tiles<ITEMS, T>(g.At, L.at_t0, L.at_t1, L.at_l0, L.at_l1, yv, ce, a, prod);
-        block_sum<3>(a.v, sh);
+        lp_tiles<ITEMS, CS>(g.At, L.at_t0, L.at_t1, L.at_l0, L.at_l1, yv, ce, a, prod);
+        grp_sum<3, CS>(a.v, sh);
         cs[0] = a.v[0]; cs[1] = a.v[1]; cs[2] = a.v[2];
     }
     if (threadIdx.x == 0) {
@@ -226,14 +281,19 @@ __device__ __forceinline__ void lp_kkt(const BatchArgs<T>& g, const BatchCtl& C,
         out->gap = fabs((cs[2] + rs[1]) + cs[1]);
         out->gap_scale = (1.0 + fabs(rs[1] + cs[1])) + fabs(cs[2]);
     }
-    __syncthreads();  // the long-row terms are rewritten by the next pass
+    Grp<CS>::sync();  // the long-row terms are rewritten by the next pass
 }
 
-// solve(milp, algo) for the LP in C (dequeued by thread 0)
-template <int ITEMS, class T>
+// solve(milp, algo) for the LP in C.  Every CTA of the group keeps its own copy
+// of C and updates it identically; rank 0 alone reads the clock and the cancel
+// flag and the others copy those two values from it.
+template <int ITEMS, class T, int CS>
 __device__ __forceinline__ void solve_one(const BatchArgs<T>& g, BatchCtl& C, T* prod,
                                           double* sh) {
     const int tid = threadIdx.x;
+    const int rank = Grp<CS>::rank();
+    const int gt = rank * BT + tid;  // thread index in the group
+    constexpr int GT = BT * CS;      // threads in the group
     const bool pdlp = g.prm.algorithm == CPDLP_ALGO_PDLP;
     const int c0 = C.L.col_off, c1 = c0 + C.L.n, r0 = C.L.row_off, r1 = r0 + C.L.m;
     // ---- step size from the power method's estimate (step_size.jl:22-27),
@@ -242,19 +302,19 @@ __device__ __forceinline__ void solve_one(const BatchArgs<T>& g, BatchCtl& C, T*
     double omega;
     {
         double q[4] = {0, 0, 0, 0};
-        for (int i = r0 + tid; i < r1; i += BT) {
+        for (int i = r0 + gt; i < r1; i += GT) {
             const double cb = combine((double)g.lc[i], (double)g.uc[i]);
             const double sv = g.invD1[i] * cb;
             q[0] += sv * sv;
             q[1] += cb * cb;
         }
-        for (int j = c0 + tid; j < c1; j += BT) {
+        for (int j = c0 + gt; j < c1; j += GT) {
             const double cj = (double)g.c[j];
             const double sv = g.invD2[j] * cj;
             q[2] += sv * sv;
             q[3] += cj * cj;
         }
-        block_sum<4>(q, sh);
+        grp_sum<4, CS>(q, sh);
         const double cn = sqrt(q[3]), bn = sqrt(q[1]);
         omega = !pdlp ? 1.0 : (cn > g.prm.zero_tol && bn > g.prm.zero_tol) ? cn / bn : 1.0;
         if (pdlp && C.L.omega0 > 0) omega = C.L.omega0;
@@ -264,15 +324,14 @@ __device__ __forceinline__ void solve_one(const BatchArgs<T>& g, BatchCtl& C, T*
             C.power_it = g.power_iters[C.lp];
         }
     }
-    double eta_sum = 0.0;
     // ---- initial iterates: sol = precondition(sol_init) (preconditioning.jl:45-51),
     // sol_last = 0, avg = sol, avg_last = 0, restart = sol (pdlp.jl:45-67)
-    for (int j = c0 + tid; j < c1; j += BT) {
+    for (int j = c0 + gt; j < c1; j += GT) {
         const T v = (C.L.warm && g.x_init) ? (T)__ddiv_rn(g.x_init[j], g.D2[j]) : T(0);
         g.x[0][j] = v; g.x[1][j] = T(0); g.xa[0][j] = v; g.xa[1][j] = T(0);
         g.xr[j] = v; g.xbar[j] = T(0);
     }
-    for (int i = r0 + tid; i < r1; i += BT) {
+    for (int i = r0 + gt; i < r1; i += GT) {
         const T v = (C.L.warm && g.y_init) ? (T)__ddiv_rn(g.y_init[i], g.D1[i]) : T(0);
         g.y[0][i] = v; g.y[1][i] = T(0); g.ya[0][i] = v; g.ya[1][i] = T(0);
         g.yr[i] = v;
@@ -288,52 +347,75 @@ __device__ __forceinline__ void solve_one(const BatchArgs<T>& g, BatchCtl& C, T*
         C.status = CPDLP_STILL_RUNNING;
         C.stop = 0;
         C.omega = omega;
+        C.eta_sum = 0.0;
+        fill_coef<T>(C, 0, eta, omega, 0.0);
     }
-    __syncthreads();
+    Grp<CS>::sync();
+    int stepc = 0;  // steps taken (the coefficient slot of the next step is stepc & 1)
     if (C.L.m == 0 && C.L.zero_cost) {  // early exit (common.jl:194-198)
-        for (int j = c0 + tid; j < c1; j += BT) g.x[0][j] = proj_box(T(0), g.lv[j], g.uv[j]);
+        for (int j = c0 + gt; j < c1; j += GT) g.x[0][j] = proj_box(T(0), g.lv[j], g.uv[j]);
         if (tid == 0) {
             C.status = CPDLP_OPTIMAL;
             C.stop = 1;
             const double nan = __longlong_as_double(0x7ff8000000000000ll);
             C.e_sol = cpdlp_kkt_errors{nan, nan, nan, nan, nan, nan};
         }
-        __syncthreads();
+        Grp<CS>::sync();
     }
     const double tlim_ns = C.L.time_limit * 1e9;
     while (!C.stop) {
         // ---- check_every steps (pdlp.jl:96-124, averaging :126-136)
         for (int st = 0; st < g.prm.check_every; st++) {
-            const double sigma = eta * omega;
+            // coefficients computed by thread 0 one step ahead (FP64 division is
+            // slow, so not every thread does it); the slot of the next step was
+            // last read two barriers ago
+            const int sl = stepc & 1;
             StepCoef<T> k;
-            k.tau = (T)(eta / omega);
-            k.sigma = (T)sigma;
-            k.inv_sigma = (T)(1.0 / sigma);
-            k.a = (T)(eta / (eta + eta_sum));
-            k.b = (T)(eta_sum / (eta + eta_sum));
-            if (pdlp) eta_sum += eta;
+            k.tau = (T)C.kd[sl][0];
+            k.sigma = (T)C.kd[sl][1];
+            k.inv_sigma = (T)C.kd[sl][2];
+            k.a = (T)C.kd[sl][3];
+            k.b = (T)C.kd[sl][4];
+            if (tid == 0) {
+                if (pdlp) C.eta_sum += eta;
+                fill_coef<T>(C, sl ^ 1, eta, C.omega, C.eta_sum);
+            }
             const int o = cur, nw = cur ^ 1;
             {
                 PrimalEpi<T, true> pe{g.x[o], g.c, g.lv, g.uv, g.x[nw], g.xbar, g.xa[o], g.xa[nw],
                                       {k}, pdlp ? 1 : 0};
                 NoAcc a;
-                lp_tiles<ITEMS, T>(g.At, C.L.at_t0, C.L.at_t1, C.L.at_l0, C.L.at_l1, g.y[o], pe, a, prod);
+                lp_tiles<ITEMS, CS>(g.At, C.L.at_t0, C.L.at_t1, C.L.at_l0, C.L.at_l1, g.y[o], pe, a, prod);
             }
-            __syncthreads();
+            Grp<CS>::sync();
             {
                 DualEpi<T, true> de{g.y[o], g.lc, g.uc, g.y[nw], g.ya[o], g.ya[nw], {k}, pdlp ? 1 : 0};
                 NoAcc a;
-                lp_tiles<ITEMS, T>(g.A, C.L.a_t0, C.L.a_t1, C.L.a_l0, C.L.a_l1, g.xbar, de, a, prod);
+                lp_tiles<ITEMS, CS>(g.A, C.L.a_t0, C.L.a_t1, C.L.a_l0, C.L.a_l1, g.xbar, de, a, prod);
             }
-            __syncthreads();
+            Grp<CS>::sync();
             cur ^= 1;
+            stepc++;
         }
         // ---- KKT errors of sol, avg, sol_last, avg_last (errors.jl:65-109)
         const int nv = pdlp ? 4 : 1;
         for (int p = 0; p < nv; p++) {
             const T* xv = p == 0 ? g.x[cur] : p == 1 ? g.xa[cur] : p == 2 ? g.x[cur ^ 1] : g.xa[cur ^ 1];
             const T* yv = p == 0 ? g.y[cur] : p == 1 ? g.ya[cur] : p == 2 ? g.y[cur ^ 1] : g.ya[cur ^ 1];
-            lp_kkt<ITEMS, T>(g, C, xv, yv, &C.e[p], prod, sh);
+            lp_kkt<ITEMS, CS, T>(g, C, xv, yv, &C.e[p], prod, sh);
+        }
+        // ---- the clock and the cancel flag, read once for the group by rank 0
+        if (rank == 0 && tid == 0) {
+            C.tl_hit = (double)(global_ns() - C.t_start) >= tlim_ns ? 1 : 0;
+            C.cancelled = *(volatile const int*)g.cancel;
+        }
+        if constexpr (CS > 1) {
+            Grp<CS>::sync();
+            if (rank != 0 && tid == 0) {
+                const BatchCtl* c0p = Grp<CS>::at(&C, 0);
+                C.tl_hit = c0p->tl_hit;
+                C.cancelled = c0p->cancelled;
+            }
         }
         // ---- termination (common.jl:218-231) and restart decision (pdlp.jl:138-170)
         if (tid == 0) {
@@ -343,10 +425,9 @@ __device__ __forceinline__ void solve_one(const BatchArgs<T>& g, BatchCtl& C, T*
                 C.total += g.prm.check_every;
             }
             C.e_sol = C.e[0];
-            const double elapsed = (double)(global_ns() - C.t_start);
             int32_t stt = CPDLP_STILL_RUNNING;
             if (rel_err(C.e_sol) <= C.L.reltol) stt = CPDLP_OPTIMAL;
-            else if (elapsed >= tlim_ns) stt = CPDLP_TIME_LIMIT;
+            else if (C.tl_hit) stt = CPDLP_TIME_LIMIT;
             else if (C.passes >= C.L.max_passes) stt = CPDLP_ITERATION_LIMIT;
             // stall: the relative error has not halved over stall_passes passes
             const double rel = rel_err(C.e_sol);
@@ -358,7 +439,7 @@ __device__ __forceinline__ void solve_one(const BatchArgs<T>& g, BatchCtl& C, T*
                 stt = CPDLP_ITERATION_LIMIT;
                 C.stalled = 1;
             }
-            const int cancelled = *(volatile const int*)g.cancel;
+            const int cancelled = C.cancelled;
             int flag = 0;
             if (stt == CPDLP_STILL_RUNNING && !cancelled && pdlp) {
                 const double w = C.omega;
@@ -371,7 +452,6 @@ __device__ __forceinline__ void solve_one(const BatchArgs<T>& g, BatchCtl& C, T*
                                           abs_err(C.e[2], w), C.inner, C.total) ? 3 : 0;
             }
             C.status = stt;
-            C.cancelled = cancelled;
             C.stop = (stt != CPDLP_STILL_RUNNING) || cancelled;
             C.flag = flag;
         }
@@ -380,7 +460,7 @@ __device__ __forceinline__ void solve_one(const BatchArgs<T>& g, BatchCtl& C, T*
         __syncthreads();
         if (flag == 2) {
             // errors of the initial restart point (sol_restart = the start)
-            lp_kkt<ITEMS, T>(g, C, g.xr, g.yr, &C.e_restart, prod, sh);
+            lp_kkt<ITEMS, CS, T>(g, C, g.xr, g.yr, &C.e_restart, prod, sh);
             if (tid == 0) {
                 C.restart_valid = 1;
                 const double w = C.omega;
@@ -396,26 +476,25 @@ __device__ __forceinline__ void solve_one(const BatchArgs<T>& g, BatchCtl& C, T*
             const T* cx = C.from_avg ? g.xa[cur] : g.x[cur];
             const T* cy = C.from_avg ? g.ya[cur] : g.y[cur];
             double q[2] = {0.0, 0.0};
-            for (int j = c0 + tid; j < c1; j += BT) {
+            for (int j = c0 + gt; j < c1; j += GT) {
                 const double d = (double)cx[j] - (double)g.xr[j];
                 q[0] += d * d;
             }
-            for (int i = r0 + tid; i < r1; i += BT) {
+            for (int i = r0 + gt; i < r1; i += GT) {
                 const double d = (double)cy[i] - (double)g.yr[i];
                 q[1] += d * d;
             }
-            block_sum<2>(q, sh);
-            eta_sum = 0.0;
+            grp_sum<2, CS>(q, sh);
             const double dx = sqrt(q[0]), dy = sqrt(q[1]), th = g.prm.primal_weight_damping;
             if (dx > g.prm.zero_tol && dy > g.prm.zero_tol)
                 omega = exp(th * log(dy / dx) + (1.0 - th) * log(omega));
-            for (int j = c0 + tid; j < c1; j += BT) {
+            for (int j = c0 + gt; j < c1; j += GT) {
                 const T v = cx[j];
                 g.x[cur][j] = v;
                 g.xr[j] = v;
                 g.xa[cur][j] = T(0);
             }
-            for (int i = r0 + tid; i < r1; i += BT) {
+            for (int i = r0 + gt; i < r1; i += GT) {
                 const T v = cy[i];
                 g.y[cur][i] = v;
                 g.yr[i] = v;
@@ -423,19 +502,21 @@ __device__ __forceinline__ void solve_one(const BatchArgs<T>& g, BatchCtl& C, T*
             }
             if (tid == 0) {
                 C.omega = omega;
+                C.eta_sum = 0.0;
+                fill_coef<T>(C, stepc & 1, eta, omega, 0.0);
                 C.e_restart = C.e_cand;
                 C.outer += 1;
                 C.inner = 0;
             }
-            __syncthreads();
+            Grp<CS>::sync();
         }
     }
     // ---- get_solution (common.jl:233-235): unscaled, double
-    for (int j = c0 + tid; j < c1; j += BT) g.out_x[j] = g.D2[j] * (double)g.x[cur][j];
-    for (int i = r0 + tid; i < r1; i += BT) g.out_y[i] = g.D1[i] * (double)g.y[cur][i];
+    for (int j = c0 + gt; j < c1; j += GT) g.out_x[j] = g.D2[j] * (double)g.x[cur][j];
+    for (int i = r0 + gt; i < r1; i += GT) g.out_y[i] = g.D1[i] * (double)g.y[cur][i];
     __threadfence_system();
-    __syncthreads();
-    if (tid == 0) {
+    Grp<CS>::sync();
+    if (rank == 0 && tid == 0) {
         BatchResult R;
         R.err = C.e_sol;
         R.kkt_passes = C.passes;
@@ -446,7 +527,7 @@ __device__ __forceinline__ void solve_one(const BatchArgs<T>& g, BatchCtl& C, T*
         R.eta = eta;
         R.theta = g.theta[C.lp];
         R.omega = omega;
-        R.eta_sum = eta_sum;
+        R.eta_sum = C.eta_sum;
         R.time_elapsed = (double)(global_ns() - C.t_start) * 1e-9;
         R.status = C.status;
         R.restart_from_avg = C.from_avg;
@@ -459,14 +540,14 @@ __device__ __forceinline__ void solve_one(const BatchArgs<T>& g, BatchCtl& C, T*
 }
 
 // an LP dequeued after a cancellation: not started
-template <class T>
+template <class T, int CS>
 __device__ __forceinline__ void skip_one(const BatchArgs<T>& g, const BatchCtl& C) {
-    const int tid = threadIdx.x;
-    for (int j = C.L.col_off + tid; j < C.L.col_off + C.L.n; j += BT) g.out_x[j] = 0.0;
-    for (int i = C.L.row_off + tid; i < C.L.row_off + C.L.m; i += BT) g.out_y[i] = 0.0;
+    const int gt = Grp<CS>::rank() * BT + threadIdx.x;
+    for (int j = C.L.col_off + gt; j < C.L.col_off + C.L.n; j += BT * CS) g.out_x[j] = 0.0;
+    for (int i = C.L.row_off + gt; i < C.L.row_off + C.L.m; i += BT * CS) g.out_y[i] = 0.0;
     __threadfence_system();
-    __syncthreads();
-    if (tid == 0) {
+    Grp<CS>::sync();
+    if (Grp<CS>::rank() == 0 && threadIdx.x == 0) {
         BatchResult R;
         memset(&R, 0, sizeof(R));
         const double nan = __longlong_as_double(0x7ff8000000000000ll);
@@ -478,50 +559,61 @@ __device__ __forceinline__ void skip_one(const BatchArgs<T>& g, const BatchCtl& 
     }
 }
 
-// powm! on A'A with IterativeSolvers' stopping rule (linalg.jl:86-96): one CTA
-// per LP from a queue, FP64 vectors
-template <int ITEMS, class V>
+// powm! on A'A with IterativeSolvers' stopping rule (linalg.jl:86-96), FP64
+// vectors; one group (a CTA or a cluster) per LP from a queue.  With FP32
+// iterates the loop also stops once the residual is below power_rtol * theta
+// (BatchLP.power_rtol > 0).
+template <int ITEMS, class V, int CS>
 __global__ void __launch_bounds__(BT) k_batch_power(PowerArgs<V> g) {
     __shared__ double prod[BW * 32 * ITEMS];
     __shared__ double sh[BW * 8 + 8];
     __shared__ BatchLP L;
     __shared__ int s_lp;
     const int tid = threadIdx.x;
+    const int rank = Grp<CS>::rank();
+    const int gt = rank * BT + tid;
+    constexpr int GT = BT * CS;
     for (int guard = 0; guard <= g.count; guard++) {
-        if (tid == 0) {
+        if (rank == 0 && tid == 0) {
             const int q = atomicAdd(g.next, 1);
             s_lp = q < g.count ? g.order[q] : -1;
-            if (s_lp >= 0) L = g.lps[s_lp];
         }
+        if constexpr (CS > 1) {
+            Grp<CS>::sync();
+            if (rank != 0 && tid == 0) s_lp = *Grp<CS>::at(&s_lp, 0);
+            Grp<CS>::sync();  // rank 0's copy is read before it changes or exits
+        }
+        if (tid == 0 && s_lp >= 0) L = g.lps[s_lp];
         __syncthreads();
         if (s_lp < 0) break;
         if (L.theta0 >= 0) {  // carried over from an earlier run of the same LP
-            if (tid == 0) {
+            if (rank == 0 && tid == 0) {
                 g.theta[s_lp] = L.theta0;
                 g.iters[s_lp] = 0;
             }
-            __syncthreads();
+            Grp<CS>::sync();
             continue;
         }
         const int c0 = L.col_off, c1 = c0 + L.n;
-        for (int j = c0 + tid; j < c1; j += BT) g.x[j] = g.x_start[j];
-        __syncthreads();
+        for (int j = c0 + gt; j < c1; j += GT) g.x[j] = g.x_start[j];
+        Grp<CS>::sync();
         double theta = 0.0, residual = INFINITY;
         int64_t it = 0;
-        while (!(it > L.power_maxiter || residual <= L.power_tol)) {
+        while (!(it > L.power_maxiter || residual <= L.power_tol ||
+                 (L.power_rtol > 0 && residual <= L.power_rtol * theta))) {
             {
                 StoreEpi<double> se{g.s};
                 NoAcc a;
-                lp_tiles<ITEMS, V, double>(g.A, L.a_t0, L.a_t1, L.a_l0, L.a_l1, g.x, se, a, prod);
+                lp_tiles<ITEMS, CS>(g.A, L.a_t0, L.a_t1, L.a_l0, L.a_l1, g.x, se, a, prod);
             }
-            __syncthreads();
+            Grp<CS>::sync();
             double th, inv;
             {
                 PowerEpi<double> pe{g.x, g.Atx, nullptr, g.longAt};
                 PowerEpi<double>::Acc a;
                 pe.init(a);
-                lp_tiles<ITEMS, V, double>(g.At, L.at_t0, L.at_t1, L.at_l0, L.at_l1, g.s, pe, a, prod);
-                block_sum<2>(a.v, sh);
+                lp_tiles<ITEMS, CS>(g.At, L.at_t0, L.at_t1, L.at_l0, L.at_l1, g.s, pe, a, prod);
+                grp_sum<2, CS>(a.v, sh);
                 double s0 = a.v[0], s1 = a.v[1];
                 for (int l = L.at_lid0; l < L.at_lid1; l++) {
                     s0 += g.longAt[(size_t)l * 2];
@@ -531,45 +623,65 @@ __global__ void __launch_bounds__(BT) k_batch_power(PowerArgs<V> g) {
                 inv = 1.0 / sqrt(s1);
             }
             double racc[1] = {0.0};
-            for (int j = c0 + tid; j < c1; j += BT) {
+            for (int j = c0 + gt; j < c1; j += GT) {
                 const double r = add_rn(mul_rn(-th, g.x[j]), g.Atx[j]);
                 racc[0] += r * r;
                 g.x[j] = mul_rn(g.Atx[j], inv);
             }
-            block_sum<1>(racc, sh);  // its barriers also order the long-row terms' reuse
+            grp_sum<1, CS>(racc, sh);  // its barriers also order the long-row terms' reuse
             residual = sqrt(racc[0]);
             theta = th;
             it++;
         }
-        if (tid == 0) {
+        if (rank == 0 && tid == 0) {
             g.theta[s_lp] = theta;
             g.iters[s_lp] = it;
         }
-        __syncthreads();
+        Grp<CS>::sync();
     }
+    Grp<CS>::sync();  // no CTA exits while another may read its shared memory
 }
 
-template <int ITEMS, class T>
+// The solve kernel: each group (a CTA, or a cluster of CS CTAs) takes LPs from
+// the queue until it is empty.  Rank 0 dequeues and reads the cancel flag; the
+// other CTAs copy both from it, so every CTA of a group leaves the loop at the
+// same LP.
+template <int ITEMS, class T, int CS>
 __global__ void __launch_bounds__(BT, CPDLP_BATCH_MINB) k_batch_pdlp(BatchArgs<T> g) {
     __shared__ T prod[BW * 32 * ITEMS];
     __shared__ double sh[BW * 8 + 8];
     __shared__ BatchCtl C;
+    const int rank = Grp<CS>::rank();
     for (int guard = 0; guard <= g.count; guard++) {
-        if (threadIdx.x == 0) {
+        if (rank == 0 && threadIdx.x == 0) {
             const int q = atomicAdd(g.next, 1);
             C.lp = q < g.count ? g.order[q] : -1;
-            if (C.lp >= 0) {
-                C.L = g.lps[C.lp];
-                C.t_start = global_ns();
-                C.cancelled = *(volatile const int*)g.cancel;
+            C.cancelled = C.lp >= 0 ? *(volatile const int*)g.cancel : 0;
+        }
+        if constexpr (CS > 1) {
+            Grp<CS>::sync();
+            if (rank != 0 && threadIdx.x == 0) {
+                const BatchCtl* c0p = Grp<CS>::at(&C, 0);
+                C.lp = c0p->lp;
+                C.cancelled = c0p->cancelled;
             }
+            // rank 0's shared memory must outlive every read of it: no CTA
+            // leaves (or rank 0 dequeues again) before all copies are done
+            Grp<CS>::sync();
+        }
+        if (threadIdx.x == 0 && C.lp >= 0) {
+            C.L = g.lps[C.lp];
+            C.t_start = global_ns();
         }
         __syncthreads();
         if (C.lp < 0) break;
-        if (C.cancelled) skip_one<T>(g, C);
-        else solve_one<ITEMS, T>(g, C, prod, sh);
-        __syncthreads();
+        if (C.cancelled) skip_one<T, CS>(g, C);
+        else solve_one<ITEMS, T, CS>(g, C, prod, sh);
+        Grp<CS>::sync();
     }
+    // every CTA of a group leaves at the same LP; none exits while another
+    // may still read its shared memory
+    Grp<CS>::sync();
 }
 
 uint64_t splitmix64_at_host(uint64_t seed, uint64_t counter) {
@@ -635,7 +747,9 @@ struct RunBase {
     int phase = 1;             // 1: first phase, 2: FP64 phase
     Handle rh;                 // the device, this run's stream
     Handle* parent = nullptr;  // owner of the host block pool
-    cudaEvent_t ev = nullptr;  // recorded after the solve kernel
+    cudaEvent_t ev = nullptr;  // recorded after both solve kernels
+    cudaStream_t s2 = nullptr; // the cluster kernel's stream
+    cudaEvent_t ev2 = nullptr; // orders s2 after the power method and ev after s2
     void* block = nullptr;
     BatchResult* h_res = nullptr;
     int* h_done = nullptr;
@@ -658,7 +772,9 @@ struct RunBase {
         rh.pinned = h.pinned_area(sizeof(double) * 64);   // shared: runs start one at a time
         rh.pinned_bytes = sizeof(double) * 64;
         CK(cudaStreamCreateWithFlags(&rh.stream, cudaStreamNonBlocking));
+        CK(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
         CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&ev2, cudaEventDisableTiming));
         const size_t a = ((size_t)count * sizeof(BatchResult) + 255) & ~(size_t)255;
         const size_t b = ((size_t)count * sizeof(int) + 255) & ~(size_t)255;
         const size_t bytes = a + b + sizeof(double) * (size_t)(std::max<int64_t>(N, 1) + std::max<int64_t>(M, 1));
@@ -682,7 +798,12 @@ struct RunBase {
         if (ev) cudaEventSynchronize(ev);
         if (rh.stream) cudaStreamSynchronize(rh.stream);
         release_device();
+        if (s2) cudaStreamSynchronize(s2);
         if (ev) cudaEventDestroy(ev);
+        if (ev2) cudaEventDestroy(ev2);
+        ev2 = nullptr;
+        if (s2) cudaStreamDestroy(s2);
+        s2 = nullptr;
         ev = nullptr;
         if (rh.stream) cudaStreamDestroy(rh.stream);
         rh.stream = nullptr;
@@ -703,6 +824,7 @@ struct Run : RunBase {
     DBuf<BatchLP> d_desc;
     DBuf<int32_t> d_order;
     DBuf<int> d_next;
+    DBuf<double> pw_x, pw_Atx, pw_s, pw_start, pw_pA, pw_pAt;  // power-method scratch
 
     ~Run() override { close(); }
 
@@ -727,11 +849,27 @@ struct Run : RunBase {
         AllocScope scope(s);
         // occupancy first: it loads the kernels, which must not wait behind
         // this run's own queued work
-        auto pk = (items == 8) ? k_batch_power<8, T> : k_batch_power<4, T>;
-        auto kern = (items == 8) ? k_batch_pdlp<8, T> : k_batch_pdlp<4, T>;
-        int per_sm_p = 0, per_sm = 0;
+        auto pk = (items == 8) ? k_batch_power<8, T, 1> : k_batch_power<4, T, 1>;
+        auto pkc = (items == 8) ? k_batch_power<8, T, CLUSTER_CTAS> : k_batch_power<4, T, CLUSTER_CTAS>;
+        auto kern = (items == 8) ? k_batch_pdlp<8, T, 1> : k_batch_pdlp<4, T, 1>;
+        auto kclu = (items == 8) ? k_batch_pdlp<8, T, CLUSTER_CTAS> : k_batch_pdlp<4, T, CLUSTER_CTAS>;
+        int per_sm_p = 0, per_sm = 0, nclusters = 0, nclusters_p = 0;
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_p, pk, BT, 0));
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BT, 0));
+        cudaLaunchAttribute cattr[1];
+        cattr[0].id = cudaLaunchAttributeClusterDimension;
+        cattr[0].val.clusterDim.x = CLUSTER_CTAS;
+        cattr[0].val.clusterDim.y = 1;
+        cattr[0].val.clusterDim.z = 1;
+        cudaLaunchConfig_t ccfg = {};
+        ccfg.gridDim = dim3(CLUSTER_CTAS);
+        ccfg.blockDim = dim3(BT);
+        ccfg.dynamicSmemBytes = 0;
+        ccfg.stream = s2;
+        ccfg.attrs = cattr;
+        ccfg.numAttrs = 1;
+        CK(cudaOccupancyMaxActiveClusters(&nclusters, kclu, &ccfg));
+        CK(cudaOccupancyMaxActiveClusters(&nclusters_p, pkc, &ccfg));
         // block-diagonal concatenation (1-based CSC)
         std::vector<int64_t> colptr((size_t)N + 1), rowval((size_t)std::max<int64_t>(NZ, 1));
         std::vector<double> nzval(rowval.size()), c((size_t)std::max<int64_t>(N, 1)),
@@ -788,6 +926,8 @@ struct Run : RunBase {
             // the power method runs in FP64 for either iterate type
             d.power_tol = prm.power_tol_override > 0 ? prm.power_tol_override : powm_tol(d.n, false);
             d.power_maxiter = prm.power_maxiter_override > 0 ? prm.power_maxiter_override : d.n;
+            // FP32 iterates need theta to about 1e-4, not to eps(Float64) n^3
+            d.power_rtol = std::is_same<T, float>::value ? POWER_RTOL_F32 : 0.0;
             d.reltol = lps[k].reltol;
             d.time_limit = lps[k].time_limit;
             d.max_passes = lps[k].max_passes;
@@ -800,6 +940,11 @@ struct Run : RunBase {
         std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
             return nz_off[a + 1] - nz_off[a] > nz_off[b + 1] - nz_off[b];
         });
+        // largest first: the first nbig LPs of the order go to the cluster kernel
+        // (the routing depends on the LP alone, so its arithmetic does too)
+        int64_t nbig = 0;
+        if (nclusters > 0 && nclusters_p > 0)
+            while (nbig < count && nz_off[order[nbig] + 1] - nz_off[order[nbig]] >= CLUSTER_MIN_NNZ) nbig++;
         // power-method start vectors: the single-LP generator, per LP from counter 0
         std::vector<double> xs((size_t)std::max<int64_t>(N, 1));
         for (int64_t k = 0; k < count; k++) {
@@ -830,7 +975,7 @@ struct Run : RunBase {
         d_piters.alloc((size_t)std::max<int64_t>(count, 1));
         longA.alloc((size_t)std::max(planA.nlong, 1) * 2);
         longAt.alloc((size_t)std::max(planAt.nlong, 1) * 3);
-        d_next.alloc(2);
+        d_next.alloc(4);
         if (any_warm) {
             d_x0.alloc(nz);
             d_y0.alloc(mz);
@@ -839,25 +984,41 @@ struct Run : RunBase {
         }
         CK(cudaMemcpyAsync(d_desc.p, desc.data(), sizeof(BatchLP) * desc.size(), cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(d_order.p, order.data(), sizeof(int32_t) * order.size(), cudaMemcpyHostToDevice, s));
-        CK(cudaMemsetAsync(d_next.p, 0, 2 * sizeof(int), s));
-        // power method (FP64 vectors, scratch released in stream order after it)
-        {
-            DBuf<double> px(nz), pAtx(nz), ps(mz), d_xs(nz);
-            DBuf<double> pA((size_t)std::max(planA.npieces, 1)), pAt((size_t)std::max(planAt.npieces, 1));
-            CK(cudaMemcpyAsync(d_xs.p, xs.data(), sizeof(double) * nz, cudaMemcpyHostToDevice, s));
-            PowerArgs<T> pg;
-            pg.A = CsrView<T, double>{P.a_ptr.p, P.a_idx.p, P.a_val.p, planA.tasks.p, planA.ntasks,
-                                      planA.ltasks.p, planA.nltasks, planA.counters.p, pA.p};
-            pg.At = CsrView<T, double>{P.at_ptr.p, P.at_idx.p, P.at_val.p, planAt.tasks.p,
-                                       planAt.ntasks, planAt.ltasks.p, planAt.nltasks,
-                                       planAt.counters.p, pAt.p};
-            pg.x = px.p; pg.Atx = pAtx.p; pg.s = ps.p; pg.x_start = d_xs.p;
-            pg.lps = d_desc.p; pg.order = d_order.p; pg.theta = d_theta.p; pg.iters = d_piters.p;
-            pg.longAt = longAt.p; pg.next = d_next.p + 1; pg.count = (int32_t)count;
-            int64_t pgrid = std::min<int64_t>(count, (int64_t)std::max(per_sm_p, 1) * rh.num_sms);
+        CK(cudaMemsetAsync(d_next.p, 0, 4 * sizeof(int), s));
+        // power method: FP64 vectors; the cluster-sized LPs on s2, the others on s
+        pw_x.alloc(nz); pw_Atx.alloc(nz); pw_s.alloc(mz); pw_start.alloc(nz);
+        pw_pA.alloc((size_t)std::max(planA.npieces, 1));
+        pw_pAt.alloc((size_t)std::max(planAt.npieces, 1));
+        CK(cudaMemcpyAsync(pw_start.p, xs.data(), sizeof(double) * nz, cudaMemcpyHostToDevice, s));
+        PowerArgs<T> pg;
+        pg.A = CsrView<T, double>{P.a_ptr.p, P.a_idx.p, P.a_val.p, planA.tasks.p, planA.ntasks,
+                                  planA.ltasks.p, planA.nltasks, planA.counters.p, pw_pA.p};
+        pg.At = CsrView<T, double>{P.at_ptr.p, P.at_idx.p, P.at_val.p, planAt.tasks.p,
+                                   planAt.ntasks, planAt.ltasks.p, planAt.nltasks,
+                                   planAt.counters.p, pw_pAt.p};
+        pg.x = pw_x.p; pg.Atx = pw_Atx.p; pg.s = pw_s.p; pg.x_start = pw_start.p;
+        pg.lps = d_desc.p; pg.theta = d_theta.p; pg.iters = d_piters.p; pg.longAt = longAt.p;
+        if (nbig > 0) {  // s2 starts after everything queued on s so far
+            CK(cudaEventRecord(ev2, s));
+            CK(cudaStreamWaitEvent(s2, ev2, 0));
+            PowerArgs<T> pb = pg;
+            pb.order = d_order.p;
+            pb.count = (int32_t)nbig;
+            pb.next = d_next.p + 3;
+            int64_t nc = std::min<int64_t>(nbig, nclusters_p);
+            if (max_ctas > 0) nc = std::min<int64_t>(nc, std::max<int64_t>(max_ctas / CLUSTER_CTAS, 1));
+            ccfg.gridDim = dim3((unsigned)(nc * CLUSTER_CTAS));
+            CK(cudaLaunchKernelEx(&ccfg, pkc, pb));
+        }
+        if (count > nbig) {
+            PowerArgs<T> ps1 = pg;
+            ps1.order = d_order.p + nbig;
+            ps1.count = (int32_t)(count - nbig);
+            ps1.next = d_next.p + 1;
+            int64_t pgrid = std::min<int64_t>(count - nbig, (int64_t)std::max(per_sm_p, 1) * rh.num_sms);
             if (max_ctas > 0) pgrid = std::min(pgrid, max_ctas);
             pgrid = std::max<int64_t>(pgrid, 1);
-            pk<<<(unsigned)pgrid, BT, 0, s>>>(pg);
+            pk<<<(unsigned)pgrid, BT, 0, s>>>(ps1);
             CK_LAUNCH();
         }
         int64_t grid = std::min<int64_t>(count, (int64_t)std::max(per_sm, 1) * rh.num_sms);
@@ -884,8 +1045,26 @@ struct Run : RunBase {
                             prm.invnorm_scaling, prm.primal_weight_damping, prm.zero_tol,
                             prm.sufficient_decay, prm.necessary_decay, prm.artificial_decay};
         setup = now_seconds() - t0;
-        kern<<<(unsigned)grid, BT, 0, s>>>(g);
-        CK_LAUNCH();
+        if (nbig > 0) {
+            // the cluster kernel on its own stream, after its LPs' power method
+            BatchArgs<T> gb = g;
+            gb.order = d_order.p;
+            gb.count = (int32_t)nbig;
+            gb.next = d_next.p + 2;
+            int64_t nc = std::min<int64_t>(nbig, nclusters);
+            if (max_ctas > 0) nc = std::min<int64_t>(nc, std::max<int64_t>(max_ctas / CLUSTER_CTAS, 1));
+            ccfg.gridDim = dim3((unsigned)(nc * CLUSTER_CTAS));
+            CK(cudaLaunchKernelEx(&ccfg, kclu, gb));  // after s2's power method
+            CK(cudaEventRecord(ev2, s2));
+        }
+        if (count > nbig) {
+            g.order = d_order.p + nbig;
+            g.count = (int32_t)(count - nbig);
+            grid = std::max<int64_t>(std::min<int64_t>(grid, count - nbig), 1);
+            kern<<<(unsigned)grid, BT, 0, s>>>(g);
+            CK_LAUNCH();
+        }
+        if (nbig > 0) CK(cudaStreamWaitEvent(s, ev2, 0));
         CK(cudaEventRecord(ev, s));
     }
     void release_device() override {
@@ -895,6 +1074,8 @@ struct Run : RunBase {
         bxr.release(); byr.release(); bxbar.release(); partA.release(); partAt.release();
         d_x0.release(); d_y0.release(); longA.release(); longAt.release(); d_desc.release();
         d_order.release(); d_theta.release(); d_piters.release(); d_next.release();
+        pw_x.release(); pw_Atx.release(); pw_s.release(); pw_start.release();
+        pw_pA.release(); pw_pAt.release();
         planA = TilePlan();
         planAt = TilePlan();
     }

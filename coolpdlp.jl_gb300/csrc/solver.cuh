@@ -11,6 +11,9 @@ namespace cpdlp {
 // FP32 iterates whose relative KKT error has not halved over this many checks
 // continue in FP64 (cpdlp_solve with refine_reltol > 0, and the batched solver)
 constexpr int64_t FP32_STALL_CHECKS = 30;
+// With FP32 iterates the power method also stops once its residual is below
+// this fraction of theta (the step size needs theta to about 1e-4)
+constexpr double POWER_RTOL_F32 = 1e-4;
 
 template <class T>
 struct StepCoef {

@@ -57,6 +57,8 @@ def lp_sets():
     from coolpdlp import generators as G
     single = [G.random_sparse_lp(1000, 2000, 5, seed=s) for s in range(3)]
     batch = G.batch_lps(12, m_lo=50, m_hi=400, seed0=1000)
+    # above the batched solver's cluster threshold (24,000 nonzeros)
+    batch += [G.random_sparse_lp(2600, 5200, 5, seed=1077), G.random_sparse_lp(4000, 8000, 4, seed=1078)]
     flows = [G.multicommodity_flow_lp(side=s, K=k, seed=20 + s) for s, k in ((6, 2), (8, 3), (10, 2))]
     return {"single": single, "batch": batch, "flow": flows}
 
