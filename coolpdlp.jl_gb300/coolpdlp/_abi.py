@@ -30,6 +30,8 @@ ERR_UNSUPPORTED = 7
 OPTIMAL, TIME_LIMIT, ITERATION_LIMIT, STILL_RUNNING = 0, 1, 2, 3
 ALGO_PDLP, ALGO_PDHG = 0, 1
 VAL_F64, VAL_F32, VAL_PM1 = 0, 1, 2
+# tile_flags bits: CPDLP_TILE_NO_NARROW keeps scaled values for a +-1 matrix
+TILE_NO_NARROW = 1
 FMT_CSR, FMT_ELL, FMT_COO = 0, 1, 2
 VEC_SOL, VEC_SOL_LAST, VEC_SOL_AVG, VEC_SOL_AVG_LAST, VEC_SOL_RESTART = 0, 1, 2, 3, 4
 

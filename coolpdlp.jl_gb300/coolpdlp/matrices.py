@@ -21,13 +21,18 @@ class _GPUSparseMatrix:
     FORMAT_ID = A.FMT_CSR
     FORMAT = "CSR"
 
-    def __init__(self, Acsc, dtype=np.float64, device: int = 0, handle=None):
+    def __init__(self, Acsc, dtype=np.float64, device: int = 0, handle=None, narrow: bool = False):
+        """narrow=True (CSR, float32, every value exactly +-1): the signs are
+        stored in the column indices and no value array exists."""
         C = CSCMatrix.from_any(Acsc)
         self.handle = handle or native.default_handle(device)
         self.dtype = np.dtype(dtype)
         if self.dtype not in (np.dtype(np.float64), np.dtype(np.float32)):
             raise A.ArgumentError(A.ERR_ARGUMENT, "matrix eltype must be float64 or float32")
-        vt = A.VAL_F64 if self.dtype == np.float64 else A.VAL_F32
+        if narrow and self.dtype != np.float32:
+            raise A.ArgumentError(A.ERR_ARGUMENT, "narrow +-1 storage has Float32 vectors")
+        self.narrow = bool(narrow)
+        vt = A.VAL_PM1 if narrow else (A.VAL_F64 if self.dtype == np.float64 else A.VAL_F32)
         ptr = c_void_p()
         cp, rv, nz = native.i64(C.colptr), native.i64(C.rowval), native.f64(C.nzval)
         self.handle.check(self.handle.lib.cpdlp_matrix_from_csc(

@@ -894,7 +894,10 @@ struct Run : RunBase {
         }
         cpdlp_lp big{M, N, NZ, colptr.data(), rowval.data(), nzval.data(), c.data(), lv.data(),
                      uv.data(), lc.data(), uc.data()};
-        PB.reset(problem_create(rh, &big, &prm));
+        // the batched kernels read the scaled values: no narrow +-1 storage
+        cpdlp_params pprm = prm;
+        pprm.tile_flags |= CPDLP_TILE_NO_NARROW;
+        PB.reset(problem_create(rh, &big, &pprm));
         auto& P = static_cast<ProblemT<T>&>(*PB);
         // tile plans with LP boundaries
         std::vector<int32_t> hpA((size_t)M + 1), hpAt((size_t)N + 1);
@@ -1213,7 +1216,7 @@ Job* job_submit(Handle& h, int64_t count, const cpdlp_lp* lps, const cpdlp_param
     if (params->check_every <= 0) fail(CPDLP_ERR_ARGUMENT, "check_every must be positive");
     if (params->float_type != CPDLP_VAL_F64 && params->float_type != CPDLP_VAL_F32)
         fail(CPDLP_ERR_ARGUMENT, "float_type must be CPDLP_VAL_F64 or CPDLP_VAL_F32");
-    if (params->tile_flags != 0) fail(CPDLP_ERR_ARGUMENT, "tile_flags is reserved and must be 0");
+    if (params->tile_flags & ~CPDLP_TILE_NO_NARROW) fail(CPDLP_ERR_ARGUMENT, "unknown tile_flags bits");
     if (count > INT32_MAX) fail(CPDLP_ERR_UNSUPPORTED, "batch too large");
     if (max_ctas < 0) fail(CPDLP_ERR_ARGUMENT, "max_ctas must be >= 0");
     for (int64_t k = 0; k < count; k++) check_lp(lps[k]);

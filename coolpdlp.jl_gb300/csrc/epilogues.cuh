@@ -32,6 +32,24 @@ struct StoreEpi {  // out = s (mul! with alpha = true, beta = false)
     __device__ void finish(Acc&) {}
 };
 
+// out_i = d_i * (d_i * s): the power method's first product over a Pm1 matrix
+// (s = (S D2 x)_i, so d1_i s is (A x)_i and the next product gathers d1 .* (A x))
+template <class T>
+struct ScaledStoreEpi {
+    T* out;
+    const T* __restrict__ dsc;
+    using Acc = NoAcc;
+    struct Pre {};
+    __device__ Pre pre_global(int) const { return Pre{}; }
+    __device__ void init(Acc&) {}
+    __device__ void row(int, int r, T s, const Pre&, Acc&) {
+        const T d = dsc[r];
+        out[r] = mul_rn(d, mul_rn(d, s));
+    }
+    __device__ void row_long(int p, int r, T s, int, Acc& a) { row(p, r, s, Pre{}, a); }
+    __device__ void finish(Acc&) {}
+};
+
 // Step coefficients tau, sigma, 1/sigma and the averaging weights: read from
 // device memory written before the launch (graph-captured step kernels), or
 // carried by value (the batched kernel, which changes them between steps
@@ -49,7 +67,12 @@ struct CoefSrc<T, true> {
     __device__ __forceinline__ const StepCoef<T>& get() const { return k; }
 };
 
-template <class T, bool BYVAL = false>
+// SCALED (the +-1 storage of Pm1 matrices): the stored matrix is the sign
+// pattern S of A, the scaled matrix is D1 S D2, so the product gathers the
+// pre-scaled vector (D1 y here), the row sum is multiplied by this row's scale
+// (d2_j), and xbar receives the pre-scaled D2 xbar that the dual product
+// gathers (the extrapolated point itself is needed nowhere else).
+template <class T, bool BYVAL = false, bool SCALED = false>
 struct PrimalEpi {
     const T* __restrict__ x;
     const T* __restrict__ c;
@@ -61,25 +84,30 @@ struct PrimalEpi {
     T* __restrict__ xa_new;
     CoefSrc<T, BYVAL> coef;
     int avg;
+    const T* __restrict__ dsc;  // SCALED: d2
     using Acc = NoAcc;
-    struct Pre { T x, c, lv, uv, xa; };
+    struct Pre { T x, c, lv, uv, xa, d; };
     __device__ __forceinline__ Pre pre_global(int j) const {
         return Pre{ld_stream(x + j), ld_stream(c + j), ld_stream(lv + j), ld_stream(uv + j),
-                   avg ? ld_stream(xa_old + j) : T(0)};
+                   avg ? ld_stream(xa_old + j) : T(0), SCALED ? ld_stream(dsc + j) : T(0)};
     }
     __device__ void init(Acc&) {}
     __device__ __forceinline__ void row(int, int j, T s, const Pre& q, Acc&) {
         const StepCoef<T>& k = coef.get();
+        if (SCALED) s = mul_rn(q.d, s);
         const T xp = proj_box(sub_rn(q.x, mul_rn(k.tau, sub_rn(q.c, s))), q.lv, q.uv);
         __stcs(xn + j, xp);
-        xbar[j] = sub_rn(mul_rn(T(2), xp), q.x);
+        const T xb = sub_rn(mul_rn(T(2), xp), q.x);
+        xbar[j] = SCALED ? mul_rn(q.d, xb) : xb;
         if (avg) __stcs(xa_new + j, add_rn(mul_rn(xp, k.a), mul_rn(q.xa, k.b)));
     }
     __device__ void row_long(int p, int j, T s, int, Acc& a) { row(p, j, s, pre_global(j), a); }
     __device__ void finish(Acc&) {}
 };
 
-template <class T, bool BYVAL = false>
+// SCALED: the product gathers D2 xbar, the row sum is multiplied by d1_i, and
+// the epilogue also writes d1 .* y+ for the next primal product
+template <class T, bool BYVAL = false, bool SCALED = false>
 struct DualEpi {
     const T* __restrict__ y;
     const T* __restrict__ lc;
@@ -89,29 +117,34 @@ struct DualEpi {
     T* __restrict__ ya_new;
     CoefSrc<T, BYVAL> coef;
     int avg;
+    const T* __restrict__ dsc;  // SCALED: d1
+    T* __restrict__ ysn;        // SCALED: d1 .* y+
     using Acc = NoAcc;
-    struct Pre { T y, lc, uc, ya; };
+    struct Pre { T y, lc, uc, ya, d; };
     __device__ __forceinline__ Pre pre_global(int i) const {
         return Pre{ld_stream(y + i), ld_stream(lc + i), ld_stream(uc + i),
-                   avg ? ld_stream(ya_old + i) : T(0)};
+                   avg ? ld_stream(ya_old + i) : T(0), SCALED ? ld_stream(dsc + i) : T(0)};
     }
     __device__ void init(Acc&) {}
     __device__ __forceinline__ void row(int, int i, T s, const Pre& q, Acc&) {
         const StepCoef<T>& k = coef.get();
+        if (SCALED) s = mul_rn(q.d, s);
         const T sigma = k.sigma;
         const T t2 = sub_rn(q.y, mul_rn(sigma, s));
         const T t4 = sub_rn(mul_rn(k.inv_sigma, q.y), s);
         const T pr = proj_box(t4, -q.uc, -q.lc);
         const T yp = sub_rn(t2, mul_rn(sigma, pr));
         yn[i] = yp;
+        if (SCALED) ysn[i] = mul_rn(q.d, yp);
         if (avg) __stcs(ya_new + i, add_rn(mul_rn(yp, k.a), mul_rn(q.ya, k.b)));
     }
     __device__ void row_long(int p, int i, T s, int, Acc& a) { row(p, i, s, pre_global(i), a); }
     __device__ void finish(Acc&) {}
 };
 
-// KKT row side (errors.jl:73-80, 87-89): s = (A x_p)_i
-template <class T, int NV>
+// KKT row side (errors.jl:73-80, 87-89): s = (A x_p)_i (SCALED: the product
+// gathered D2 x_p and s is multiplied by d1_i)
+template <class T, int NV, bool SCALED = false>
 struct KktRowEpi {
     const T* __restrict__ lc;
     const T* __restrict__ uc;
@@ -119,6 +152,7 @@ struct KktRowEpi {
     const T* y[NV];
     double* block_out;
     double* long_out;
+    const T* __restrict__ dsc = nullptr;
     struct Acc { double v[2 * NV]; };
     // inputs are read when the row is reduced (no prefetch): four iterates
     // per row would cost too many registers
@@ -129,6 +163,7 @@ struct KktRowEpi {
     }
     __device__ __forceinline__ Pre pre_global(int) const { return Pre{}; }
     __device__ __forceinline__ void terms(int p, int i, T s, double& pr2, double& pc) const {
+        if (SCALED) s = mul_rn(dsc[i], s);
         const double l = (double)lc[i], u = (double)uc[i];
         const double sd = (double)s;
         const double d = __dmul_rn(invD1[i], __dsub_rn(sd, proj_box(sd, l, u)));
@@ -151,8 +186,9 @@ struct KktRowEpi {
     __device__ void finish(Acc& a) { block_reduce_store<2 * NV>(a.v, block_out); }
 };
 
-// KKT column side (errors.jl:74-75, 82-95): s = (A' y_p)_j
-template <class T, int NV>
+// KKT column side (errors.jl:74-75, 82-95): s = (A' y_p)_j (SCALED: the
+// product gathered D1 y_p and s is multiplied by d2_j)
+template <class T, int NV, bool SCALED = false>
 struct KktColEpi {
     const T* __restrict__ c;
     const T* __restrict__ lv;
@@ -161,6 +197,7 @@ struct KktColEpi {
     const T* x[NV];
     double* block_out;
     double* long_out;
+    const T* __restrict__ dsc = nullptr;
     struct Acc { double v[3 * NV]; };
     struct Pre {};
     __device__ void init(Acc& a) {
@@ -170,6 +207,7 @@ struct KktColEpi {
     __device__ __forceinline__ Pre pre_global(int) const { return Pre{}; }
     __device__ __forceinline__ void terms(int p, int j, T s, double& du2, double& pv,
                                           double& cx) const {
+        if (SCALED) s = mul_rn(dsc[j], s);
         const double cj = (double)c[j], l = (double)lv[j], u = (double)uv[j];
         const double g = __dsub_rn(cj, (double)s);
         const double r = proj_multiplier(g, l, u);
@@ -197,22 +235,26 @@ struct KktColEpi {
 };
 
 // power method, second product: Ax_j = (A' s)_j; accumulates x.Ax and Ax.Ax
-template <class T>
+// (SCALED: the product gathered D1 s and Ax_j is the row sum times d2_j)
+template <class T, bool SCALED = false>
 struct PowerEpi {
     const T* __restrict__ x;
     T* __restrict__ out;
     double* block_out;
     double* long_out;
+    const T* __restrict__ dsc = nullptr;
     struct Acc { double v[2]; };
     struct Pre { T x; };
     __device__ Pre pre_global(int j) const { return Pre{ld_stream(x + j)}; }
     __device__ void init(Acc& a) { a.v[0] = a.v[1] = 0.0; }
     __device__ __forceinline__ void row(int, int j, T s, const Pre& q, Acc& a) {
+        if (SCALED) s = mul_rn(dsc[j], s);
         out[j] = s;
         a.v[0] += (double)q.x * (double)s;
         a.v[1] += (double)s * (double)s;
     }
     __device__ void row_long(int, int j, T s, int lid, Acc&) {
+        if (SCALED) s = mul_rn(dsc[j], s);
         out[j] = s;
         long_out[(size_t)lid * 2] = (double)ld_stream(x + j) * (double)s;
         long_out[(size_t)lid * 2 + 1] = (double)s * (double)s;

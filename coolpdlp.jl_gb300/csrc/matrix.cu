@@ -1,6 +1,7 @@
 // matrix.cu -- the pluggable sparse matrix types (src/utils/mat_csr.jl,
 // mat_ell.jl, mat_coo.jl): device builds, export and mul!.
 #include <algorithm>
+#include <cmath>
 #include <memory>
 #include <type_traits>
 
@@ -85,6 +86,19 @@ template <class T>
 __global__ void k_to_f64(const T* __restrict__ in, double* __restrict__ out, int64_t len) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < len) out[i] = (double)in[i];
+}
+// narrow +-1 CSR (CPDLP_VAL_PM1): the stored index is col for +1, ~col for -1
+__global__ void k_pm1_encode(int32_t* __restrict__ idx, const double* __restrict__ v, int64_t nnz) {
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nnz && v[k] < 0.0) idx[k] = ~idx[k];
+}
+__global__ void k_pm1_decode(const int32_t* __restrict__ idx, int64_t* __restrict__ col1,
+                             double* __restrict__ val, int64_t nnz) {
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nnz) return;
+    const int32_t c = idx[k];
+    if (col1) col1[k] = (int64_t)pm1_col(c) + 1;
+    if (val) val[k] = c < 0 ? -1.0 : 1.0;
 }
 
 template <class T>
@@ -219,14 +233,70 @@ void export_T(Handle& h, const Matrix& M, int64_t* ptr, int64_t* idx, double* va
     }
 }
 
+// CPDLP_VAL_PM1: CSR of A with the signs in the column indices, no values
+void build_pm1(Handle& h, Matrix& M, CscPair& S) {
+    cudaStream_t s = h.stream;
+    const int64_t m = M.m, nnz = M.nnz;
+    DBuf<double> v2((size_t)(nnz > 0 ? nnz : 1));
+    gather_values<double, double>(S.val1.p, S.p21.p, v2.p, nnz, s);
+    if (nnz > 0) {
+        k_pm1_encode<<<grid_for(nnz, 256), 256, 0, s>>>(S.idx2.p, v2.p, nnz);
+        CK_LAUNCH();
+    }
+    std::vector<int32_t> hp((size_t)m + 1);
+    CK(cudaMemcpyAsync(hp.data(), S.ptr2.p, sizeof(int32_t) * (m + 1), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    M.ptr = std::move(S.ptr2);
+    M.idx = std::move(S.idx2);
+    build_tile_plan(hp, (int32_t)m, choose_items(nnz, m, 0), M.plan, s);
+    M.part.alloc((size_t)(M.plan.npieces > 0 ? M.plan.npieces : 1) * sizeof(double));
+}
+
+void spmv_pm1(Handle& h, const Matrix& M, const float* b, float* c, double alpha, double beta) {
+    CsrView<Pm1, float> v{M.ptr.p, M.idx.p, nullptr, M.plan.tasks.p, M.plan.ntasks,
+                          M.plan.ltasks.p, M.plan.nltasks, M.plan.counters.p,
+                          reinterpret_cast<float*>(M.part.p)};
+    MulEpi<float> e{c, (float)alpha, (float)beta, beta != 0.0};
+    launch_tiles<1>(M.plan, v, VecSet<float, 1>{{b}}, e, h.stream);
+}
+
+void export_pm1(Handle& h, const Matrix& M, int64_t* ptr, int64_t* idx, double* val) {
+    cudaStream_t s = h.stream;
+    if (ptr && M.m + 1 > 0) {
+        DBuf<int64_t> t((size_t)(M.m + 1));
+        k_to_i64_plus<<<grid_for(M.m + 1, 256), 256, 0, s>>>(M.ptr.p, t.p, M.m + 1, 1);
+        CK_LAUNCH();
+        CK(cudaMemcpyAsync(ptr, t.p, sizeof(int64_t) * (M.m + 1), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+    }
+    if ((idx || val) && M.nnz > 0) {
+        DBuf<int64_t> ti((size_t)M.nnz);
+        DBuf<double> tv((size_t)M.nnz);
+        k_pm1_decode<<<grid_for(M.nnz, 256), 256, 0, s>>>(M.idx.p, idx ? ti.p : nullptr,
+                                                          val ? tv.p : nullptr, M.nnz);
+        CK_LAUNCH();
+        if (idx) CK(cudaMemcpyAsync(idx, ti.p, sizeof(int64_t) * M.nnz, cudaMemcpyDeviceToHost, s));
+        if (val) CK(cudaMemcpyAsync(val, tv.p, sizeof(double) * M.nnz, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+    }
+}
+
 }  // namespace
 
 Matrix* matrix_from_csc(Handle& h, int64_t m, int64_t n, int64_t nnz, const int64_t* colptr,
                         const int64_t* rowval, const double* nzval, int32_t format, int32_t vt) {
     if (format != CPDLP_FMT_CSR && format != CPDLP_FMT_ELL && format != CPDLP_FMT_COO)
         fail(CPDLP_ERR_ARGUMENT, "unknown matrix format");
-    if (vt != CPDLP_VAL_F64 && vt != CPDLP_VAL_F32)
-        fail(CPDLP_ERR_ARGUMENT, "matrix value type must be CPDLP_VAL_F64 or CPDLP_VAL_F32");
+    if (vt != CPDLP_VAL_F64 && vt != CPDLP_VAL_F32 && vt != CPDLP_VAL_PM1)
+        fail(CPDLP_ERR_ARGUMENT, "matrix value type must be CPDLP_VAL_F64, F32 or PM1");
+    if (vt == CPDLP_VAL_PM1) {
+        if (format != CPDLP_FMT_CSR)
+            fail(CPDLP_ERR_UNSUPPORTED, "CPDLP_VAL_PM1 storage is CSR only");
+        if (nnz > 0 && !nzval) fail(CPDLP_ERR_ARGUMENT, "null nzval");
+        for (int64_t k = 0; k < nnz; k++)
+            if (std::fabs(nzval[k]) != 1.0)
+                fail(CPDLP_ERR_ARGUMENT, "CPDLP_VAL_PM1 needs every value to be exactly +1 or -1");
+    }
     auto M = std::make_unique<Matrix>();
     M->h = &h;
     M->format = format;
@@ -235,6 +305,7 @@ Matrix* matrix_from_csc(Handle& h, int64_t m, int64_t n, int64_t nnz, const int6
     CscPair S;
     build_csc_pair(h, m, n, nnz, colptr, rowval, nzval, S);
     if (vt == CPDLP_VAL_F64) build_T<double>(h, *M, S);
+    else if (vt == CPDLP_VAL_PM1) build_pm1(h, *M, S);
     else build_T<float>(h, *M, S);
     return M.release();
 }
@@ -243,12 +314,15 @@ void matrix_spmv(Handle& h, const Matrix& M, const void* b, void* c, double alph
     if ((!b && M.n > 0) || (!c && M.m > 0)) fail(CPDLP_ERR_ARGUMENT, "null vector pointer");
     if (M.vt == CPDLP_VAL_F64)
         spmv_T<double>(h, M, static_cast<const double*>(b), static_cast<double*>(c), alpha, beta);
+    else if (M.vt == CPDLP_VAL_PM1)
+        spmv_pm1(h, M, static_cast<const float*>(b), static_cast<float*>(c), alpha, beta);
     else
         spmv_T<float>(h, M, static_cast<const float*>(b), static_cast<float*>(c), alpha, beta);
 }
 
 void matrix_export(Handle& h, const Matrix& M, int64_t* ptr, int64_t* idx, double* val) {
     if (M.vt == CPDLP_VAL_F64) export_T<double>(h, M, ptr, idx, val);
+    else if (M.vt == CPDLP_VAL_PM1) export_pm1(h, M, ptr, idx, val);
     else export_T<float>(h, M, ptr, idx, val);
 }
 

@@ -131,6 +131,23 @@ __global__ void k_invert_perm(const int32_t* __restrict__ p21, int32_t* __restri
     int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k < nnz) p12[p21[k]] = (int32_t)k;
 }
+// narrow +-1 storage: the index of a -1 entry becomes ~col (sign of v[k])
+__global__ void k_encode_sign(int32_t* __restrict__ idx, const double* __restrict__ v, int64_t nnz) {
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nnz && v[k] < 0.0) idx[k] = ~idx[k];
+}
+template <class T>
+__global__ void k_narrow(const double* __restrict__ v, T* __restrict__ out, int64_t len) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < len) out[i] = (T)v[i];
+}
+// out = a .* b (the pre-scaled copies D2 x, D1 y of a narrow matrix's products)
+template <class T>
+__global__ void k_mul_vec(const T* __restrict__ a, const T* __restrict__ b, T* __restrict__ out,
+                          int64_t len) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < len) out[i] = mul_rn(a[i], b[i]);
+}
 // precondition(milp, prec) on the vectors (preconditioning.jl:61-91)
 template <class T>
 __global__ void k_scale_vec_n(const double* __restrict__ c, const double* __restrict__ lv,
@@ -203,16 +220,20 @@ __global__ void k_power_theta(const double* __restrict__ q, double* __restrict__
         ring[*it % depth].theta = theta;
     }
 }
+// (d2, xs non-null: a narrow matrix, whose first product gathers xs = d2 .* x)
 __global__ void __launch_bounds__(RED_THREADS)
     k_power_residual(double* __restrict__ x, const double* __restrict__ Ax,
-                     const double* __restrict__ scal, int64_t n, double* __restrict__ part) {
+                     const double* __restrict__ scal, int64_t n, double* __restrict__ part,
+                     const double* __restrict__ d2, double* __restrict__ xs) {
     const double theta = scal[0], inv = scal[1];
     double acc[1] = {0.0};
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
         const double r = add_rn(mul_rn(-theta, x[j]), Ax[j]);
         acc[0] += r * r;
-        x[j] = mul_rn(Ax[j], inv);
+        const double xn = mul_rn(Ax[j], inv);
+        x[j] = xn;
+        if (xs) xs[j] = mul_rn(d2[j], xn);
     }
     block_reduce_store<1>(acc, part);
 }
@@ -284,6 +305,17 @@ template <class T>
 CsrView<T, T> view_At(ProblemT<T>& P) {
     return CsrView<T, T>{P.at_ptr.p, P.at_idx.p, P.at_val.p, P.planAt.tasks.p, P.planAt.ntasks,
                          P.planAt.ltasks.p, P.planAt.nltasks, P.planAt.counters.p, P.partAt.p};
+}
+// the same matrices in narrow +-1 storage (signs in the indices, no values)
+template <class T>
+CsrView<Pm1, T> view_A_pm1(ProblemT<T>& P) {
+    return CsrView<Pm1, T>{P.a_ptr.p, P.a_idx.p, nullptr, P.planA.tasks.p, P.planA.ntasks,
+                           P.planA.ltasks.p, P.planA.nltasks, P.planA.counters.p, P.partA.p};
+}
+template <class T>
+CsrView<Pm1, T> view_At_pm1(ProblemT<T>& P) {
+    return CsrView<Pm1, T>{P.at_ptr.p, P.at_idx.p, nullptr, P.planAt.tasks.p, P.planAt.ntasks,
+                           P.planAt.ltasks.p, P.planAt.nltasks, P.planAt.counters.p, P.partAt.p};
 }
 
 // Autotuner of the tile shape (nonzeros per lane) of one CSR matrix: each
@@ -438,12 +470,25 @@ ProblemBase* make_problem(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm
         k_invert_perm<<<gz, 256, 0, s>>>(S.p21.p, p12.p, nnz);
         CK_LAUNCH();
     }
-    P->a_val.alloc(zn + PAD_ELEMS);
-    P->at_val.alloc(zn + PAD_ELEMS);
-    CK(cudaMemsetAsync(P->a_val.p, 0, sizeof(T) * (zn + PAD_ELEMS), s));
-    CK(cudaMemsetAsync(P->at_val.p, 0, sizeof(T) * (zn + PAD_ELEMS), s));
-    gather_values<T, double>(tA.p, S.p21.p, P->a_val.p, nnz, s);
-    gather_values<T, double>(tAt.p, p12.p, P->at_val.p, nnz, s);
+    // narrow +-1 storage: FP32 iterates and every value exactly +-1 (the
+    // products with the sign pattern are exact; D1, D2 are applied per row)
+    bool pm1 = std::is_same<T, float>::value && !(prm->tile_flags & CPDLP_TILE_NO_NARROW) &&
+               nnz > 0;
+    for (int64_t k = 0; pm1 && k < lp->nnz; k++) pm1 = std::fabs(lp->nzval[k]) == 1.0;
+    P->pm1 = pm1;
+    if (pm1) {
+        // rows of A: S2 order, original values vAt; rows of A': S1 order, vA
+        k_encode_sign<<<gz, 256, 0, s>>>(S.idx2.p, vAt.p, nnz);
+        k_encode_sign<<<gz, 256, 0, s>>>(S.idx1.p, vA.p, nnz);
+        CK_LAUNCH();
+    } else {
+        P->a_val.alloc(zn + PAD_ELEMS);
+        P->at_val.alloc(zn + PAD_ELEMS);
+        CK(cudaMemsetAsync(P->a_val.p, 0, sizeof(T) * (zn + PAD_ELEMS), s));
+        CK(cudaMemsetAsync(P->at_val.p, 0, sizeof(T) * (zn + PAD_ELEMS), s));
+        gather_values<T, double>(tA.p, S.p21.p, P->a_val.p, nnz, s);
+        gather_values<T, double>(tAt.p, p12.p, P->at_val.p, nnz, s);
+    }
     P->a_ptr = std::move(S.ptr2);
     P->a_idx = std::move(S.idx2);
     P->at_ptr = std::move(S.ptr1);
@@ -465,6 +510,13 @@ ProblemBase* make_problem(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm
                                         P->invD2.p, n);
     k_scale_vec_m<T><<<gm, 256, 0, s>>>(hlc.p, huc.p, D1.p, P->lc.p, P->uc.p, P->invD1.p, m);
     CK_LAUNCH();
+    if (pm1) {
+        P->d1t.alloc(mz);
+        P->d2t.alloc(nzv);
+        k_narrow<T><<<gm, 256, 0, s>>>(D1.p, P->d1t.p, m);
+        k_narrow<T><<<gn, 256, 0, s>>>(D2.p, P->d2t.p, n);
+        CK_LAUNCH();
+    }
     P->D1 = std::move(D1);
     P->D2 = std::move(D2);
     // tile plans from the row pointers
@@ -475,23 +527,42 @@ ProblemBase* make_problem(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm
     int items_A = choose_items(nnz, m, prm->tile_nnz), items_At = choose_items(nnz, n, prm->tile_nnz);
     if (prm->tile_nnz == 0 && nnz >= AUTOTUNE_MIN_NNZ) {
         // scratch iterates (zeros) for the fused step kernels being timed
-        DBuf<T> vx(nzv), vxn(nzv), vxb(nzv), vxa(nzv), vxa2(nzv), vy(mz), vyn(mz), vya(mz), vya2(mz);
-        for (DBuf<T>* b : {&vx, &vxn, &vxb, &vxa, &vxa2, &vy, &vyn, &vya, &vya2})
+        DBuf<T> vx(nzv), vxn(nzv), vxb(nzv), vxa(nzv), vxa2(nzv), vy(mz), vyn(mz), vya(mz),
+            vya2(mz), vys(pm1 ? mz : 1);
+        for (DBuf<T>* b : {&vx, &vxn, &vxb, &vxa, &vxa2, &vy, &vyn, &vya, &vya2, &vys})
             CK(cudaMemsetAsync(b->p, 0, sizeof(T) * b->n, s));
         DBuf<StepCoef<T>> cf(1);
         CK(cudaMemsetAsync(cf.p, 0, sizeof(StepCoef<T>), s));
         ProblemT<T>* Q = P;
-        items_At = tune_items<T>(h, hp1, (int32_t)n, m, nnz, items_At, 1, [&](TilePlan& pl, T* part) {
-            const CsrView<T, T> V{Q->at_ptr.p, Q->at_idx.p, Q->at_val.p, pl.tasks.p, pl.ntasks,
-                                  pl.ltasks.p, pl.nltasks, pl.counters.p, part};
-            PrimalEpi<T> pe{vx.p, Q->c.p, Q->lv.p, Q->uv.p, vxn.p, vxb.p, vxa.p, vxa2.p, {cf.p}, 1};
-            launch_tiles<1>(pl, V, VecSet<T, 1>{{vy.p}}, pe, s);
+        items_At = tune_items<T>(h, hp1, (int32_t)n, m, nnz, items_At, pm1 ? 3 : 1,
+                                 [&](TilePlan& pl, T* part) {
+            if (pm1) {
+                const CsrView<Pm1, T> V{Q->at_ptr.p, Q->at_idx.p, nullptr, pl.tasks.p, pl.ntasks,
+                                        pl.ltasks.p, pl.nltasks, pl.counters.p, part};
+                PrimalEpi<T, false, true> pe{vx.p, Q->c.p, Q->lv.p, Q->uv.p, vxn.p, vxb.p,
+                                             vxa.p, vxa2.p, {cf.p}, 1, Q->d2t.p};
+                launch_tiles<1>(pl, V, VecSet<T, 1>{{vy.p}}, pe, s);
+            } else {
+                const CsrView<T, T> V{Q->at_ptr.p, Q->at_idx.p, Q->at_val.p, pl.tasks.p, pl.ntasks,
+                                      pl.ltasks.p, pl.nltasks, pl.counters.p, part};
+                PrimalEpi<T> pe{vx.p, Q->c.p, Q->lv.p, Q->uv.p, vxn.p, vxb.p, vxa.p, vxa2.p, {cf.p}, 1};
+                launch_tiles<1>(pl, V, VecSet<T, 1>{{vy.p}}, pe, s);
+            }
         });
-        items_A = tune_items<T>(h, hp2, (int32_t)m, n, nnz, items_A, 0, [&](TilePlan& pl, T* part) {
-            const CsrView<T, T> V{Q->a_ptr.p, Q->a_idx.p, Q->a_val.p, pl.tasks.p, pl.ntasks,
-                                  pl.ltasks.p, pl.nltasks, pl.counters.p, part};
-            DualEpi<T> de{vy.p, Q->lc.p, Q->uc.p, vyn.p, vya.p, vya2.p, {cf.p}, 1};
-            launch_tiles<1>(pl, V, VecSet<T, 1>{{vxb.p}}, de, s);
+        items_A = tune_items<T>(h, hp2, (int32_t)m, n, nnz, items_A, pm1 ? 2 : 0,
+                                [&](TilePlan& pl, T* part) {
+            if (pm1) {
+                const CsrView<Pm1, T> V{Q->a_ptr.p, Q->a_idx.p, nullptr, pl.tasks.p, pl.ntasks,
+                                        pl.ltasks.p, pl.nltasks, pl.counters.p, part};
+                DualEpi<T, false, true> de{vy.p, Q->lc.p, Q->uc.p, vyn.p, vya.p, vya2.p, {cf.p}, 1,
+                                           Q->d1t.p, vys.p};
+                launch_tiles<1>(pl, V, VecSet<T, 1>{{vxb.p}}, de, s);
+            } else {
+                const CsrView<T, T> V{Q->a_ptr.p, Q->a_idx.p, Q->a_val.p, pl.tasks.p, pl.ntasks,
+                                      pl.ltasks.p, pl.nltasks, pl.counters.p, part};
+                DualEpi<T> de{vy.p, Q->lc.p, Q->uc.p, vyn.p, vya.p, vya2.p, {cf.p}, 1};
+                launch_tiles<1>(pl, V, VecSet<T, 1>{{vxb.p}}, de, s);
+            }
         });
     }
     build_tile_plan(hp2, (int32_t)m, items_A, P->planA, s);
@@ -580,6 +651,19 @@ double spectral_norm_T(Handle& h, ProblemT<V>& P, const cpdlp_params* prm, int64
     const CsrView<V, double> At{P.at_ptr.p, P.at_idx.p, P.at_val.p, P.planAt.tasks.p,
                                 P.planAt.ntasks, P.planAt.ltasks.p, P.planAt.nltasks,
                                 P.planAt.counters.p, pAt.p};
+    // narrow +-1 storage: A = D1 S D2; the first product gathers xs = D2 x and
+    // stores D1 (A x) = D1 D1 (S xs), the second multiplies S' (D1 A x) by D2
+    const CsrView<Pm1, double> A1{P.a_ptr.p, P.a_idx.p, nullptr, P.planA.tasks.p,
+                                  P.planA.ntasks, P.planA.ltasks.p, P.planA.nltasks,
+                                  P.planA.counters.p, pA.p};
+    const CsrView<Pm1, double> At1{P.at_ptr.p, P.at_idx.p, nullptr, P.planAt.tasks.p,
+                                   P.planAt.ntasks, P.planAt.ltasks.p, P.planAt.nltasks,
+                                   P.planAt.counters.p, pAt.p};
+    DBuf<double> xs((size_t)(P.pm1 && n > 0 ? n : 1));
+    if (P.pm1 && n > 0) {
+        k_mul_vec<double><<<grid_for(n, 256), 256, 0, s>>>(x.p, P.D2.p, xs.p, n);
+        CK_LAUNCH();
+    }
     constexpr int DEPTH = 8;  // iterations queued ahead of the host's stopping check
     void* block = h.host_get(sizeof(PowerSlot) * DEPTH);
     PowerSlot* ring = static_cast<PowerSlot*>(block);
@@ -602,12 +686,23 @@ double spectral_norm_T(Handle& h, ProblemT<V>& P, const cpdlp_params* prm, int64
     {
         cudaGraph_t g = nullptr;
         CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        launch_tiles<1>(P.planA, A, VecSet<double, 1>{{x.p}}, StoreEpi<double>{sv.p}, s);
-        PowerEpi<double> pe{x.p, Ax.p, P.red_cols.p, P.red_cols.p + (size_t)tiles_grid(P.planAt) * 2};
-        launch_tiles<1>(P.planAt, At, VecSet<double, 1>{{sv.p}}, pe, s);
+        double* const blk = P.red_cols.p;
+        double* const lng = P.red_cols.p + (size_t)tiles_grid(P.planAt) * 2;
+        if (P.pm1) {
+            launch_tiles<1>(P.planA, A1, VecSet<double, 1>{{xs.p}},
+                            ScaledStoreEpi<double>{sv.p, P.D1.p}, s);
+            PowerEpi<double, true> pe{x.p, Ax.p, blk, lng, P.D2.p};
+            launch_tiles<1>(P.planAt, At1, VecSet<double, 1>{{sv.p}}, pe, s);
+        } else {
+            launch_tiles<1>(P.planA, A, VecSet<double, 1>{{x.p}}, StoreEpi<double>{sv.p}, s);
+            PowerEpi<double> pe{x.p, Ax.p, blk, lng};
+            launch_tiles<1>(P.planAt, At, VecSet<double, 1>{{sv.p}}, pe, s);
+        }
         reduce_partials(P.red_cols.p, P.rows_At_partials, 2, P.red_out.p, s);
         k_power_theta<<<1, 32, 0, s>>>(P.red_out.p, scal.p, d_it.p, dring, DEPTH);
-        k_power_residual<<<gr, RED_THREADS, 0, s>>>(x.p, Ax.p, scal.p, n, P.red_rows.p);
+        k_power_residual<<<gr, RED_THREADS, 0, s>>>(x.p, Ax.p, scal.p, n, P.red_rows.p,
+                                                    P.pm1 ? P.D2.p : nullptr,
+                                                    P.pm1 ? xs.p : nullptr);
         reduce_partials(P.red_rows.p, gr, 1, P.red_out.p + 2, s);
         k_power_finish<<<1, 32, 0, s>>>(P.red_out.p + 2, d_it.p, dring, DEPTH);
         const cudaError_t launch_err = cudaGetLastError();
@@ -646,6 +741,10 @@ struct StateT : StateBase {
     Handle* h = nullptr;
     DBuf<T> x[2], y[2], xa[2], ya[2], xr, yr, xbar;
     int cur = 0;  // sol = (x[cur], y[cur]); sol_last = (x[cur^1], y[cur^1]); same for averages
+    // narrow +-1 storage: ys[b] = D1 .* y[b] (the primal product's gather; the
+    // dual step writes it beside y), xbar holds D2 .* xbar, and the KKT
+    // products gather the scratch copies kx = D2 .* x, ky = D1 .* y
+    DBuf<T> ys[2], kx[4], ky[4];
     DBuf<StepCoef<T>> coef, coef1;
     std::vector<StepCoef<T>> coef_host;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
@@ -670,15 +769,41 @@ struct StateT : StateBase {
         return k;
     }
 
+    // primal step: x+ = proj(x - tau (c - A'y)), xbar, the running average
+    // (narrow storage: gathers yg = D1 y, and xb receives D2 xbar)
+    void launch_primal(const T* xo, T* xn, T* xb, const T* xao, T* xan, const T* yg,
+                       const StepCoef<T>* c, cudaStream_t s) {
+        ProblemT<T>& P = *PT;
+        const int avg = pdlp() ? 1 : 0;
+        if (P.pm1) {
+            PrimalEpi<T, false, true> pe{xo, P.c.p, P.lv.p, P.uv.p, xn, xb, xao, xan, {c}, avg,
+                                         P.d2t.p};
+            launch_tiles<1>(P.planAt, view_At_pm1(P), VecSet<T, 1>{{yg}}, pe, s);
+        } else {
+            PrimalEpi<T> pe{xo, P.c.p, P.lv.p, P.uv.p, xn, xb, xao, xan, {c}, avg};
+            launch_tiles<1>(P.planAt, view_At(P), VecSet<T, 1>{{yg}}, pe, s);
+        }
+    }
+    // dual step: y+ from A xbar (narrow storage: also writes ysn = D1 y+)
+    void launch_dual(const T* yo, T* yn, T* ysn, const T* yao, T* yan, const T* xg,
+                     const StepCoef<T>* c, cudaStream_t s) {
+        ProblemT<T>& P = *PT;
+        const int avg = pdlp() ? 1 : 0;
+        if (P.pm1) {
+            DualEpi<T, false, true> de{yo, P.lc.p, P.uc.p, yn, yao, yan, {c}, avg, P.d1t.p, ysn};
+            launch_tiles<1>(P.planA, view_A_pm1(P), VecSet<T, 1>{{xg}}, de, s);
+        } else {
+            DualEpi<T> de{yo, P.lc.p, P.uc.p, yn, yao, yan, {c}, avg};
+            launch_tiles<1>(P.planA, view_A(P), VecSet<T, 1>{{xg}}, de, s);
+        }
+    }
+
     // One step!: kernels only.  `c` points at this step's coefficients.
     void enqueue_step(int parity_in, const StepCoef<T>* c, cudaStream_t s) {
-        ProblemT<T>& P = *PT;
+        const bool pm = PT->pm1;
         const int o = parity_in, nw = parity_in ^ 1;  // read old, write new
-        PrimalEpi<T> pe{x[o].p, P.c.p, P.lv.p, P.uv.p, x[nw].p, xbar.p, xa[o].p, xa[nw].p, c,
-                        pdlp() ? 1 : 0};
-        launch_tiles<1>(P.planAt, view_At(P), VecSet<T, 1>{{y[o].p}}, pe, s);
-        DualEpi<T> de{y[o].p, P.lc.p, P.uc.p, y[nw].p, ya[o].p, ya[nw].p, c, pdlp() ? 1 : 0};
-        launch_tiles<1>(P.planA, view_A(P), VecSet<T, 1>{{xbar.p}}, de, s);
+        launch_primal(x[o].p, x[nw].p, xbar.p, xa[o].p, xa[nw].p, pm ? ys[o].p : y[o].p, c, s);
+        launch_dual(y[o].p, y[nw].p, pm ? ys[nw].p : nullptr, ya[o].p, ya[nw].p, xbar.p, c, s);
     }
 
     void advance_counters(int64_t k) {
@@ -760,19 +885,36 @@ struct StateT : StateBase {
     void enqueue_kkt_pair(int p, const T* xp, const T* yp) {
         ProblemT<T>& P = *PT;
         cudaStream_t s = h->stream;
+        if (P.pm1) {
+            if (P.n > 0) k_mul_vec<T><<<grid_for(P.n, 256), 256, 0, s>>>(xp, P.d2t.p, kx[p].p, P.n);
+            if (P.m > 0) k_mul_vec<T><<<grid_for(P.m, 256), 256, 0, s>>>(yp, P.d1t.p, ky[p].p, P.m);
+            CK_LAUNCH();
+            kkt_pair_impl<true>(p, xp, yp, kx[p].p, ky[p].p, view_A_pm1(P), view_At_pm1(P), s);
+        } else {
+            kkt_pair_impl<false>(p, xp, yp, xp, yp, view_A(P), view_At(P), s);
+        }
+    }
+    // gx / gy: the vectors the two products gather (x, y, or their D2 / D1
+    // pre-scaled copies for a narrow matrix)
+    template <bool SC, class VA, class VAt>
+    void kkt_pair_impl(int p, const T* xp, const T* yp, const T* gx, const T* gy, const VA& vA,
+                       const VAt& vAt, cudaStream_t s) {
+        ProblemT<T>& P = *PT;
         const unsigned gA = tiles_grid(P.planA), gAt = tiles_grid(P.planAt);
-        KktRowEpi<T, 1> re;
+        KktRowEpi<T, 1, SC> re;
         re.lc = P.lc.p; re.uc = P.uc.p; re.invD1 = P.invD1.p;
         re.y[0] = yp;
         re.block_out = P.red_rows.p + (size_t)p * P.rows_A_partials * 2;
         re.long_out = re.block_out + (size_t)gA * 2;
-        launch_tiles<1>(P.planA, view_A(P), VecSet<T, 1>{{xp}}, re, s);
-        KktColEpi<T, 1> ce;
+        re.dsc = SC ? P.d1t.p : nullptr;
+        launch_tiles<1>(P.planA, vA, VecSet<T, 1>{{gx}}, re, s);
+        KktColEpi<T, 1, SC> ce;
         ce.c = P.c.p; ce.lv = P.lv.p; ce.uv = P.uv.p; ce.invD2 = P.invD2.p;
         ce.x[0] = xp;
         ce.block_out = P.red_cols.p + (size_t)p * P.rows_At_partials * 3;
         ce.long_out = ce.block_out + (size_t)gAt * 3;
-        launch_tiles<1>(P.planAt, view_At(P), VecSet<T, 1>{{yp}}, ce, s);
+        ce.dsc = SC ? P.d2t.p : nullptr;
+        launch_tiles<1>(P.planAt, vAt, VecSet<T, 1>{{gy}}, ce, s);
     }
 
     template <int NV>
@@ -782,7 +924,8 @@ struct StateT : StateBase {
         for (int p = 0; p < NV; p++) enqueue_kkt_pair(p, xs[p], ys[p]);
         reduce_partials(P.red_rows.p, P.rows_A_partials, 2, P.red_out.p, s, NV);
         reduce_partials(P.red_cols.p, P.rows_At_partials, 3, P.red_out.p + 2 * NV, s, NV);
-        launches += NV * (tiles_launches(P.planA) + tiles_launches(P.planAt)) + 2;
+        launches += NV * (tiles_launches(P.planA) + tiles_launches(P.planAt)) + 2 +
+                    (P.pm1 ? NV * ((P.n > 0) + (P.m > 0)) : 0);
         double* pin = h->pinned_area(sizeof(double) * 64);
         CK(cudaMemcpyAsync(pin, P.red_out.p, sizeof(double) * 5 * NV, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
@@ -893,6 +1036,11 @@ struct StateT : StateBase {
         if (restart_from_avg) {
             CK(cudaMemcpyAsync(x[cur].p, xa[cur].p, sizeof(T) * P.n, cudaMemcpyDeviceToDevice, s));
             CK(cudaMemcpyAsync(y[cur].p, ya[cur].p, sizeof(T) * P.m, cudaMemcpyDeviceToDevice, s));
+            if (P.pm1 && P.m > 0) {
+                k_mul_vec<T><<<grid_for(P.m, 256), 256, 0, s>>>(y[cur].p, P.d1t.p, ys[cur].p, P.m);
+                CK_LAUNCH();
+                launches += 1;
+            }
         }
         CK(cudaMemsetAsync(xa[cur].p, 0, sizeof(T) * P.n, s));
         CK(cudaMemsetAsync(ya[cur].p, 0, sizeof(T) * P.m, s));
@@ -944,7 +1092,7 @@ struct StateT : StateBase {
         ProblemT<T>& P = *PT;
         cudaStream_t s = h->stream;
         const size_t nz = (size_t)std::max<int64_t>(P.n, 1), mz = (size_t)std::max<int64_t>(P.m, 1);
-        DBuf<T> tx(nz), tb(nz), txa(nz), ty(mz), tya(mz);
+        DBuf<T> tx(nz), tb(nz), txa(nz), ty(mz), tya(mz), tys(P.pm1 ? mz : 1);
         if (!coef1.p) coef1.alloc(1);
         StepCoef<T> k = coef_for(eta_sum);
         CK(cudaMemcpyAsync(coef1.p, &k, sizeof(k), cudaMemcpyHostToDevice, s));
@@ -963,13 +1111,10 @@ struct StateT : StateBase {
             return (double)t / reps;
         };
         ms[0] = timed([&] {
-            PrimalEpi<T> pe{x[o].p, P.c.p, P.lv.p, P.uv.p, tx.p, tb.p, xa[o].p, txa.p, coef1.p,
-                            pdlp() ? 1 : 0};
-            launch_tiles<1>(P.planAt, view_At(P), VecSet<T, 1>{{y[o].p}}, pe, s);
+            launch_primal(x[o].p, tx.p, tb.p, xa[o].p, txa.p, P.pm1 ? ys[o].p : y[o].p, coef1.p, s);
         });
         ms[1] = timed([&] {
-            DualEpi<T> de{y[o].p, P.lc.p, P.uc.p, ty.p, ya[o].p, tya.p, coef1.p, pdlp() ? 1 : 0};
-            launch_tiles<1>(P.planA, view_A(P), VecSet<T, 1>{{xbar.p}}, de, s);
+            launch_dual(y[o].p, ty.p, P.pm1 ? tys.p : nullptr, ya[o].p, tya.p, xbar.p, coef1.p, s);
         });
         ms[2] = timed([&] {
             enqueue_kkt_pair(0, x[cur].p, y[cur].p);
@@ -984,18 +1129,24 @@ struct StateT : StateBase {
     void kernel_bytes(double* bytes) const override {
         const ProblemT<T>& P = *PT;
         const double nnz = (double)P.nnz, m = (double)P.m, n = (double)P.n;
-        const double sv = sizeof(T), si = sizeof(int32_t), sf = sizeof(T);
+        const double sv = P.pm1 ? 0.0 : sizeof(T), si = sizeof(int32_t), sf = sizeof(T);
         const bool avg = prm.algorithm == CPDLP_ALGO_PDLP;
         // primal: A' values+indices, row pointer, gather y (m), read x c lv uv,
-        // write x+ xbar (+ avg read/write)
-        bytes[0] = nnz * (sv + si) + (n + 1) * si + sf * (m + (avg ? 8 : 6) * n);
+        // write x+ xbar (+ avg read/write); narrow: no values, read d2
+        bytes[0] = nnz * (sv + si) + (n + 1) * si + sf * (m + (avg ? 8 : 6) * n) +
+                   (P.pm1 ? sf * n : 0.0);
         // dual: A values+indices, row pointer, gather xbar (n), read y lc uc,
-        // write y+ (+ avg read/write)
-        bytes[1] = nnz * (sv + si) + (m + 1) * si + sf * (n + (avg ? 6 : 4) * m);
-        // KKT of 4 pairs: both matrices once, 4 gathered vectors per side,
-        // bounds, the 4 epilogue vectors per side, D1/D2 inverses (FP64)
+        // write y+ (+ avg read/write); narrow: no values, read d1, write D1 y+
+        bytes[1] = nnz * (sv + si) + (m + 1) * si + sf * (n + (avg ? 6 : 4) * m) +
+                   (P.pm1 ? 2 * sf * m : 0.0);
+        // KKT of 4 pairs: both matrices once (the minimum; the kernels read
+        // them once per pair), 4 gathered vectors per side, bounds, the 4
+        // epilogue vectors per side, D1/D2 inverses (FP64); narrow: the scale
+        // reads per pair and the pre-scaling passes (read x, d2, write D2 x;
+        // the same for y)
         bytes[2] = 2 * nnz * (sv + si) + (m + n + 2) * si + sf * (4 * n + 4 * m) +
-                   sf * (2 * m + 4 * m) + sf * (3 * n + 4 * n) + 8.0 * (m + n);
+                   sf * (2 * m + 4 * m) + sf * (3 * n + 4 * n) + 8.0 * (m + n) +
+                   (P.pm1 ? sf * (4 * (m + n) + 12 * (m + n)) : 0.0);
     }
 
     void early_exit_zero_problem() override {
@@ -1077,6 +1228,18 @@ StateBase* make_state(Handle& h, ProblemT<T>* P, const cpdlp_params* prm, const 
     CK(cudaMemcpyAsync(S->xr.p, S->x[0].p, sizeof(T) * nz, cudaMemcpyDeviceToDevice, s));
     CK(cudaMemcpyAsync(S->yr.p, S->y[0].p, sizeof(T) * mz, cudaMemcpyDeviceToDevice, s));
     CK(cudaMemsetAsync(S->xbar.p, 0, sizeof(T) * nz, s));
+    if (P->pm1) {
+        for (int b = 0; b < 2; b++) S->ys[b].alloc(mz);
+        for (int q = 0; q < 4; q++) {
+            S->kx[q].alloc(nz);
+            S->ky[q].alloc(mz);
+        }
+        CK(cudaMemsetAsync(S->ys[1].p, 0, sizeof(T) * mz, s));
+        if (m > 0) {
+            k_mul_vec<T><<<grid_for(m, 256), 256, 0, s>>>(S->y[0].p, P->d1t.p, S->ys[0].p, m);
+            CK_LAUNCH();
+        }
+    }
     S->cur = 0;
     // fixed_stepsize (step_size.jl:22-27)
     if (eta0 > 0) {  // continuation of an earlier solve of the same LP

@@ -46,6 +46,10 @@ struct ProblemT : ProblemBase {
     DBuf<T> a_val, at_val;
     DBuf<T> c, lv, uv, lc, uc;
     DBuf<T> partA, partAt;   // long-row piece partials, NVEC = 4
+    // narrow +-1 storage: the index arrays carry the signs of A (Pm1), the
+    // value arrays are empty, and the products apply d1 / d2 (as T)
+    bool pm1 = false;
+    DBuf<T> d1t, d2t;
 };
 
 struct StateBase {

@@ -23,6 +23,8 @@
 // the aligned 128-bit window may read up to 3 elements past the last row.
 #pragma once
 
+#include <type_traits>
+
 #include "cpdlp_common.cuh"
 
 namespace cpdlp {
@@ -75,6 +77,18 @@ struct CsrView {
     int32_t* counters;
     T* partials;   // npieces * NVEC
 };
+
+// Matrices whose values are all exactly +-1 store no value array: the sign is
+// carried by the column index (col for +1, ~col for -1), so a nonzero costs 4
+// bytes instead of 8 or 12.  Products with +-1 are exact.
+struct Pm1 {};
+template <class V>
+struct is_pm1 : std::false_type {};
+template <>
+struct is_pm1<Pm1> : std::true_type {};
+__host__ __device__ __forceinline__ int pm1_col(int c) { return c ^ (c >> 31); }
+template <class T>
+__device__ __forceinline__ T pm1_apply(int c, T x) { return c < 0 ? -x : x; }
 
 // The input vectors of one product.  COH = false gathers them through the
 // non-coherent read-only path, valid when nothing in the same launch writes
@@ -192,7 +206,8 @@ __device__ __forceinline__ void short_tile(const CsrView<V, T>& A, const VecSet<
         const int e = base + 4 * (lane + 32 * j);
         if (e < nz1) {
             load4(A.idx + e, cc[j]);
-            load4v<T>(A.val + e, vv[j]);
+            if constexpr (!is_pm1<V>::value) load4v<T>(A.val + e, vv[j]);
+            else vv[j][0] = vv[j][1] = vv[j][2] = vv[j][3] = T(0);
         } else {
 #pragma unroll
             for (int q = 0; q < 4; q++) { cc[j][q] = 0; vv[j][q] = T(0); }
@@ -208,15 +223,18 @@ __device__ __forceinline__ void short_tile(const CsrView<V, T>& A, const VecSet<
             const int e = base + 4 * (lane + 32 * j);
 #pragma unroll
             for (int q = 0; q < 4; q++)
-                xg[j][q] = (e + q >= nz0 && e + q < nz1) ? gather<COH>(xs.v[p] + cc[j][q])
-                                                         : T(0);
+                xg[j][q] = (e + q >= nz0 && e + q < nz1)
+                               ? gather<COH>(xs.v[p] + (is_pm1<V>::value ? pm1_col(cc[j][q]) : cc[j][q]))
+                               : T(0);
         }
 #pragma unroll
         for (int j = 0; j < NV4; j++) {
             const int e = base + 4 * (lane + 32 * j);
 #pragma unroll
             for (int q = 0; q < 4; q++)
-                if (e + q >= nz0 && e + q < nz1) prod[e + q - nz0] = mul_rn(vv[j][q], xg[j][q]);
+                if (e + q >= nz0 && e + q < nz1)
+                    prod[e + q - nz0] = is_pm1<V>::value ? pm1_apply(cc[j][q], xg[j][q])
+                                                         : mul_rn(vv[j][q], xg[j][q]);
         }
         __syncwarp();
 #pragma unroll
@@ -250,10 +268,16 @@ __device__ __forceinline__ void long_piece(const CsrView<V, T>& A, const VecSet<
 #pragma unroll
     for (int p = 0; p < NVEC; p++) s[p] = T(0);
     for (int e = a + lane; e < b; e += 32) {
-        const T vv = load1v<V, T>(A.val + e);
         const int cc = __ldcs(A.idx + e);
+        if constexpr (is_pm1<V>::value) {
 #pragma unroll
-        for (int p = 0; p < NVEC; p++) s[p] = add_rn(s[p], mul_rn(vv, gather<COH>(xs.v[p] + cc)));
+            for (int p = 0; p < NVEC; p++)
+                s[p] = add_rn(s[p], pm1_apply(cc, gather<COH>(xs.v[p] + pm1_col(cc))));
+        } else {
+            const T vv = load1v<V, T>(A.val + e);
+#pragma unroll
+            for (int p = 0; p < NVEC; p++) s[p] = add_rn(s[p], mul_rn(vv, gather<COH>(xs.v[p] + cc)));
+        }
     }
 #pragma unroll
     for (int p = 0; p < NVEC; p++) s[p] = warp_sum_tree(s[p]);

@@ -58,7 +58,8 @@ enum {
 enum { CPDLP_ALGO_PDLP = 0, CPDLP_ALGO_PDHG = 1 };
 
 /* float_type of ConversionParameters (src/components/conversion.jl:14-30).
- * CPDLP_VAL_PM1 stores matrix values of exactly +-1 as one signed byte. */
+ * CPDLP_VAL_PM1 (matrices only): values that are all exactly +-1, stored as
+ * the signs of the column indices (no value array, FP32 vectors, CSR). */
 enum { CPDLP_VAL_F64 = 0, CPDLP_VAL_F32 = 1, CPDLP_VAL_PM1 = 2 };
 
 /* matrix_type: GPUSparseMatrixCSR / ELL / COO (src/utils/mat_*.jl) */
@@ -126,9 +127,16 @@ typedef struct cpdlp_params {
     double refine_reltol;
     /* EXT: CSR tile size in nonzeros for the SpMV work partition (0 = autotune). */
     int32_t tile_nnz;
-    /* EXT: reserved for autotuner flags; must be 0. */
+    /* EXT: storage flags (CPDLP_TILE_*); 0 = defaults. */
     int32_t tile_flags;
 } cpdlp_params;
+
+/* tile_flags bits.  By default a single-LP solve with FP32 iterates whose
+ * matrix values are all exactly +-1 stores the matrix narrow: the signs ride
+ * in the column indices (4 bytes per nonzero, no value array) and the kernels
+ * apply the diagonal scalings D1, D2 themselves.  CPDLP_TILE_NO_NARROW keeps
+ * the scaled values instead. */
+enum { CPDLP_TILE_NO_NARROW = 1 };
 
 /* An LP in the reference's "cuPDLPx form" (src/problems/milp.jl:1-20):
  *   min c'x  s.t.  lv <= x <= uv,  lc <= A x <= uc
@@ -197,7 +205,9 @@ void* cpdlp_stream(cpdlp_handle* h);
 /* M(::SparseMatrixCSC): GPUSparseMatrixCSR (mat_csr.jl:58-61),
  * GPUSparseMatrixELL (mat_ell.jl:54-70), GPUSparseMatrixCOO (mat_coo.jl:50-53).
  * The format is built on the device from the 1-based CSC arrays.
- * value_type: CPDLP_VAL_F64 or CPDLP_VAL_F32 (the matrix eltype T). */
+ * value_type: CPDLP_VAL_F64 or CPDLP_VAL_F32 (the matrix eltype T), or
+ * CPDLP_VAL_PM1 (CSR only, every value exactly +-1, Float32 vectors; the
+ * export decodes the signs back into nzval). */
 int cpdlp_matrix_from_csc(cpdlp_handle* h, int64_t m, int64_t n, int64_t nnz,
                           const int64_t* colptr, const int64_t* rowval,
                           const double* nzval, int32_t format, int32_t value_type,
