@@ -193,7 +193,8 @@ def _stats_from(st, hist, starting_time) -> ConvergenceStats:
         kkt_passes=st.kkt_passes, termination_status=TerminationStatus(st.termination_status),
         error_history=[(p, KKTErrors.from_c(e)) for p, e in hist], outer=st.outer,
         inner=st.inner, total=st.total, eta=st.eta, omega=st.omega,
-        power_iterations=st.power_iterations, setup_seconds=st.setup_seconds)
+        power_iterations=st.power_iterations, setup_seconds=st.setup_seconds,
+        refine_kkt_passes=st.refine_kkt_passes)
 
 
 def preprocess(milp: MILP, sol: PrimalDualSolution, algo: Algorithm):
@@ -243,50 +244,19 @@ def solve(milp: MILP, *args):
                              milp.c, milp.lv, milp.uv, milp.lc, milp.uc)
         x, y, st = native.solve_lp(handle, lp, algo.params, sol.x, sol.y)
         return PrimalDualSolution(x, y), _stats_from(st, [], t0)
+    p = algo.params
+    if p.float_type == A.VAL_F32 and p.refine_reltol > 0:
+        # mixed precision (FP32 phase, then refinement rounds on the residual
+        # LP with FP64 residuals and KKT errors) runs inside cpdlp_solve
+        handle = native.default_handle(algo.device)
+        lp = native.LPStruct(milp.A.m, milp.A.n, milp.A.colptr, milp.A.rowval, milp.A.nzval,
+                             milp.c, milp.lv, milp.uv, milp.lc, milp.uc)
+        x, y, st = native.solve_lp(handle, lp, p, sol.x, sol.y)
+        return PrimalDualSolution(x, y), _stats_from(st, [], t0)
     dmilp, sol = preprocess(milp, sol, algo)
     state = initialize(dmilp, sol, algo, starting_time=t0)
-    p = algo.params
-    mixed = p.float_type == A.VAL_F32 and p.refine_reltol > 0
-    stalled = False
-    if mixed:
-        # FP32 phase one check at a time: iterates whose relative KKT error has
-        # not halved over STALL_CHECKS checks continue in FP64 (as cpdlp_solve)
-        best, mark = math.inf, 0
-        while True:
-            s_now = state.native.solve_blocks(1)
-            if s_now.termination_status != A.STILL_RUNNING:
-                break
-            rel = relative(KKTErrors.from_c(s_now.err))
-            if rel < 0.5 * best:
-                best, mark = rel, s_now.kkt_passes
-            elif s_now.kkt_passes - mark >= STALL_CHECKS * p.check_every:
-                stalled = True
-                break
-    else:
-        solve_inplace(state)
-    stats = state.stats()
-    sol_out = state.solution()
-    if mixed and ((stats.termination_status == OPTIMAL
-                   and p.refine_reltol < p.termination_reltol) or stalled):
-        # FP64 phase: continue from the FP32 solution in Float64 until
-        # refine_reltol (same scaling, recomputed in FP64)
-        kw = algo.kwargs()
-        kw.update(termination_reltol=p.refine_reltol,
-                  max_kkt_passes=max(p.max_kkt_passes - stats.kkt_passes, 1),
-                  time_limit=p.time_limit - (time.time() - t0), refine_reltol=0.0)
-        algo64 = Algorithm(algo.name, np.float64, algo.Ti, algo.M, device=algo.device, **kw)
-        dm64, _ = preprocess(milp, sol_out, algo64)
-        st64 = initialize(dm64, sol_out, algo64, starting_time=t0)
-        solve_inplace(st64)
-        s64 = st64.stats()
-        hist = stats.error_history + [(stats.kkt_passes + k, e) for k, e in s64.error_history]
-        passes32, passes64 = stats.kkt_passes, s64.kkt_passes
-        stats = s64
-        stats.error_history = hist
-        stats.kkt_passes = passes32 + passes64
-        stats.refine_kkt_passes = passes64
-        sol_out = st64.solution()
-    return sol_out, stats
+    solve_inplace(state)
+    return state.solution(), state.stats()
 
 
 def nbcons_zero_cost(milp: MILP) -> bool:

@@ -106,8 +106,14 @@ struct PrimalEpi {
 };
 
 // SCALED: the product gathers D2 xbar, the row sum is multiplied by d1_i, and
-// the epilogue also writes d1 .* y+ for the next primal product
-template <class T, bool BYVAL = false, bool SCALED = false>
+// the epilogue also writes d1 .* y+ for the next primal product.
+// SHIFT (a refinement round on the residual LP, whose multipliers are the
+// corrections dy to base multipliers y0): the projection that decides each
+// row's activity sees the whole multiplier, (yoff_i + dy_i)/sigma - s, with
+// yoff the scaled base multipliers; the rest of the step acts on dy.  yoff is
+// FP64 and so is this row's arithmetic: yoff can exceed dy by many orders of
+// magnitude, and the activity decision needs dy's precision.
+template <class T, bool BYVAL = false, bool SCALED = false, bool SHIFT = false>
 struct DualEpi {
     const T* __restrict__ y;
     const T* __restrict__ lc;
@@ -117,23 +123,33 @@ struct DualEpi {
     T* __restrict__ ya_new;
     CoefSrc<T, BYVAL> coef;
     int avg;
-    const T* __restrict__ dsc;  // SCALED: d1
-    T* __restrict__ ysn;        // SCALED: d1 .* y+
+    const T* __restrict__ dsc;   // SCALED: d1
+    T* __restrict__ ysn;         // SCALED: d1 .* y+
+    const double* __restrict__ yoff;  // SHIFT: scaled base multipliers
     using Acc = NoAcc;
-    struct Pre { T y, lc, uc, ya, d; };
+    struct Pre { T y, lc, uc, ya, d; double yo; };
     __device__ __forceinline__ Pre pre_global(int i) const {
         return Pre{ld_stream(y + i), ld_stream(lc + i), ld_stream(uc + i),
-                   avg ? ld_stream(ya_old + i) : T(0), SCALED ? ld_stream(dsc + i) : T(0)};
+                   avg ? ld_stream(ya_old + i) : T(0), SCALED ? ld_stream(dsc + i) : T(0),
+                   SHIFT ? ld_stream(yoff + i) : 0.0};
     }
     __device__ void init(Acc&) {}
     __device__ __forceinline__ void row(int, int i, T s, const Pre& q, Acc&) {
         const StepCoef<T>& k = coef.get();
         if (SCALED) s = mul_rn(q.d, s);
         const T sigma = k.sigma;
-        const T t2 = sub_rn(q.y, mul_rn(sigma, s));
-        const T t4 = sub_rn(mul_rn(k.inv_sigma, q.y), s);
-        const T pr = proj_box(t4, -q.uc, -q.lc);
-        const T yp = sub_rn(t2, mul_rn(sigma, pr));
+        T yp;
+        if constexpr (SHIFT) {
+            const double sd = (double)s, sg = (double)sigma;
+            const double t4 = __dsub_rn(__dmul_rn((double)k.inv_sigma, __dadd_rn(q.yo, (double)q.y)), sd);
+            const double pr = proj_box(t4, -(double)q.uc, -(double)q.lc);
+            yp = (T)__dsub_rn(__dsub_rn((double)q.y, __dmul_rn(sg, sd)), __dmul_rn(sg, pr));
+        } else {
+            const T t2 = sub_rn(q.y, mul_rn(sigma, s));
+            const T t4 = sub_rn(mul_rn(k.inv_sigma, q.y), s);
+            const T pr = proj_box(t4, -q.uc, -q.lc);
+            yp = sub_rn(t2, mul_rn(sigma, pr));
+        }
         yn[i] = yp;
         if (SCALED) ysn[i] = mul_rn(q.d, yp);
         if (avg) __stcs(ya_new + i, add_rn(mul_rn(yp, k.a), mul_rn(q.ya, k.b)));

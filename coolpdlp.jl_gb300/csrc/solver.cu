@@ -16,7 +16,10 @@
 // device->host read; restart and termination decisions run on the host in
 // FP64 exactly as restart.jl:40-57, termination.jl:89-101 state them.
 #include <algorithm>
+#include <cstdlib>
+#include <cstdio>
 #include <chrono>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -629,8 +632,12 @@ double powm_default_tol(int64_t n, bool f32) {
 // is IterativeSolvers' default for Float64 (eps * n^3): with eps(Float32) that
 // rule stops large FP32 problems after one iteration, and the step size
 // eta = 0.9 / |A| then overshoots.
+// `deadline` (now_seconds() clock): the iterations also stop there.  The
+// reference's default rule can ask for n iterations (tol = eps * n^3 wraps
+// negative for some n), which a solve's time limit then bounds.
 template <class V>
-double spectral_norm_T(Handle& h, ProblemT<V>& P, const cpdlp_params* prm, int64_t* iters_out) {
+double spectral_norm_T(Handle& h, ProblemT<V>& P, const cpdlp_params* prm, int64_t* iters_out,
+                       double deadline = INFINITY) {
     cudaStream_t s = h.stream;
     const int64_t m = P.m, n = P.n;
     double tol = prm->power_tol_override > 0 ? prm->power_tol_override : powm_default_tol(n, false);
@@ -727,6 +734,7 @@ double spectral_norm_T(Handle& h, ProblemT<V>& P, const cpdlp_params* prm, int64
         it++;
         theta_d = slot.theta;
         if (it > maxiter || slot.residual <= tol || slot.residual <= rtol * slot.theta) break;
+        if (now_seconds() >= deadline) break;
     }
     if (iters_out) *iters_out = it;
     return std::sqrt(theta_d);
@@ -745,6 +753,11 @@ struct StateT : StateBase {
     // dual step writes it beside y), xbar holds D2 .* xbar, and the KKT
     // products gather the scratch copies kx = D2 .* x, ky = D1 .* y
     DBuf<T> ys[2], kx[4], ky[4];
+    // refinement round on the residual LP: the dual step's activity offset
+    // (scaled base multipliers), and the KKT evaluation of the combined iterate
+    // (base + correction) that replaces the state's own
+    const double* yoff = nullptr;
+    std::function<void(int, const T* const*, const T* const*, cpdlp_kkt_errors*)> kkt_hook;
     DBuf<StepCoef<T>> coef, coef1;
     std::vector<StepCoef<T>> coef_host;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
@@ -789,9 +802,17 @@ struct StateT : StateBase {
                      const StepCoef<T>* c, cudaStream_t s) {
         ProblemT<T>& P = *PT;
         const int avg = pdlp() ? 1 : 0;
-        if (P.pm1) {
+        if (P.pm1 && yoff) {
+            DualEpi<T, false, true, true> de{yo, P.lc.p, P.uc.p, yn, yao, yan, {c}, avg,
+                                             P.d1t.p, ysn, yoff};
+            launch_tiles<1>(P.planA, view_A_pm1(P), VecSet<T, 1>{{xg}}, de, s);
+        } else if (P.pm1) {
             DualEpi<T, false, true> de{yo, P.lc.p, P.uc.p, yn, yao, yan, {c}, avg, P.d1t.p, ysn};
             launch_tiles<1>(P.planA, view_A_pm1(P), VecSet<T, 1>{{xg}}, de, s);
+        } else if (yoff) {
+            DualEpi<T, false, false, true> de{yo, P.lc.p, P.uc.p, yn, yao, yan, {c}, avg,
+                                              nullptr, nullptr, yoff};
+            launch_tiles<1>(P.planA, view_A(P), VecSet<T, 1>{{xg}}, de, s);
         } else {
             DualEpi<T> de{yo, P.lc.p, P.uc.p, yn, yao, yan, {c}, avg};
             launch_tiles<1>(P.planA, view_A(P), VecSet<T, 1>{{xg}}, de, s);
@@ -919,6 +940,10 @@ struct StateT : StateBase {
 
     template <int NV>
     void kkt_multi(const T* const (&xs)[NV], const T* const (&ys)[NV], cpdlp_kkt_errors* out) {
+        if (kkt_hook) {
+            kkt_hook(NV, xs, ys, out);
+            return;
+        }
         ProblemT<T>& P = *PT;
         cudaStream_t s = h->stream;
         for (int p = 0; p < NV; p++) enqueue_kkt_pair(p, xs[p], ys[p]);
@@ -1246,7 +1271,7 @@ StateBase* make_state(Handle& h, ProblemT<T>* P, const cpdlp_params* prm, const 
         S->eta = eta0;
         S->power_iterations = 0;
     } else {
-        double sn = spectral_norm_T(h, *P, prm, &S->power_iterations);
+        double sn = spectral_norm_T(h, *P, prm, &S->power_iterations, t0 + prm->time_limit);
         S->eta = prm->invnorm_scaling * (1.0 / sn);
     }
     // primal_weight_init (step_size.jl:29-40); PDHG: omega = 1 (pdhg.jl:48)
@@ -1270,6 +1295,259 @@ StateBase* make_state(Handle& h, ProblemT<T>* P, const cpdlp_params* prm, const 
     S->setup_seconds = P->setup_seconds + (now_seconds() - t0);
     guard.release();
     return S;
+}
+
+// ---------------------------------------------------------------------------
+// refinement on the residual LP (FP32 rounds, FP64 residuals)
+// ---------------------------------------------------------------------------
+// A round fixes a base point (x0, y0) of the scaled LP (FP64) and solves, with
+// FP32 iterates, for the correction (dx, dy) of
+//   min r'dx  s.t.  lc - A x0 <= A dx <= uc - A x0,  lv - x0 <= dx <= uv - x0,
+// r = c - A'y0.  Its saddle function is the original one shifted by (x0, y0),
+// so it has the same KKT errors; the dual step decides each row's activity on
+// y0 + dy (DualEpi SHIFT).  The residual data are computed in FP64 and scaled
+// by powers of two, dp on the primal side and dd on the dual side, so that the
+// FP32 iterates resolve them.  After the round, x0 += dx/dp and y0 += dy/dd in
+// FP64.
+constexpr int REFINE_MAX_ROUNDS = 8;
+// a round ends once the combined relative KKT error fell by this factor
+constexpr double REFINE_ROUND_DECAY = 1e-4;
+constexpr double REFINE_MAX_SCALE = 1099511627776.0;  // 2^40
+
+// CPDLP_TRACE=1 in the environment prints one line per refinement round to
+// stderr, CPDLP_TRACE=2 also one line per check
+int trace_level() {
+    static const int lvl = [] {
+        const char* v = std::getenv("CPDLP_TRACE");
+        return v ? std::atoi(v) : 0;
+    }();
+    return lvl;
+}
+bool trace_on() { return trace_level() > 0; }
+
+__global__ void k_refine_rows(const double* __restrict__ lc, const double* __restrict__ uc,
+                              const double* __restrict__ Ax0, const double* __restrict__ y0,
+                              double dp, double dd, float* __restrict__ lco,
+                              float* __restrict__ uco, double* __restrict__ yoff, int64_t m) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    lco[i] = (float)__dmul_rn(dp, __dsub_rn(lc[i], Ax0[i]));
+    uco[i] = (float)__dmul_rn(dp, __dsub_rn(uc[i], Ax0[i]));
+    yoff[i] = __dmul_rn(dd, y0[i]);
+}
+__global__ void k_refine_cols(const double* __restrict__ c, const double* __restrict__ lv,
+                              const double* __restrict__ uv, const double* __restrict__ Aty0,
+                              const double* __restrict__ x0, double dp, double dd,
+                              float* __restrict__ co, float* __restrict__ lvo,
+                              float* __restrict__ uvo, int64_t n) {
+    int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    co[j] = (float)__dmul_rn(dd, __dsub_rn(c[j], Aty0[j]));
+    lvo[j] = (float)__dmul_rn(dp, __dsub_rn(lv[j], x0[j]));
+    uvo[j] = (float)__dmul_rn(dp, __dsub_rn(uv[j], x0[j]));
+}
+// combined iterate: x = proj(x0 + dx/dp, lv, uv); y = y0 + dy/dd restricted to
+// the signs its row's bounds allow (>= 0 with only lc finite, <= 0 with only
+// uc finite, 0 for a free row), as the dual step keeps them
+template <class T>
+__global__ void k_refine_combine(const double* x0, const T* __restrict__ dx, double inv_dp,
+                                 const double* __restrict__ lv, const double* __restrict__ uv,
+                                 double* xo, int64_t n, const double* y0,
+                                 const T* __restrict__ dy, double inv_dd,
+                                 const double* __restrict__ lc, const double* __restrict__ uc,
+                                 double* yo, int64_t m) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride)
+        xo[j] = proj_box(__dadd_rn(x0[j], __dmul_rn((double)dx[j], inv_dp)), lv[j], uv[j]);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += stride) {
+        double v = __dadd_rn(y0[i], __dmul_rn((double)dy[i], inv_dd));
+        const bool lo = !isinf(lc[i]), up = !isinf(uc[i]);
+        if (lo && !up) v = fmax(v, 0.0);
+        else if (!lo && up) v = fmin(v, 0.0);
+        else if (!lo && !up) v = 0.0;
+        yo[i] = v;
+    }
+}
+
+// Progress of an FP32 run, checked after every block: stalled once the error
+// has not halved over `window` passes while at most `max_rel`, or over `long_window`
+// passes at any level
+struct StallWatch {
+    double best = INFINITY;
+    int64_t mark = 0;
+    bool stalled(double rel, int64_t passes, int64_t window, int64_t long_window, double max_rel) {
+        if (rel < 0.5 * best) {
+            best = rel;
+            mark = passes;
+            return false;
+        }
+        const int64_t since = passes - mark;
+        return (since >= window && best <= max_rel) || since >= long_window;
+    }
+};
+
+double rel_err(const cpdlp_kkt_errors& e) {
+    return jl_max(jl_max(e.primal / e.primal_scale, e.dual / e.dual_scale), e.gap / e.gap_scale);
+}
+// 2^k nearest below 1/v, within [1, 2^40]
+double pow2_scale(double v) {
+    if (!(v > 0.0)) return REFINE_MAX_SCALE;
+    double sc = 1.0 / v;
+    if (!(sc >= 1.0)) return 1.0;
+    if (sc > REFINE_MAX_SCALE) return REFINE_MAX_SCALE;
+    return std::exp2(std::floor(std::log2(sc)));
+}
+
+struct RefineResult {
+    int32_t status = CPDLP_STILL_RUNNING;
+    bool progress = true;  // false: a round did not halve the error (continue in FP64)
+    int rounds = 0;
+    int64_t passes = 0, launches = 0;
+    double omega = 1.0;    // primal weight in the original scaling
+    cpdlp_kkt_errors err{};
+};
+
+// Rounds from the base point (x0, y0) (FP64, scaled space) until refine_reltol,
+// the pass or time limit, a round without progress or REFINE_MAX_ROUNDS.  P32's
+// bound and cost vectors are overwritten with each round's residual data; S64
+// is a state of P64 used for its FP64 KKT passes.
+RefineResult refine_residual(Handle& h, ProblemT<float>& P32, ProblemT<double>& P64,
+                             StateT<double>& S64, DBuf<double>& x0, DBuf<double>& y0,
+                             const cpdlp_params& prm, double t0, double eta, double omega,
+                             int64_t passes_left) {
+    RefineResult R;
+    R.omega = omega;
+    cudaStream_t s = h.stream;
+    const int64_t m = P64.m, n = P64.n;
+    const size_t nz = (size_t)std::max<int64_t>(n, 1), mz = (size_t)std::max<int64_t>(m, 1);
+    DBuf<double> Ax0(mz), Aty0(nz), cx[4], cy[4];
+    DBuf<double> yoff(mz);
+    for (int q = 0; q < 4; q++) {
+        cx[q].alloc(nz);
+        cy[q].alloc(mz);
+    }
+    const unsigned gc = red_grid(h, std::max(m, n));
+    auto kkt_base = [&](cpdlp_kkt_errors* e) {
+        const double* const xs[1] = {x0.p};
+        const double* const ys[1] = {y0.p};
+        S64.kkt_multi<1>(xs, ys, e);
+    };
+    cpdlp_kkt_errors e;
+    kkt_base(&e);
+    const int ce = prm.check_every > 0 ? prm.check_every : 100;
+    for (;;) {
+        R.err = e;
+        const double r0 = rel_err(e);
+        if (r0 <= prm.refine_reltol) { R.status = CPDLP_OPTIMAL; break; }
+        if (now_seconds() - t0 >= prm.time_limit) { R.status = CPDLP_TIME_LIMIT; break; }
+        if (passes_left <= 0) { R.status = CPDLP_ITERATION_LIMIT; break; }
+        if (R.rounds >= REFINE_MAX_ROUNDS) { R.progress = false; break; }
+        const double ep = e.primal / e.primal_scale, ed = e.dual / e.dual_scale,
+                     eg = e.gap / e.gap_scale;
+        const double dp = pow2_scale(jl_max(ep, eg)), dd = pow2_scale(jl_max(ed, eg));
+        // the round's residual LP, in P32's vectors
+        launch_tiles<1>(P64.planA, view_A(P64), VecSet<double, 1>{{x0.p}}, StoreEpi<double>{Ax0.p}, s);
+        launch_tiles<1>(P64.planAt, view_At(P64), VecSet<double, 1>{{y0.p}},
+                        StoreEpi<double>{Aty0.p}, s);
+        if (m > 0)
+            k_refine_rows<<<grid_for(m, 256), 256, 0, s>>>(P64.lc.p, P64.uc.p, Ax0.p, y0.p, dp, dd,
+                                                           P32.lc.p, P32.uc.p, yoff.p, m);
+        if (n > 0)
+            k_refine_cols<<<grid_for(n, 256), 256, 0, s>>>(P64.c.p, P64.lv.p, P64.uv.p, Aty0.p,
+                                                           x0.p, dp, dd, P32.c.p, P32.lv.p,
+                                                           P32.uv.p, n);
+        CK_LAUNCH();
+        R.launches += tiles_launches(P64.planA) + tiles_launches(P64.planAt) + 2;
+        cpdlp_params pr = prm;
+        pr.float_type = CPDLP_VAL_F32;
+        pr.termination_reltol = 0.0;  // the rounds' own rule below decides
+        pr.max_kkt_passes = passes_left;
+        std::unique_ptr<StateBase> SB(
+            make_state<float>(h, &P32, &pr, nullptr, nullptr, eta, R.omega * dd / dp));
+        auto& S = static_cast<StateT<float>&>(*SB);
+        S.starting_time = t0;
+        S.yoff = yoff.p;
+        cpdlp_kkt_errors e_cur = e, e_avg = e;
+        S.kkt_hook = [&](int nv, const float* const* xs, const float* const* ys,
+                         cpdlp_kkt_errors* o) {
+            for (int q = 0; q < nv; q++)
+                k_refine_combine<float><<<gc, RED_THREADS, 0, s>>>(
+                    x0.p, xs[q], 1.0 / dp, P64.lv.p, P64.uv.p, cx[q].p, n, y0.p, ys[q], 1.0 / dd,
+                    P64.lc.p, P64.uc.p, cy[q].p, m);
+            CK_LAUNCH();
+            S.launches += nv;
+            if (nv == 4) {
+                const double* const X[4] = {cx[0].p, cx[1].p, cx[2].p, cx[3].p};
+                const double* const Y[4] = {cy[0].p, cy[1].p, cy[2].p, cy[3].p};
+                S64.kkt_multi<4>(X, Y, o);
+                e_cur = o[0];  // the current iterate (checked after every block)
+                e_avg = o[1];
+            } else {
+                const double* const X[1] = {cx[0].p};
+                const double* const Y[1] = {cy[0].p};
+                S64.kkt_multi<1>(X, Y, o);
+                if (!S.pdlp()) e_cur = o[0];  // PDHG checks sol alone
+            }
+            // the residual LP's errors in its own (dp, dd) scaling, for the
+            // restart rule and the primal weight
+            for (int q = 0; q < nv; q++) {
+                o[q].primal *= dp;
+                o[q].dual *= dd;
+                o[q].gap *= dp * dd;
+            }
+        };
+        const double target = jl_max(prm.refine_reltol, REFINE_ROUND_DECAY * r0);
+        // a round counts as stalled once it gained a factor 100 and stopped
+        // halving, or after FP32_STALL_LONG windows without halving
+        StallWatch watch;
+        const char* why = "limit";
+        int64_t outer_before = S.outer;
+        bool use_avg = false;
+        while (S.solve_blocks(1) == CPDLP_STILL_RUNNING) {
+            // the better of sol and its average (unless the check restarted, which
+            // moved the chosen candidate into sol)
+            use_avg = S.pdlp() && S.outer == outer_before && rel_err(e_avg) < rel_err(e_cur);
+            outer_before = S.outer;
+            const double rc = jl_min(rel_err(e_cur), use_avg ? rel_err(e_avg) : INFINITY);
+            if (trace_level() > 1)
+                fprintf(stderr, "[cpdlp refine]   %lld: rel %.3e (p %.2e d %.2e g %.2e) omega %.3g\n",
+                        (long long)S.kkt_passes, rc, e_cur.primal / e_cur.primal_scale,
+                        e_cur.dual / e_cur.dual_scale, e_cur.gap / e_cur.gap_scale, S.omega);
+            if (rc <= target) { why = "target"; break; }
+            if (watch.stalled(rc, S.kkt_passes, FP32_STALL_CHECKS * (int64_t)ce,
+                              FP32_STALL_LONG * FP32_STALL_CHECKS * (int64_t)ce, 1e-2 * r0)) {
+                why = "stall";
+                break;
+            }
+        }
+        // the new base point: the round's solution (sol, or its average when
+        // that was better at the last check) added in FP64
+        const float* dxp = use_avg ? S.xa[S.cur].p : S.x[S.cur].p;
+        const float* dyp = use_avg ? S.ya[S.cur].p : S.y[S.cur].p;
+        k_refine_combine<float><<<gc, RED_THREADS, 0, s>>>(x0.p, dxp, 1.0 / dp, P64.lv.p, P64.uv.p,
+                                                          x0.p, n, y0.p, dyp, 1.0 / dd, P64.lc.p,
+                                                          P64.uc.p, y0.p, m);
+        CK_LAUNCH();
+        R.launches += S.launches + 1;
+        R.passes += S.kkt_passes;
+        passes_left -= S.kkt_passes;
+        R.omega = S.omega * dp / dd;
+        R.rounds++;
+        kkt_base(&e);
+        if (trace_on())
+            fprintf(stderr,
+                    "[cpdlp refine] round %d: rel %.3e (p %.2e d %.2e g %.2e) dp %.3g dd %.3g "
+                    "-> %.3e after %lld passes (%s, %lld restarts)\n",
+                    R.rounds, r0, ep, ed, eg, dp, dd, rel_err(e), (long long)S.kkt_passes, why,
+                    (long long)S.outer);
+        if (!(rel_err(e) <= 0.5 * r0)) {
+            R.err = e;
+            R.progress = false;
+            break;
+        }
+    }
+    R.launches += S64.launches;
+    return R;
 }
 
 }  // namespace
@@ -1328,18 +1606,22 @@ void solve_full(Handle& h, const cpdlp_lp* lp, const cpdlp_params* params, const
     if (P->m == 0 && P->zero_cost) {
         S->early_exit_zero_problem();  // common.jl:194-198
     } else if (mixed) {
-        // FP32 phase, one check at a time: iterates whose relative KKT error has
-        // not halved over FP32_STALL_CHECKS checks continue in FP64
-        double best = INFINITY;
-        int64_t mark = 0;
+        // FP32 phase, one check at a time, until a stall or the tighter of the
+        // two tolerances (FP32 iterates often get well below termination_reltol)
+        StallWatch watch;
+        S->prm.termination_reltol = std::min(params->termination_reltol,
+                                             params->refine_reltol > 0 ? params->refine_reltol
+                                                                       : INFINITY);
+        const int64_t win = FP32_STALL_CHECKS * (int64_t)params->check_every;
         while (S->solve_blocks(1) == CPDLP_STILL_RUNNING) {
             const cpdlp_kkt_errors& e = S->err;
             const double rel = std::max(std::max(e.primal / e.primal_scale, e.dual / e.dual_scale),
                                         e.gap / e.gap_scale);
-            if (rel < 0.5 * best) {
-                best = rel;
-                mark = S->kkt_passes;
-            } else if (S->kkt_passes - mark >= FP32_STALL_CHECKS * (int64_t)params->check_every) {
+            if (trace_level() > 1)
+                fprintf(stderr, "[cpdlp refine]   FP32 %lld: rel %.3e (p %.2e d %.2e g %.2e)\n",
+                        (long long)S->kkt_passes, rel, e.primal / e.primal_scale,
+                        e.dual / e.dual_scale, e.gap / e.gap_scale);
+            if (watch.stalled(rel, S->kkt_passes, win, FP32_STALL_LONG * win, FP32_STALL_REL)) {
                 stalled = true;
                 break;
             }
@@ -1347,43 +1629,90 @@ void solve_full(Handle& h, const cpdlp_lp* lp, const cpdlp_params* params, const
     } else {
         S->solve();
     }
-    // FP64 phase: the FP32 solution reached termination_reltol and a tighter
-    // refine_reltol is asked for, or the FP32 iterates stalled
-    const bool refine = mixed && !(P->m == 0 && P->zero_cost) &&
-                        ((S->status == CPDLP_OPTIMAL &&
-                          params->refine_reltol < params->termination_reltol) || stalled);
+    if (mixed && trace_on())
+        fprintf(stderr, "[cpdlp refine] FP32 phase: rel %.3e after %lld passes%s\n",
+                rel_err(S->err), (long long)S->kkt_passes, stalled ? " (stalled)" : "");
+    // refinement: the FP32 iterates stalled before the tolerance
+    const bool refine = mixed && stalled;
     if (!refine) {
         S->solution(x_out, y_out);
         if (stats) S->stats(stats);
         return;
     }
-    // FP64 refinement from the FP32 solution (original units)
-    std::vector<double> xs((size_t)std::max<int64_t>(P->n, 1)), ys((size_t)std::max<int64_t>(P->m, 1));
-    S->solution(xs.data(), ys.data());
+    // Refinement on the residual LP: FP32 rounds from the FP32 solution, with
+    // the residuals, the combination and the KKT errors in FP64 (the step size
+    // is a property of A and carries over; so does the adapted primal weight
+    // after a converged FP32 phase)
+    cpdlp_stats st32;
+    S->stats(&st32);
+    const double eta32 = S->eta, omega32 = S->omega;
+    auto& P32 = static_cast<ProblemT<float>&>(*P);
+    const int64_t m = P->m, n = P->n;
+    const size_t nz = (size_t)std::max<int64_t>(n, 1), mz = (size_t)std::max<int64_t>(m, 1);
+    DBuf<double> bx(nz), by(mz);
+    {
+        auto& S32 = static_cast<StateT<float>&>(*S);
+        if (n > 0) k_widen<float><<<grid_for(n, 256), 256, 0, h.stream>>>(S32.x[S32.cur].p, bx.p, n);
+        if (m > 0) k_widen<float><<<grid_for(m, 256), 256, 0, h.stream>>>(S32.y[S32.cur].p, by.p, m);
+        CK_LAUNCH();
+    }
+    S.reset();
     cpdlp_params p64 = *params;
     p64.float_type = CPDLP_VAL_F64;
     p64.termination_reltol = params->refine_reltol;
-    p64.max_kkt_passes = std::max<int64_t>(params->max_kkt_passes - S->kkt_passes, 1);
-    p64.time_limit = params->time_limit - (now_seconds() - t0);
-    const int64_t passes32 = S->kkt_passes;
-    const int64_t launches32 = S->launches;
-    // continuation: the FP64 phase keeps the step size (an FP64 power method over
-    // the same values up to FP32 rounding) and, after a converged FP32 phase, the
-    // adapted primal weight
-    const double eta32 = S->eta, omega32 = S->omega;
-    S.reset();
-    P.reset();
     std::unique_ptr<ProblemBase> P64(problem_create(h, lp, &p64));
-    std::unique_ptr<StateBase> S64(
-        state_create(h, P64.get(), &p64, xs.data(), ys.data(), eta32, stalled ? 0.0 : omega32));
-    S64->starting_time = t0;
-    S64->solve();
-    S64->solution(x_out, y_out);
+    auto& Q64 = static_cast<ProblemT<double>&>(*P64);
+    std::unique_ptr<StateBase> S64(state_create(h, P64.get(), &p64, nullptr, nullptr, eta32, omega32));
+    auto& T64 = static_cast<StateT<double>&>(*S64);
+    const RefineResult R = refine_residual(h, P32, Q64, T64, bx, by, *params, t0, eta32, omega32,
+                                           params->max_kkt_passes - st32.kkt_passes);
+    int64_t passes = st32.kkt_passes + R.passes;
+    int64_t launches = st32.kernel_launches + R.launches;
+    if (R.progress || R.status != CPDLP_STILL_RUNNING) {
+        if (n > 0) k_unscale<double><<<grid_for(n, 256), 256, 0, h.stream>>>(bx.p, Q64.D2.p, T64.xr.p, n);
+        if (m > 0) k_unscale<double><<<grid_for(m, 256), 256, 0, h.stream>>>(by.p, Q64.D1.p, T64.yr.p, m);
+        CK_LAUNCH();
+        if (x_out && n > 0)
+            CK(cudaMemcpyAsync(x_out, T64.xr.p, sizeof(double) * n, cudaMemcpyDeviceToHost, h.stream));
+        if (y_out && m > 0)
+            CK(cudaMemcpyAsync(y_out, T64.yr.p, sizeof(double) * m, cudaMemcpyDeviceToHost, h.stream));
+        CK(cudaStreamSynchronize(h.stream));
+        if (stats) {
+            *stats = st32;
+            stats->err = R.err;
+            stats->termination_status = R.status;
+            stats->kkt_passes = passes;
+            stats->refine_kkt_passes = R.passes;
+            stats->omega = R.omega;
+            stats->time_elapsed = now_seconds() - t0;
+            stats->kernel_launches = launches;
+        }
+        return;
+    }
+    // a round made no progress: continue in FP64 from the refined point
+    if (trace_on())
+        fprintf(stderr, "[cpdlp refine] no progress after %d rounds: FP64 continuation\n",
+                R.rounds);
+    std::vector<double> xs(nz), ys(mz);
+    if (n > 0) k_unscale<double><<<grid_for(n, 256), 256, 0, h.stream>>>(bx.p, Q64.D2.p, T64.xr.p, n);
+    if (m > 0) k_unscale<double><<<grid_for(m, 256), 256, 0, h.stream>>>(by.p, Q64.D1.p, T64.yr.p, m);
+    CK_LAUNCH();
+    if (n > 0) CK(cudaMemcpyAsync(xs.data(), T64.xr.p, sizeof(double) * n, cudaMemcpyDeviceToHost, h.stream));
+    if (m > 0) CK(cudaMemcpyAsync(ys.data(), T64.yr.p, sizeof(double) * m, cudaMemcpyDeviceToHost, h.stream));
+    CK(cudaStreamSynchronize(h.stream));
+    S64.reset();
+    P.reset();
+    p64.max_kkt_passes = std::max<int64_t>(params->max_kkt_passes - passes, 1);
+    std::unique_ptr<StateBase> C64(
+        state_create(h, P64.get(), &p64, xs.data(), ys.data(), eta32, stalled ? 0.0 : R.omega));
+    C64->starting_time = t0;
+    C64->solve();
+    C64->solution(x_out, y_out);
     if (stats) {
-        S64->stats(stats);
-        stats->refine_kkt_passes = S64->kkt_passes;
-        stats->kkt_passes = passes32 + S64->kkt_passes;
-        stats->kernel_launches += launches32;
+        C64->stats(stats);
+        stats->refine_kkt_passes = R.passes + C64->kkt_passes;
+        stats->kkt_passes = passes + C64->kkt_passes;
+        stats->kernel_launches += launches;
     }
 }
 

@@ -11,6 +11,13 @@ namespace cpdlp {
 // FP32 iterates whose relative KKT error has not halved over this many checks
 // continue in FP64 (cpdlp_solve with refine_reltol > 0, and the batched solver)
 constexpr int64_t FP32_STALL_CHECKS = 30;
+// The single-LP rule also asks that the error be at most this (PDLP's error
+// is noisy and can plateau for thousands of iterations far from a solution,
+// where FP32 rounding is not what holds it back; FP32 iterates commonly reach
+// 1e-6 to 1e-7), or that no halving came for FP32_STALL_LONG times as many
+// checks
+constexpr double FP32_STALL_REL = 1e-5;
+constexpr int64_t FP32_STALL_LONG = 10;
 // With FP32 iterates the power method also stops once its residual is below
 // this fraction of theta (the step size needs theta to about 1e-4)
 constexpr double POWER_RTOL_F32 = 1e-4;
@@ -91,10 +98,13 @@ StateBase* state_create(Handle& h, ProblemBase* P, const cpdlp_params* prm, cons
                         const double* y0, double eta0 = 0.0, double omega0 = 0.0);
 double problem_spectral_norm(Handle& h, ProblemBase* P, const cpdlp_params* prm, int64_t* iters);
 
-// solve(milp, sol, algo) (common.jl:186-209) on the device, plus the FP64
-// refinement phase: when params->float_type is FP32, refine_reltol > 0 and the
-// FP32 solve ends OPTIMAL, PDLP continues in FP64 from the FP32 solution
-// until refine_reltol.  x_out (n) / y_out (m) may be null.
+// solve(milp, sol, algo) (common.jl:186-209) on the device, plus mixed
+// precision: with FP32 iterates and 0 < refine_reltol < termination_reltol the
+// FP32 phase runs on towards refine_reltol until its error stalls; from there
+// (or from an FP32 phase that stalls above termination_reltol) refinement
+// rounds solve the residual LP of the FP64 point with FP32 iterates and add
+// the correction in FP64, and PDLP continues in FP64 if a round makes no
+// progress.  x_out (n) / y_out (m) may be null.
 void solve_full(Handle& h, const cpdlp_lp* lp, const cpdlp_params* params, const double* x0,
                 const double* y0, double* x_out, double* y_out, cpdlp_stats* stats);
 void problem_scaling(Handle& h, ProblemBase* P, double* d1, double* d2);
