@@ -119,11 +119,14 @@ typedef struct cpdlp_params {
     double power_tol_override;      /* 0 = reference default */
     int64_t power_maxiter_override; /* 0 = reference default */
     uint64_t power_seed;            /* start vector seed (EXT; the reference uses StableRNG(0)) */
-    /* EXT: mixed precision for float_type CPDLP_VAL_F32 (0 = off): when the
-     * FP32 solve reaches termination_reltol and refine_reltol is smaller, or
-     * when the FP32 iterates stall (the relative KKT error does not halve over
-     * 30 checks), the solve continues in FP64 from the FP32 iterate until
-     * refine_reltol. */
+    /* EXT: mixed precision for float_type CPDLP_VAL_F32 (0 = off).
+     * cpdlp_solve: the FP32 run aims at the smaller of termination_reltol and
+     * refine_reltol; when its relative KKT error stalls short of that (not
+     * halved over 30 checks while at most 1e-5, or over 300 checks),
+     * refinement rounds solve the residual LP of the FP64 point with FP32
+     * iterates and add each correction in FP64 (FP64 residuals and KKT
+     * errors), and PDLP continues in FP64 if a round makes no progress.
+     * Batched solves and jobs continue in FP64 instead (cpdlp_batch_solve). */
     double refine_reltol;
     /* EXT: CSR tile size in nonzeros for the SpMV work partition (0 = autotune). */
     int32_t tile_nnz;
