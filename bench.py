@@ -15,6 +15,13 @@ with the LP resident in HBM, timed with CUDA events on the library's stream;
 timed region).  The working set (~0.6 GB per iteration) is larger than L2,
 so no flush is needed between steps.
 
+The same JSON line also carries `flow` (the 256x256 grid multicommodity flow
+LP with K=16: FP32 iterations/s with the narrow +-1 storage and with scaled
+values, and solves to 1e-4 and, with refinement rounds, to 1e-8), `batch`
+(4,096 random LPs in persistent launches against the one-at-a-time FP64
+path) and `serving` (a Poisson stream through the continuous-batching
+server, p50/p99).
+
 --impl reference times the CPU restatement of the reference algorithm
 (oracle/, Float64, all host threads) on the same LP.
 Under torchrun with N ranks every rank solves its own copy (one LP does not
@@ -59,6 +66,13 @@ def parse_args():
     ap.add_argument("--serve-rate", type=float, default=8.0, help="Poisson arrivals per second")
     ap.add_argument("--batch-m-hi", type=int, default=5000,
                     help="largest m of the batched LPs (5000 = the named workload)")
+    ap.add_argument("--flow-side", type=int, default=256,
+                    help="grid side of the multicommodity flow LP (0 skips the flow section)")
+    ap.add_argument("--flow-k", type=int, default=16, help="commodities of the flow LP")
+    ap.add_argument("--flow-no-solve", action="store_true",
+                    help="flow section without the solves to 1e-4 / 1e-8")
+    ap.add_argument("--only-flow", action="store_true",
+                    help="run only the flow measurement (profiling); no headline value")
     ap.add_argument("--only-batch", action="store_true",
                     help="run only the batched measurement (profiling small cases)")
     return ap.parse_args()
@@ -213,6 +227,10 @@ def measure_batch(h, count: int, sample: int, m_hi: int = 5000) -> dict:
     out["max_obj_rel_diff_fp32_vs_fp64"] = float(max(
         abs(obj(k, res["fp32_refined"][k]) - obj(k, res["fp64_batched"][k]))
         / max(1.0, abs(obj(k, res["fp64_batched"][k]))) for k in range(count)))
+    out["workload"] = (f"{count} random sparse LPs, m log-U[50,{m_hi}], n=2m, 3-8 nnz/column, "
+                       "seed 1000+i, 1e-4 relative KKT")
+    if sample <= 0:
+        return out
     idx = list(range(0, count, max(1, count // max(sample, 1))))[:sample]
     p = native.default_params()
     t0 = time.perf_counter()
@@ -226,8 +244,76 @@ def measure_batch(h, count: int, sample: int, m_hi: int = 5000) -> dict:
                               "mean_passes": passes / len(idx)}
     out["speedup_fp32_refined_vs_sequential"] = out["fp32_refined"]["lps_per_s"] / seq
     out["speedup_fp64_batched_vs_sequential"] = out["fp64_batched"]["lps_per_s"] / seq
-    out["workload"] = (f"{count} random sparse LPs, m log-U[50,{m_hi}], n=2m, 3-8 nnz/column, "
-                       "seed 1000+i, 1e-4 relative KKT")
+    return out
+
+
+def measure_flow(h, side: int, K: int, blocks: int = 10, solves: bool = True) -> dict:
+    """The structured multicommodity min-cost flow LP (side x side grid, K
+    commodities, matrix values exactly +-1): FP32 PDLP iterations per second
+    with the narrow +-1 storage (the default) and with the scaled values
+    (CPDLP_TILE_NO_NARROW), per-kernel GB/s from CUDA events, and cpdlp_solve to
+    1e-4 (FP32) and to 1e-8 (FP32 + refinement rounds with FP64 residuals)."""
+    import ctypes
+    import numpy as np
+    import torch
+    from coolpdlp import _abi as A
+    from coolpdlp import generators as G
+    from coolpdlp import native
+    lp = G.multicommodity_flow_lp(side=side, K=K, seed=2)
+    L = native.LPStruct(lp.m, lp.n, lp.colptr, lp.rowval, lp.nzval, lp.c, lp.lv, lp.uv, lp.lc,
+                        lp.uc)
+    peak, peak_kind = load_peak()
+    out = {"workload": (f"multicommodity flow LP, {side}x{side} grid, K={K}, seed 2: "
+                        f"m={lp.m:,} n={lp.n:,} nnz={lp.nnz:,}, values exactly +-1"),
+           "peak_gbs": peak, "peak_source": peak_kind}
+    ext = torch.cuda.ExternalStream(h.stream)
+    for name, flags in (("narrow", 0), ("valued", A.TILE_NO_NARROW)):
+        prm = A.default_params_py(A.ALGO_PDLP)
+        prm.float_type = A.VAL_F32
+        prm.tile_flags = flags
+        prm.termination_reltol = 0.0
+        prm.max_kkt_passes = 1 << 60
+        prm.time_limit = 1e30
+        P = native.Problem(h, L, prm)
+        S = native.State(P, prm)
+        for _ in range(3):
+            S.solve_blocks(1)
+        h.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        for _ in range(blocks):
+            S.solve_blocks(1)
+        e1.record(ext)
+        h.synchronize()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        prof = S.profile(20)
+        kb = S.kernel_bytes()
+        out[name] = {
+            "iters_per_s": blocks * CHECK_EVERY / (ms * 1e-3),
+            "kernels": {nm: {"ms": float(prof[i]), "bytes": float(kb[i]),
+                             "gbs": float(kb[i] / (prof[i] * 1e-3) / 1e9),
+                             "frac": float(kb[i] / (prof[i] * 1e-3) / 1e9 / peak)}
+                        for i, nm in enumerate(("primal_step", "dual_step", "kkt4"))}}
+        del S, P
+    out["narrow_speedup"] = out["narrow"]["iters_per_s"] / out["valued"]["iters_per_s"]
+    for tag, tol, refine in ((("solve_1e-4", 1e-4, 0.0), ("solve_1e-8", 1e-4, 1e-8))
+                             if solves else ()):
+        prm = A.default_params_py(A.ALGO_PDLP)
+        prm.float_type = A.VAL_F32
+        prm.termination_reltol = tol
+        prm.refine_reltol = refine
+        prm.max_kkt_passes = 1 << 40
+        prm.time_limit = 300.0
+        t0 = time.perf_counter()
+        x, y, st = native.solve_lp(h, L, prm)
+        dt = time.perf_counter() - t0
+        e = st.err
+        rel = max(e.primal / e.primal_scale, e.dual / e.dual_scale, e.gap / e.gap_scale)
+        out[tag] = {"status": int(st.termination_status), "iterations": int(st.kkt_passes),
+                    "refine_iterations": int(st.refine_kkt_passes), "rel_kkt": rel,
+                    "seconds": dt, "objective": float(np.dot(lp.c, x))}
     return out
 
 
@@ -315,6 +401,13 @@ def run_ours(args):
     from coolpdlp import _abi as A
     from coolpdlp import native
 
+    if args.only_flow:
+        if rank == 0:
+            h = native.Handle(local)
+            print(json.dumps({"metric": METRIC, "impl": "ours", "value": None,
+                              "flow": measure_flow(h, args.flow_side, args.flow_k,
+                                                   solves=not args.flow_no_solve)}), flush=True)
+        return
     if args.only_batch:
         # the batched workload alone (small cases for profilers); no headline value
         if rank == 0:
@@ -453,6 +546,9 @@ def run_ours(args):
         }
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(lp)
+        if args.flow_side > 0:
+            line["flow"] = measure_flow(h, args.flow_side, args.flow_k,
+                                        solves=not args.flow_no_solve)
         if args.batch_lps > 0:
             line["batch"] = measure_batch(h, args.batch_lps, args.sequential_sample,
                                           args.batch_m_hi)
