@@ -894,9 +894,12 @@ struct Run : RunBase {
         }
         cpdlp_lp big{M, N, NZ, colptr.data(), rowval.data(), nzval.data(), c.data(), lv.data(),
                      uv.data(), lc.data(), uc.data()};
-        // the batched kernels read the scaled values: no narrow +-1 storage
+        // the batched kernels read the scaled values (no narrow +-1 storage)
+        // and cut their own tile plans at LP boundaries (no autotuning of the
+        // concatenation's plans)
         cpdlp_params pprm = prm;
         pprm.tile_flags |= CPDLP_TILE_NO_NARROW;
+        if (pprm.tile_nnz == 0) pprm.tile_nnz = 32 * BATCH_ITEMS;
         PB.reset(problem_create(rh, &big, &pprm));
         auto& P = static_cast<ProblemT<T>&>(*PB);
         // tile plans with LP boundaries
@@ -929,7 +932,7 @@ struct Run : RunBase {
             // the power method runs in FP64 for either iterate type
             d.power_tol = prm.power_tol_override > 0 ? prm.power_tol_override : powm_tol(d.n, false);
             d.power_maxiter = prm.power_maxiter_override > 0 ? prm.power_maxiter_override : d.n;
-            // FP32 iterates need theta to about 1e-4, not to eps(Float64) n^3
+            // FP32 iterates need theta to about 1%, not to eps(Float64) n^3
             d.power_rtol = std::is_same<T, float>::value ? POWER_RTOL_F32 : 0.0;
             d.reltol = lps[k].reltol;
             d.time_limit = lps[k].time_limit;

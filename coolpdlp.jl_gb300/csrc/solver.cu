@@ -642,7 +642,7 @@ double spectral_norm_T(Handle& h, ProblemT<V>& P, const cpdlp_params* prm, int64
     const int64_t m = P.m, n = P.n;
     double tol = prm->power_tol_override > 0 ? prm->power_tol_override : powm_default_tol(n, false);
     int64_t maxiter = prm->power_maxiter_override > 0 ? prm->power_maxiter_override : n;
-    // FP32 iterates need theta to about 1e-4, not to eps(Float64) n^3 (which
+    // FP32 iterates need theta to about 1%, not to eps(Float64) n^3 (which
     // can ask for n iterations on small or, through the Int64 wrap, huge LPs)
     const double rtol = std::is_same<V, float>::value ? POWER_RTOL_F32 : -1.0;
     std::vector<double> x0;
