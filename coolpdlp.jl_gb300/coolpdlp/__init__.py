@@ -12,7 +12,8 @@ from .algorithms import (ITERATION_LIMIT, OPTIMAL, STILL_RUNNING, TIME_LIMIT, PD
                          relative, solve, solve_, solve_inplace)
 from .matrices import GPUSparseMatrixCOO, GPUSparseMatrixCSR, GPUSparseMatrixELL
 from .problems import (CSCMatrix, MILP, PrimalDualSolution, axpby, is_feasible, nbcons,
-                       nbcons_eq, nbcons_ineq, nbvar, nbvar_cont, nbvar_int, objective_value)
+                       nbcons_eq, nbcons_ineq, nbvar, nbvar_cont, nbvar_int, objective_value,
+                       sort_rows_columns)
 
 __all__ = [
     "GPUSparseMatrixCOO", "GPUSparseMatrixCSR", "GPUSparseMatrixELL",
@@ -21,4 +22,5 @@ __all__ = [
     "PDHG", "PDLP", "Algorithm", "is_feasible", "objective_value", "TerminationStatus",
     "KKTErrors", "ConvergenceStats", "OPTIMAL", "TIME_LIMIT", "ITERATION_LIMIT",
     "STILL_RUNNING", "DimensionMismatch", "ArgumentError", "CpdlpError", "CSCMatrix",
+    "sort_rows_columns",
 ]

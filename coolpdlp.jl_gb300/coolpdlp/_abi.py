@@ -165,7 +165,7 @@ EXPORTED_SYMBOLS = (
     "cpdlp_state_kernel_bytes", "cpdlp_spmv_csr_noalloc",
     "cpdlp_submit", "cpdlp_poll", "cpdlp_wait", "cpdlp_cancel", "cpdlp_collect",
     "cpdlp_job_count", "cpdlp_job_destroy", "cpdlp_batch_footprint", "cpdlp_job_ready",
-    "cpdlp_collect_lp",
+    "cpdlp_collect_lp", "cpdlp_sort_rows_columns",
 )
 
 _LIB = None
@@ -223,6 +223,8 @@ def _declare(lib):
         "cpdlp_collect_lp": (c_int32, [H, H, c_int64, PD, PD, POINTER(StatsC)]),
         "cpdlp_job_destroy": (c_int32, [H]),
         "cpdlp_batch_footprint": (c_int64, [c_int64, POINTER(LPC), POINTER(ParamsC)]),
+        "cpdlp_sort_rows_columns": (c_int32, [H, POINTER(LPC), P64, P64, P64, P64, PD, PD, PD,
+                                              PD, PD, PD]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

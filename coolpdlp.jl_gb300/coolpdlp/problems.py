@@ -216,3 +216,34 @@ def is_feasible(x, milp: MILP, cons_tol: float = 1e-6, int_tol: float = 1e-5,
 def objective_value(x, milp: MILP) -> float:
     """solution.jl:40"""
     return float(np.dot(np.asarray(x, dtype=np.float64), milp.c))
+
+
+def sort_rows_columns(milp: MILP) -> MILP:
+    """sort_rows_columns(milp) (permutation.jl:16-46): a new MILP whose variables
+    are ordered by increasing column length and whose constraints by increasing
+    row length (stable), through cpdlp_sort_rows_columns."""
+    from ctypes import byref
+    from . import native
+    m, n, nnz = milp.A.m, milp.A.n, milp.A.nnz
+    lp = native.LPStruct(m, n, milp.A.colptr, milp.A.rowval, milp.A.nzval, milp.c, milp.lv,
+                         milp.uv, milp.lc, milp.uc)
+    pv = np.empty(max(n, 1), dtype=np.int64)
+    pc = np.empty(max(m, 1), dtype=np.int64)
+    colptr = np.empty(n + 1, dtype=np.int64)
+    rowval = np.empty(max(nnz, 1), dtype=np.int64)
+    nzval = np.empty(max(nnz, 1))
+    c, lv, uv = np.empty(max(n, 1)), np.empty(max(n, 1)), np.empty(max(n, 1))
+    lc, uc = np.empty(max(m, 1)), np.empty(max(m, 1))
+    lib = A.load_library()
+    rc = lib.cpdlp_sort_rows_columns(None, byref(lp.s), native._p64(pv), native._p64(pc),
+                                     native._p64(colptr), native._p64(rowval), native._pd(nzval),
+                                     native._pd(c), native._pd(lv), native._pd(uv),
+                                     native._pd(lc), native._pd(uc))
+    if rc != A.OK:
+        A.raise_for(rc, "sort_rows_columns: invalid LP")
+    pv, pc = pv[:n] - 1, pc[:m] - 1
+    return MILP(c=c[:n], lv=lv[:n], uv=uv[:n],
+                A=CSCMatrix(m, n, colptr, rowval[:nnz], nzval[:nnz]), lc=lc[:m], uc=uc[:m],
+                D1=milp.D1[pc], D2=milp.D2[pv], int_var=milp.int_var[pv],
+                var_names=[milp.var_names[j] for j in pv], dataset=milp.dataset, name=milp.name,
+                path=milp.path)

@@ -8,6 +8,7 @@
 #include "tiles.cuh"
 #include "matrix.cuh"
 #include "noalloc.cuh"
+#include "permutation.cuh"
 #include "solver.cuh"
 
 using namespace cpdlp;
@@ -184,6 +185,18 @@ int cpdlp_spmv_csr_noalloc(cpdlp_handle* h, int64_t m, int64_t n, int64_t nnz,
     NEED(h);
     return guarded(h, [&] {
         spmv_csr_noalloc(*H(h), m, n, nnz, rowptr, colval, nzval, value_type, b, c, alpha, beta);
+    });
+}
+
+int cpdlp_sort_rows_columns(cpdlp_handle* h, const cpdlp_lp* lp, int64_t* perm_var,
+                            int64_t* perm_cons, int64_t* colptr, int64_t* rowval, double* nzval,
+                            double* c, double* lv, double* uv, double* lc, double* uc) {
+    if (!lp) {
+        if (h) h->last_error = "null LP";
+        return CPDLP_ERR_ARGUMENT;
+    }
+    return guarded(h, [&] {
+        sort_rows_columns(*lp, perm_var, perm_cons, colptr, rowval, nzval, c, lv, uv, lc, uc);
     });
 }
 

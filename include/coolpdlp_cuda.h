@@ -235,6 +235,20 @@ int cpdlp_matrix_export(cpdlp_handle* h, const cpdlp_matrix* A, int64_t* ptr,
 int cpdlp_spmv(cpdlp_handle* h, const cpdlp_matrix* A, const void* b, void* c,
                double alpha, double beta);
 
+/* sort_rows_columns(milp) (src/components/permutation.jl:1-46): the LP with
+ * its variables ordered by increasing column length and its constraints by
+ * increasing row length (stable: ties keep their index order, as Julia's
+ * sortperm).  perm_var (n) / perm_cons (m) receive the 1-based permutations
+ * (new position k holds old index perm[k]); colptr (n+1), rowval (nnz), nzval
+ * (nnz) the permuted CSC A[perm_cons, perm_var], rows ascending per column;
+ * c, lv, uv (n) and lc, uc (m) the permuted vectors.  Every output may be NULL.
+ * Host computation (the reference runs it on the CPU and solve never calls
+ * it); h may be NULL, and then only the status code reports an error. */
+int cpdlp_sort_rows_columns(cpdlp_handle* h, const cpdlp_lp* lp, int64_t* perm_var,
+                            int64_t* perm_cons, int64_t* colptr, int64_t* rowval,
+                            double* nzval, double* c, double* lv, double* uv, double* lc,
+                            double* uc);
+
 /* ---- solve path (src/algorithms/common.jl, pdlp.jl, pdhg.jl) ----------- */
 
 /* preprocess(milp, sol, algo) (common.jl:154-169): Ruiz + Pock-Chambolle

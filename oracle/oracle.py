@@ -308,3 +308,22 @@ def gaussian_vector(seed: int, n: int) -> np.ndarray:
 
 def scalar(name, *args):
     return getattr(lib(), "orc_" + name)(*args)
+
+
+def sort_rows_columns(lp):
+    """sort_rows_columns (src/components/permutation.jl:1-46) restated with
+    numpy/scipy: perm_var = stable sortperm of the column lengths of A
+    (increasing_column_order, :1-4), perm_cons = the same for A' (its column
+    lengths are A's row lengths); the permuted matrix is A[perm_cons, perm_var]
+    (permute_rows_columns, :6-14).  Returns 0-based permutations and the 1-based
+    CSC arrays with rows ascending per column."""
+    import scipy.sparse as sp
+    A_ = sp.csc_matrix((lp.nzval, lp.rowval - 1, lp.colptr - 1), shape=(lp.m, lp.n))
+    collen = np.diff(lp.colptr)
+    rowlen = np.bincount(lp.rowval - 1, minlength=lp.m) if lp.nnz else np.zeros(lp.m, np.int64)
+    pv = np.argsort(collen, kind="stable")
+    pc = np.argsort(rowlen, kind="stable")
+    B = A_[pc][:, pv].tocsc()
+    B.sort_indices()
+    return (pv, pc, B.indptr.astype(np.int64) + 1, B.indices.astype(np.int64) + 1,
+            B.data.astype(np.float64))
