@@ -119,6 +119,23 @@ class MILP:
                    A=CSCMatrix(lp.m, lp.n, lp.colptr, lp.rowval, lp.nzval), lc=lp.lc, uc=lp.uc,
                    name=kw.pop("name", getattr(lp, "name", "")), **kw)
 
+    @classmethod
+    def from_qps(cls, qps, **kw) -> "MILP":
+        """MILP(qps::QPSData) (milp.jl:117-136): A = sparse(arows, acols, avals)
+        (duplicate entries summed, as Julia's sparse does), int_var from the
+        Binary / Integer variable types, var_names from the QPS names.  The
+        objective constant and sense are not carried, as in the reference."""
+        import scipy.sparse as sp
+        from .qps import VTYPE_Binary, VTYPE_Integer
+        m, n = len(qps.lcon), len(qps.lvar)
+        A_ = sp.coo_matrix((qps.avals, (qps.arows - 1, qps.acols - 1)), shape=(m, n)).tocsc()
+        A_.sum_duplicates()
+        A_.sort_indices()
+        vt = np.asarray(qps.vartypes, dtype=np.int64)
+        return cls(c=qps.c, lv=qps.lvar, uv=qps.uvar, A=A_, lc=qps.lcon, uc=qps.ucon,
+                   int_var=(vt == VTYPE_Binary) | (vt == VTYPE_Integer),
+                   var_names=list(qps.varnames), name=kw.pop("name", qps.name), **kw)
+
     def __repr__(self):
         return (f"MILP instance {self.name} from dataset {self.dataset}:\n"
                 f"- variables: {nbvar(self)}\n  - {nbvar_cont(self)} continuous\n"
