@@ -188,55 +188,66 @@ def cpu_baseline(lp, budget_s: float = 20.0) -> dict:
                        f"{t_setup:.1f} s of untimed preprocessing"), "seconds": t}
 
 
-def measure_batch(h, count: int, sample: int, m_hi: int = 5000) -> dict:
+def measure_batch(h, count: int, sample: int, m_hi: int = 5000, rank: int = 0, world: int = 1,
+                  device=None) -> dict:
     """LPs/s to 1e-4 relative KKT on `count` random sparse LPs (m log-U[50,5000],
     n = 2m, 3-8 nonzeros per column, seed 1000 + i): the batched solver with
     FP32 iterates (stalled FP32 LPs finish in its FP64 phase) and with FP64
     iterates, against the plain FP64 one-LP-at-a-time path (cpdlp_solve) on an
     evenly spaced sample of the same LPs.  Every result's relative KKT error
-    is read back and checked; objectives are compared with the FP64 batch."""
+    is read back and checked; objectives are compared with the FP64 batch.
+    Under torchrun every rank solves its shard (index = rank mod world) and the
+    LPs/s figures use the slowest rank's time; the sample runs on rank 0."""
     import numpy as np
     from coolpdlp import _abi as A
     from coolpdlp import generators as G
     from coolpdlp import native
-    lps = G.batch_lps(count, m_hi=m_hi)
+    from coolpdlp.distributed import reduce_over_ranks, shard_indices
+    all_lps = G.batch_lps(count, m_hi=m_hi)
+    lps = [all_lps[k] for k in shard_indices(count, rank, world)]
     S = [native.LPStruct(lp.m, lp.n, lp.colptr, lp.rowval, lp.nzval, lp.c, lp.lv, lp.uv, lp.lc,
                          lp.uc) for lp in lps]
     warm = native.default_params()
     native.batch_solve(h, S[:4], warm)          # loads the kernels
-    out = {"lps": count, "nnz_total": int(sum(lp.nnz for lp in lps))}
+    out = {"lps": count, "nnz_total": int(sum(lp.nnz for lp in all_lps)), "ranks": world}
     res = {}
     for name, ft in (("fp32_refined", A.VAL_F32), ("fp64_batched", A.VAL_F64)):
         p = native.default_params()
         p.float_type = ft
         t0 = time.perf_counter()
         xs, ys, st = native.batch_solve(h, S, p)
-        dt = time.perf_counter() - t0
+        dt = reduce_over_ranks(time.perf_counter() - t0, "max", device)
         rel = np.array([max(s.err.primal / s.err.primal_scale, s.err.dual / s.err.dual_scale,
                             s.err.gap / s.err.gap_scale) for s in st])
         res[name] = xs
         te = np.array([s.time_elapsed for s in st])
         out[name] = {"lps_per_s": count / dt, "seconds": dt,
-                     "lp_seconds_sum": float(te.sum()), "lp_seconds_max": float(te.max()),
+                     "lp_seconds_sum": reduce_over_ranks(float(te.sum()), "sum", device),
+                     "lp_seconds_max": reduce_over_ranks(float(te.max()), "max", device),
                      "setup_seconds": float(st[0].setup_seconds),
-                     "optimal": int(sum(s.termination_status == 0 for s in st)),
-                     "max_rel_kkt": float(np.nanmax(rel)),
-                     "fp64_phase_lps": int(sum(s.refine_kkt_passes > 0 for s in st)),
-                     "mean_passes": float(np.mean([s.kkt_passes for s in st]))}
+                     "optimal": int(reduce_over_ranks(
+                         sum(s.termination_status == 0 for s in st), "sum", device)),
+                     "max_rel_kkt": reduce_over_ranks(float(np.nanmax(rel)), "max", device),
+                     "fp64_phase_lps": int(reduce_over_ranks(
+                         sum(s.refine_kkt_passes > 0 for s in st), "sum", device)),
+                     "mean_passes": reduce_over_ranks(
+                         float(np.sum([s.kkt_passes for s in st])), "sum", device) / count}
     obj = lambda k, x: float(np.dot(lps[k].c, x))
-    out["max_obj_rel_diff_fp32_vs_fp64"] = float(max(
+    out["max_obj_rel_diff_fp32_vs_fp64"] = reduce_over_ranks(float(max(
         abs(obj(k, res["fp32_refined"][k]) - obj(k, res["fp64_batched"][k]))
-        / max(1.0, abs(obj(k, res["fp64_batched"][k]))) for k in range(count)))
+        / max(1.0, abs(obj(k, res["fp64_batched"][k]))) for k in range(len(lps)))), "max", device)
     out["workload"] = (f"{count} random sparse LPs, m log-U[50,{m_hi}], n=2m, 3-8 nnz/column, "
                        "seed 1000+i, 1e-4 relative KKT")
-    if sample <= 0:
+    if sample <= 0 or rank != 0:
         return out
     idx = list(range(0, count, max(1, count // max(sample, 1))))[:sample]
     p = native.default_params()
     t0 = time.perf_counter()
     passes = 0
     for k in idx:
-        _, _, s1 = native.solve_lp(h, S[k], p)
+        lp = all_lps[k]
+        _, _, s1 = native.solve_lp(h, native.LPStruct(lp.m, lp.n, lp.colptr, lp.rowval, lp.nzval,
+                                                      lp.c, lp.lv, lp.uv, lp.lc, lp.uc), p)
         passes += s1.kkt_passes
     dt = time.perf_counter() - t0
     seq = len(idx) / dt
@@ -410,11 +421,11 @@ def run_ours(args):
         return
     if args.only_batch:
         # the batched workload alone (small cases for profilers); no headline value
+        h = native.Handle(local)
+        b = measure_batch(h, args.batch_lps, args.sequential_sample, args.batch_m_hi, rank, ws,
+                          torch.device("cuda", local))
         if rank == 0:
-            h = native.Handle(local)
-            print(json.dumps({"metric": METRIC, "impl": "ours", "value": None,
-                              "batch": measure_batch(h, args.batch_lps, args.sequential_sample,
-                                                     args.batch_m_hi)}),
+            print(json.dumps({"metric": METRIC, "impl": "ours", "value": None, "batch": b}),
                   flush=True)
         return
     lp = workload(args.scale)
@@ -529,6 +540,11 @@ def run_ours(args):
     h2d = (lp.n + 1) * 8 + lp.nnz * 16 + (3 * lp.n + 2 * lp.m) * 8
     d2h = (lp.n + lp.m) * 8 + ctypes.sizeof(A.StatsC)
 
+    # the batched LPs shard over the ranks (every rank takes part)
+    batch = None
+    if args.batch_lps > 0:
+        batch = measure_batch(h, args.batch_lps, args.sequential_sample, args.batch_m_hi, rank,
+                              ws, torch.device("cuda", local))
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -549,9 +565,8 @@ def run_ours(args):
         if args.flow_side > 0:
             line["flow"] = measure_flow(h, args.flow_side, args.flow_k,
                                         solves=not args.flow_no_solve)
-        if args.batch_lps > 0:
-            line["batch"] = measure_batch(h, args.batch_lps, args.sequential_sample,
-                                          args.batch_m_hi)
+        if batch is not None:
+            line["batch"] = batch
         if args.serve_requests > 0:
             line["serving"] = measure_serving(args.serve_requests, args.serve_rate)
         print(json.dumps(line), flush=True)
