@@ -48,6 +48,9 @@ constexpr int BATCH_RPL = 1;    // rows per lane: short tiles of at most 32 rows
 // cluster of CLUSTER_CTAS CTAs instead of one CTA
 constexpr int CLUSTER_CTAS = 8;
 constexpr int64_t CLUSTER_MIN_NNZ = 24000;
+// In the FP64 phase (few LPs, the tail of a job) the threshold is lower: a
+// single CTA takes seconds on the slowest stalled LPs while most SMs are idle
+constexpr int64_t PHASE_CLUSTER_MIN_NNZ = 4000;
 
 #ifndef CPDLP_BATCH_MINB
 #define CPDLP_BATCH_MINB 2      // resident CTAs per SM the solve kernel is compiled for
@@ -947,10 +950,12 @@ struct Run : RunBase {
             return nz_off[a + 1] - nz_off[a] > nz_off[b + 1] - nz_off[b];
         });
         // largest first: the first nbig LPs of the order go to the cluster kernel
-        // (the routing depends on the LP alone, so its arithmetic does too)
+        // (the routing depends on the LP and its phase alone, so its arithmetic
+        // does too)
+        const int64_t cmin = phase == 2 ? PHASE_CLUSTER_MIN_NNZ : CLUSTER_MIN_NNZ;
         int64_t nbig = 0;
         if (nclusters > 0 && nclusters_p > 0)
-            while (nbig < count && nz_off[order[nbig] + 1] - nz_off[order[nbig]] >= CLUSTER_MIN_NNZ) nbig++;
+            while (nbig < count && nz_off[order[nbig] + 1] - nz_off[order[nbig]] >= cmin) nbig++;
         // power-method start vectors: the single-LP generator, per LP from counter 0
         std::vector<double> xs((size_t)std::max<int64_t>(N, 1));
         for (int64_t k = 0; k < count; k++) {
