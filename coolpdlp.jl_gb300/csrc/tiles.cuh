@@ -124,13 +124,6 @@ __device__ __forceinline__ void load4v(const double* p, T (&o)[4]) {
     asm volatile("ld.global.cs.v2.f64 {%0, %1}, [%2];" : "=d"(c), "=d"(d) : "l"(p + 2));
     o[0] = (T)a; o[1] = (T)b; o[2] = (T)c; o[3] = (T)d;
 }
-template <class T>
-__device__ __forceinline__ void load4v(const int8_t* p, T (&o)[4]) {
-    int v;
-    asm volatile("ld.global.cs.s32 %0, [%1];" : "=r"(v) : "l"(p));
-    o[0] = (T)(int8_t)(v & 0xff); o[1] = (T)(int8_t)((v >> 8) & 0xff);
-    o[2] = (T)(int8_t)((v >> 16) & 0xff); o[3] = (T)(int8_t)((v >> 24) & 0xff);
-}
 // gathers of x[col]: through the read-only path (COH = false) or with a
 // coherent load (COH = true); same ordering property as the loads above
 template <bool COH>
@@ -150,14 +143,6 @@ __device__ __forceinline__ double gather(const double* p) {
 template <class V, class T>
 __device__ __forceinline__ T load1v(const V* p) {
     return (T)__ldcs(p);
-}
-template <>
-__device__ __forceinline__ float load1v<int8_t, float>(const int8_t* p) {
-    return (float)__ldcs(reinterpret_cast<const signed char*>(p));
-}
-template <>
-__device__ __forceinline__ double load1v<int8_t, double>(const int8_t* p) {
-    return (double)__ldcs(reinterpret_cast<const signed char*>(p));
 }
 
 template <class T>
