@@ -127,11 +127,10 @@ struct DualEpi {
     T* __restrict__ ysn;         // SCALED: d1 .* y+
     const double* __restrict__ yoff;  // SHIFT: scaled base multipliers
     using Acc = NoAcc;
-    struct Pre { T y, lc, uc, ya, d; double yo; };
+    struct Pre { T y, lc, uc, ya, d; };
     __device__ __forceinline__ Pre pre_global(int i) const {
         return Pre{ld_stream(y + i), ld_stream(lc + i), ld_stream(uc + i),
-                   avg ? ld_stream(ya_old + i) : T(0), SCALED ? ld_stream(dsc + i) : T(0),
-                   SHIFT ? ld_stream(yoff + i) : 0.0};
+                   avg ? ld_stream(ya_old + i) : T(0), SCALED ? ld_stream(dsc + i) : T(0)};
     }
     __device__ void init(Acc&) {}
     __device__ __forceinline__ void row(int, int i, T s, const Pre& q, Acc&) {
@@ -140,8 +139,11 @@ struct DualEpi {
         const T sigma = k.sigma;
         T yp;
         if constexpr (SHIFT) {
+            // read here, not prefetched with the row's other inputs: an FP64
+            // value per prefetched row doubled the kernel's registers
+            const double yo = ld_stream(yoff + i);
             const double sd = (double)s, sg = (double)sigma;
-            const double t4 = __dsub_rn(__dmul_rn((double)k.inv_sigma, __dadd_rn(q.yo, (double)q.y)), sd);
+            const double t4 = __dsub_rn(__dmul_rn((double)k.inv_sigma, __dadd_rn(yo, (double)q.y)), sd);
             const double pr = proj_box(t4, -(double)q.uc, -(double)q.lc);
             yp = (T)__dsub_rn(__dsub_rn((double)q.y, __dmul_rn(sg, sd)), __dmul_rn(sg, pr));
         } else {
