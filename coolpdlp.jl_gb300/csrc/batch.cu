@@ -52,9 +52,21 @@ constexpr int64_t CLUSTER_MIN_NNZ = 24000;
 // single CTA takes seconds on the slowest stalled LPs while most SMs are idle
 constexpr int64_t PHASE_CLUSTER_MIN_NNZ = 4000;
 
-#ifndef CPDLP_BATCH_MINB
-#define CPDLP_BATCH_MINB 2      // resident CTAs per SM the solve kernel is compiled for
+// resident CTAs per SM the solve kernel is compiled for (registers = 65536 /
+// (256 threads x this)).  Each CTA's solve is a latency-bound chain of
+// dependent half-steps, so more resident CTAs beat fewer spills: with 4
+// (64 registers, some spilled to L1) the 4,096-LP FP32 batch takes 2.3 s
+// against 3.0 s with 2 (128 registers, no spills).
+#ifndef CPDLP_BATCH_MINB_F32
+#define CPDLP_BATCH_MINB_F32 4
 #endif
+#ifndef CPDLP_BATCH_MINB_F64
+#define CPDLP_BATCH_MINB_F64 4
+#endif
+template <class T>
+constexpr int batch_min_blocks() {
+    return std::is_same<T, float>::value ? CPDLP_BATCH_MINB_F32 : CPDLP_BATCH_MINB_F64;
+}
 
 struct BatchLP {
     int32_t m, n, row_off, col_off;
@@ -650,7 +662,7 @@ __global__ void __launch_bounds__(BT) k_batch_power(PowerArgs<V> g) {
 // other CTAs copy both from it, so every CTA of a group leaves the loop at the
 // same LP.
 template <int ITEMS, class T, int CS>
-__global__ void __launch_bounds__(BT, CPDLP_BATCH_MINB) k_batch_pdlp(BatchArgs<T> g) {
+__global__ void __launch_bounds__(BT, batch_min_blocks<T>()) k_batch_pdlp(BatchArgs<T> g) {
     __shared__ T prod[BW * 32 * ITEMS];
     __shared__ double sh[BW * 8 + 8];
     __shared__ BatchCtl C;
