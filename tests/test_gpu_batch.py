@@ -19,7 +19,7 @@ pytestmark = pytest.mark.gpu
 
 def _set(count=20, seed0=500):
     """Small random LPs (one CTA each), the reference suite's two tiny LPs, a
-    flow LP, and two LPs above 24,000 nonzeros (a thread-block cluster each)."""
+    flow LP, and two LPs above 12,000 nonzeros (a thread-block cluster each)."""
     from coolpdlp import generators as G
     lps = G.batch_lps(count, m_lo=40, m_hi=400, seed0=seed0)
     lps.append(G.two_variable_lp())
