@@ -26,6 +26,7 @@
 #include <algorithm>
 #include <memory>
 #include <numeric>
+#include <thread>
 #include <type_traits>
 
 #include <cooperative_groups.h>
@@ -35,6 +36,25 @@
 #include "solver.cuh"
 
 namespace cpdlp {
+
+namespace {
+// f(k) for k in [0, count) on up to 16 host threads (contiguous blocks of k)
+template <class F>
+void parallel_for(int64_t count, F&& f) {
+    const int64_t hw = std::max<int64_t>(1, std::min<int64_t>(16, std::thread::hardware_concurrency()));
+    const int64_t nt = std::min<int64_t>(hw, std::max<int64_t>(1, count / 64));
+    if (nt <= 1) {
+        for (int64_t k = 0; k < count; k++) f(k);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (int64_t t = 0; t < nt; t++)
+        th.emplace_back([&, t] {
+            for (int64_t k = count * t / nt; k < count * (t + 1) / nt; k++) f(k);
+        });
+    for (auto& x : th) x.join();
+}
+}  // namespace
 
 namespace {
 
@@ -901,7 +921,8 @@ struct Run : RunBase {
         std::vector<double> nzval(rowval.size()), c((size_t)std::max<int64_t>(N, 1)),
             lv(c.size()), uv(c.size()), lc((size_t)std::max<int64_t>(M, 1)), uc(lc.size());
         colptr[0] = 1;
-        for (int64_t k = 0; k < count; k++) {
+        // each LP's slices are disjoint: host threads copy LPs in parallel
+        parallel_for(count, [&](int64_t k) {
             const cpdlp_lp& L = all[lps[k].id].v;
             for (int64_t j = 0; j < L.n; j++) colptr[col_off[k] + j + 1] = nz_off[k] + L.colptr[j + 1];
             for (int64_t q = 0; q < L.nnz; q++) {
@@ -917,16 +938,14 @@ struct Run : RunBase {
                 std::copy(L.lc, L.lc + L.m, lc.begin() + row_off[k]);
                 std::copy(L.uc, L.uc + L.m, uc.begin() + row_off[k]);
             }
-        }
+        });
         cpdlp_lp big{M, N, NZ, colptr.data(), rowval.data(), nzval.data(), c.data(), lv.data(),
                      uv.data(), lc.data(), uc.data()};
         // the batched kernels read the scaled values (no narrow +-1 storage)
-        // and cut their own tile plans at LP boundaries (no autotuning of the
-        // concatenation's plans)
+        // and cut their own tile plans at LP boundaries (the problem builds none)
         cpdlp_params pprm = prm;
         pprm.tile_flags |= CPDLP_TILE_NO_NARROW;
-        if (pprm.tile_nnz == 0) pprm.tile_nnz = 32 * BATCH_ITEMS;
-        PB.reset(problem_create(rh, &big, &pprm));
+        PB.reset(problem_create(rh, &big, &pprm, false));
         auto& P = static_cast<ProblemT<T>&>(*PB);
         // tile plans with LP boundaries
         std::vector<int32_t> hpA((size_t)M + 1), hpAt((size_t)N + 1);
@@ -979,17 +998,21 @@ struct Run : RunBase {
         int64_t nbig = 0;
         if (nclusters > 0 && nclusters_p > 0)
             while (nbig < count && nz_off[order[nbig] + 1] - nz_off[order[nbig]] >= cmin) nbig++;
-        // power-method start vectors: the single-LP generator, per LP from counter 0
-        std::vector<double> xs((size_t)std::max<int64_t>(N, 1));
-        for (int64_t k = 0; k < count; k++) {
-            for (int64_t j = 0; j < col_off[k + 1] - col_off[k]; j++) {
-                const double u1 = (double)((splitmix64_at_host(prm.power_seed, 2 * (uint64_t)j) >> 11) + 1) *
-                                  (1.0 / 9007199254740992.0);
-                const double u2 = (double)((splitmix64_at_host(prm.power_seed, 2 * (uint64_t)j + 1) >> 11) + 1) *
-                                  (1.0 / 9007199254740992.0);
-                xs[(size_t)(col_off[k] + j)] = std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
-            }
+        // power-method start vectors: the single-LP generator, per LP from counter
+        // 0, so every LP's vector is a prefix of one vector (computed once)
+        int64_t nmax = 0;
+        for (int64_t k = 0; k < count; k++) nmax = std::max(nmax, col_off[k + 1] - col_off[k]);
+        std::vector<double> g0((size_t)nmax);
+        for (int64_t j = 0; j < nmax; j++) {
+            const double u1 = (double)((splitmix64_at_host(prm.power_seed, 2 * (uint64_t)j) >> 11) + 1) *
+                              (1.0 / 9007199254740992.0);
+            const double u2 = (double)((splitmix64_at_host(prm.power_seed, 2 * (uint64_t)j + 1) >> 11) + 1) *
+                              (1.0 / 9007199254740992.0);
+            g0[(size_t)j] = std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
         }
+        std::vector<double> xs((size_t)std::max<int64_t>(N, 1));
+        for (int64_t k = 0; k < count; k++)
+            std::copy(g0.begin(), g0.begin() + (col_off[k + 1] - col_off[k]), xs.begin() + col_off[k]);
         const size_t nz = (size_t)std::max<int64_t>(N, 1), mz = (size_t)std::max<int64_t>(M, 1);
         std::vector<double> hx0, hy0;
         if (any_warm) {

@@ -390,7 +390,7 @@ void fetch_reduced(Handle& h, const double* part, int64_t rows, int q, double* d
 // problem creation: preprocess (common.jl:154-169) on the device
 // ---------------------------------------------------------------------------
 template <class T>
-ProblemBase* make_problem(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm) {
+ProblemBase* make_problem(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm, bool plans) {
     double t0 = now_seconds();
     cudaStream_t s = h.stream;
     auto* P = new ProblemT<T>();
@@ -522,6 +522,13 @@ ProblemBase* make_problem(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm
     }
     P->D1 = std::move(D1);
     P->D2 = std::move(D2);
+    if (!plans) {  // the batched solver partitions the matrices itself
+        P->zero_cost = false;
+        CK(cudaStreamSynchronize(s));
+        P->setup_seconds = now_seconds() - t0;
+        guard.release();
+        return P;
+    }
     // tile plans from the row pointers
     std::vector<int32_t> hp2((size_t)m + 1), hp1((size_t)n + 1);
     CK(cudaMemcpyAsync(hp2.data(), P->a_ptr.p, sizeof(int32_t) * (m + 1), cudaMemcpyDeviceToHost, s));
@@ -1572,11 +1579,11 @@ void StateBase::stats(cpdlp_stats* st) const {
     st->kernel_launches = launches;
 }
 
-ProblemBase* problem_create(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm) {
+ProblemBase* problem_create(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm, bool plans) {
     if (!lp || !prm) fail(CPDLP_ERR_ARGUMENT, "null lp or params");
     if (lp->m < 0 || lp->n < 0) fail(CPDLP_ERR_DIMENSION, "negative problem size");
-    if (prm->float_type == CPDLP_VAL_F32) return make_problem<float>(h, lp, prm);
-    if (prm->float_type == CPDLP_VAL_F64) return make_problem<double>(h, lp, prm);
+    if (prm->float_type == CPDLP_VAL_F32) return make_problem<float>(h, lp, prm, plans);
+    if (prm->float_type == CPDLP_VAL_F64) return make_problem<double>(h, lp, prm, plans);
     fail(CPDLP_ERR_ARGUMENT, "float_type must be CPDLP_VAL_F64 or CPDLP_VAL_F32");
 }
 

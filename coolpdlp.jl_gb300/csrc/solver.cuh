@@ -93,7 +93,10 @@ struct StateBase {
     void stats(cpdlp_stats* st) const;
 };
 
-ProblemBase* problem_create(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm);
+// plans = false: scaling and device arrays only, no tile plans, reduction
+// scratch or constant scales (the batched solver builds its own plans)
+ProblemBase* problem_create(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm,
+                            bool plans = true);
 // eta0 > 0 / omega0 > 0 continue an earlier solve of the same LP: the step size
 // (no power method) and the primal weight start from these values
 StateBase* state_create(Handle& h, ProblemBase* P, const cpdlp_params* prm, const double* x0,
