@@ -1648,8 +1648,8 @@ void solve_full(Handle& h, const cpdlp_lp* lp, const cpdlp_params* params, const
     }
     // Refinement on the residual LP: FP32 rounds from the FP32 solution, with
     // the residuals, the combination and the KKT errors in FP64 (the step size
-    // is a property of A and carries over; so does the adapted primal weight
-    // after a converged FP32 phase)
+    // is a property of A and carries over, and the rounds start from the FP32
+    // run's primal weight)
     cpdlp_stats st32;
     S->stats(&st32);
     const double eta32 = S->eta, omega32 = S->omega;
@@ -1710,8 +1710,10 @@ void solve_full(Handle& h, const cpdlp_lp* lp, const cpdlp_params* params, const
     S64.reset();
     P.reset();
     p64.max_kkt_passes = std::max<int64_t>(params->max_kkt_passes - passes, 1);
+    // the primal weight starts cold (primal_weight_init): the FP32 run's and
+    // the rounds' weights belong to iterates that stopped making progress
     std::unique_ptr<StateBase> C64(
-        state_create(h, P64.get(), &p64, xs.data(), ys.data(), eta32, stalled ? 0.0 : R.omega));
+        state_create(h, P64.get(), &p64, xs.data(), ys.data(), eta32, 0.0));
     C64->starting_time = t0;
     C64->solve();
     C64->solution(x_out, y_out);
