@@ -28,6 +28,8 @@ ERR_UNSUPPORTED = 7
 
 # enums
 OPTIMAL, TIME_LIMIT, ITERATION_LIMIT, STILL_RUNNING = 0, 1, 2, 3
+# extensions (infeasibility_tol > 0)
+PRIMAL_INFEASIBLE, DUAL_INFEASIBLE = 4, 5
 ALGO_PDLP, ALGO_PDHG = 0, 1
 VAL_F64, VAL_F32, VAL_PM1 = 0, 1, 2
 # tile_flags bits: CPDLP_TILE_NO_NARROW keeps scaled values for a +-1 matrix
@@ -65,6 +67,7 @@ class ParamsC(Structure):
         ("refine_reltol", c_double),
         ("tile_nnz", c_int32),
         ("tile_flags", c_int32),
+        ("infeasibility_tol", c_double),
     ]
 
 
@@ -122,6 +125,7 @@ def default_params_py(algorithm: int = ALGO_PDLP) -> ParamsC:
     p.refine_reltol = 0.0
     p.tile_nnz = 0
     p.tile_flags = 0
+    p.infeasibility_tol = 0.0
     return p
 
 

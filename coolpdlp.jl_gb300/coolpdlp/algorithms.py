@@ -24,6 +24,9 @@ class TerminationStatus(enum.IntEnum):
     TIME_LIMIT = A.TIME_LIMIT
     ITERATION_LIMIT = A.ITERATION_LIMIT
     STILL_RUNNING = A.STILL_RUNNING
+    # extensions of this library (infeasibility_tol > 0); the reference has none
+    PRIMAL_INFEASIBLE = A.PRIMAL_INFEASIBLE
+    DUAL_INFEASIBLE = A.DUAL_INFEASIBLE
 
 
 OPTIMAL = TerminationStatus.OPTIMAL
@@ -105,7 +108,7 @@ class Algorithm:
                 "zero_tol", "sufficient_decay", "necessary_decay", "artificial_decay",
                 "show_progress", "check_every", "record_error_history", "termination_reltol",
                 "max_kkt_passes", "time_limit", "power_tol_override", "power_maxiter_override",
-                "power_seed", "refine_reltol", "tile_nnz", "tile_flags")
+                "power_seed", "refine_reltol", "tile_nnz", "tile_flags", "infeasibility_tol")
 
     def __init__(self, name: str = "PDLP", T=np.float64, Ti=np.int64, M="CSR", *, device: int = 0,
                  backend=None, **kw):

@@ -39,12 +39,15 @@ class TerminationStatusCode(enum.Enum):
     TIME_LIMIT = "TIME_LIMIT"
     ITERATION_LIMIT = "ITERATION_LIMIT"
     OTHER_ERROR = "OTHER_ERROR"
+    INFEASIBLE = "INFEASIBLE"            # infeasibility_tol > 0 only
+    DUAL_INFEASIBLE = "DUAL_INFEASIBLE"  # infeasibility_tol > 0 only
 
 
 class ResultStatusCode(enum.Enum):
     UNKNOWN_RESULT_STATUS = "UNKNOWN_RESULT_STATUS"
     FEASIBLE_POINT = "FEASIBLE_POINT"
     NO_SOLUTION = "NO_SOLUTION"
+    INFEASIBILITY_CERTIFICATE = "INFEASIBILITY_CERTIFICATE"
 
 
 class Sense(enum.Enum):
@@ -292,6 +295,14 @@ class Optimizer:
             ts, ps, ds = (TerminationStatusCode.ITERATION_LIMIT,
                           ResultStatusCode.UNKNOWN_RESULT_STATUS,
                           ResultStatusCode.UNKNOWN_RESULT_STATUS)
+        elif cts == alg.TerminationStatus.PRIMAL_INFEASIBLE:
+            # extension: the returned y is the dual ray
+            ts, ps, ds = (TerminationStatusCode.INFEASIBLE, ResultStatusCode.NO_SOLUTION,
+                          ResultStatusCode.INFEASIBILITY_CERTIFICATE)
+        elif cts == alg.TerminationStatus.DUAL_INFEASIBLE:
+            # extension: the returned x is the primal ray
+            ts, ps, ds = (TerminationStatusCode.DUAL_INFEASIBLE,
+                          ResultStatusCode.INFEASIBILITY_CERTIFICATE, ResultStatusCode.NO_SOLUTION)
         else:
             assert cts == alg.STILL_RUNNING
             ts, ps, ds = (TerminationStatusCode.OTHER_ERROR, ResultStatusCode.NO_SOLUTION,

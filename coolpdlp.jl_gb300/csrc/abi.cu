@@ -73,6 +73,7 @@ void cpdlp_params_default(cpdlp_params* p, int32_t algorithm) {
     p->power_seed = 0;
     p->refine_reltol = 0.0;
     p->tile_nnz = 0;
+    p->infeasibility_tol = 0.0;
 }
 
 int cpdlp_create(int32_t device, cpdlp_handle** out) {

@@ -252,6 +252,94 @@ struct KktColEpi {
     __device__ void finish(Acc& a) { block_reduce_store<3 * NV>(a.v, block_out); }
 };
 
+// Infeasibility certificates (an extension; the reference has no detection).
+// Row side, primal ray x: s = (A x)_i (SCALED: the product gathered D2 x and s
+// is multiplied by d1_i); accumulates the squared distance of s to the
+// recession cone of [lc_i, uc_i] and the dual ray y's row objective
+// (lc_i y_i for y_i > 0, uc_i y_i for y_i < 0; y's signs are already those
+// the bounds allow).
+template <class T, bool SCALED = false>
+struct RayRowEpi {
+    const T* __restrict__ lc;
+    const T* __restrict__ uc;
+    const double* __restrict__ ry;
+    const double* __restrict__ dsc;
+    double* block_out;
+    double* long_out;
+    struct Acc { double v[2]; };
+    struct Pre {};
+    __device__ void init(Acc& a) { a.v[0] = a.v[1] = 0.0; }
+    __device__ __forceinline__ Pre pre_global(int) const { return Pre{}; }
+    __device__ __forceinline__ void terms(int i, double s, double& r2, double& ob) const {
+        if (SCALED) s = __dmul_rn(dsc[i], s);
+        const double l = (double)lc[i], u = (double)uc[i];
+        const bool lo = !isinf(l), up = !isinf(u);
+        const double res = (lo && up) ? s : lo ? fmin(s, 0.0) : up ? fmax(s, 0.0) : 0.0;
+        r2 = __dmul_rn(res, res);
+        const double y = ry[i];
+        ob = y > 0.0 ? __dmul_rn(l, y) : (y < 0.0 ? __dmul_rn(u, y) : 0.0);
+    }
+    __device__ __forceinline__ void row(int, int i, double s, const Pre&, Acc& a) {
+        double r2, ob;
+        terms(i, s, r2, ob);
+        a.v[0] += r2;
+        a.v[1] += ob;
+    }
+    __device__ void row_long(int, int i, double s, int lid, Acc&) {
+        double r2, ob;
+        terms(i, s, r2, ob);
+        long_out[(size_t)lid * 2] = r2;
+        long_out[(size_t)lid * 2 + 1] = ob;
+    }
+    __device__ void finish(Acc& a) { block_reduce_store<2>(a.v, block_out); }
+};
+
+// Column side, dual ray y: g = -(A' y)_j (SCALED: gathered D1 y, times d2_j),
+// r = the part of g the variable bounds allow (proj_multiplier); accumulates
+// |g - r|^2, the ray objective of r (lv_j r for r > 0, uv_j r for r < 0) and
+// c'x of the primal ray
+template <class T, bool SCALED = false>
+struct RayColEpi {
+    const T* __restrict__ c;
+    const T* __restrict__ lv;
+    const T* __restrict__ uv;
+    const double* __restrict__ rx;
+    const double* __restrict__ dsc;
+    double* block_out;
+    double* long_out;
+    struct Acc { double v[3]; };
+    struct Pre {};
+    __device__ void init(Acc& a) { a.v[0] = a.v[1] = a.v[2] = 0.0; }
+    __device__ __forceinline__ Pre pre_global(int) const { return Pre{}; }
+    __device__ __forceinline__ void terms(int j, double s, double& r2, double& ob,
+                                          double& cx) const {
+        if (SCALED) s = __dmul_rn(dsc[j], s);
+        const double l = (double)lv[j], u = (double)uv[j];
+        const double g = -s;
+        const double r = proj_multiplier(g, l, u);
+        const double res = __dsub_rn(g, r);
+        r2 = __dmul_rn(res, res);
+        ob = r > 0.0 ? __dmul_rn(l, r) : (r < 0.0 ? __dmul_rn(u, r) : 0.0);
+        cx = __dmul_rn((double)c[j], rx[j]);
+    }
+    __device__ __forceinline__ void row(int, int j, double s, const Pre&, Acc& a) {
+        double r2, ob, cx;
+        terms(j, s, r2, ob, cx);
+        a.v[0] += r2;
+        a.v[1] += ob;
+        a.v[2] += cx;
+    }
+    __device__ void row_long(int, int j, double s, int lid, Acc&) {
+        double r2, ob, cx;
+        terms(j, s, r2, ob, cx);
+        double* o = long_out + (size_t)lid * 3;
+        o[0] = r2;
+        o[1] = ob;
+        o[2] = cx;
+    }
+    __device__ void finish(Acc& a) { block_reduce_store<3>(a.v, block_out); }
+};
+
 // power method, second product: Ax_j = (A' s)_j; accumulates x.Ax and Ax.Ax
 // (SCALED: the product gathered D1 s and Ax_j is the row sum times d2_j)
 template <class T, bool SCALED = false>

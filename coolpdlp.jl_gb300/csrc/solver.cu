@@ -151,6 +151,34 @@ __global__ void k_mul_vec(const T* __restrict__ a, const T* __restrict__ b, T* _
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < len) out[i] = mul_rn(a[i], b[i]);
 }
+// Infeasibility certificates (an extension): the rays are the change of the
+// iterates since the previous check, x projected onto the recession cone of
+// [lv, uv] and y onto the multiplier cone of [lc, uc] (>= 0 with only lc
+// finite, <= 0 with only uc finite, 0 for a free row); FP64.  rxs / rys
+// (narrow storage): D2 .* rx and D1 .* ry, the vectors its products gather.
+template <class T>
+__global__ void k_ray(const T* __restrict__ x, const T* __restrict__ xp, const T* __restrict__ lv,
+                      const T* __restrict__ uv, double* __restrict__ rx, double* __restrict__ rxs,
+                      const double* __restrict__ D2, int64_t n, const T* __restrict__ y,
+                      const T* __restrict__ yp, const T* __restrict__ lc,
+                      const T* __restrict__ uc, double* __restrict__ ry,
+                      double* __restrict__ rys, const double* __restrict__ D1, int64_t m) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
+        double d = __dsub_rn((double)x[j], (double)xp[j]);
+        const bool lo = !isinf((double)lv[j]), up = !isinf((double)uv[j]);
+        d = (lo && up) ? 0.0 : lo ? fmax(d, 0.0) : up ? fmin(d, 0.0) : d;
+        rx[j] = d;
+        if (rxs) rxs[j] = __dmul_rn(D2[j], d);
+    }
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += stride) {
+        double d = __dsub_rn((double)y[i], (double)yp[i]);
+        const bool lo = !isinf((double)lc[i]), up = !isinf((double)uc[i]);
+        d = (lo && up) ? d : lo ? fmax(d, 0.0) : up ? fmin(d, 0.0) : 0.0;
+        ry[i] = d;
+        if (rys) rys[i] = __dmul_rn(D1[i], d);
+    }
+}
 // precondition(milp, prec) on the vectors (preconditioning.jl:61-91)
 template <class T>
 __global__ void k_scale_vec_n(const double* __restrict__ c, const double* __restrict__ lv,
@@ -764,6 +792,11 @@ struct StateT : StateBase {
     // (scaled base multipliers), and the KKT evaluation of the combined iterate
     // (base + correction) that replaces the state's own
     const double* yoff = nullptr;
+    // infeasibility detection (prm.infeasibility_tol > 0): the iterates at the
+    // previous check and the FP64 rays
+    DBuf<T> xprev, yprev;
+    DBuf<double> rx, ry, rxs, rys, rpart_A, rpart_At;
+    bool have_prev = false;
     std::function<void(int, const T* const*, const T* const*, cpdlp_kkt_errors*)> kkt_hook;
     DBuf<StepCoef<T>> coef, coef1;
     std::vector<StepCoef<T>> coef_host;
@@ -993,6 +1026,88 @@ struct StateT : StateBase {
         kkt_multi<1>(xs, ys, e);
     }
 
+    // Tests the change of the iterates since the previous check as an
+    // infeasibility certificate; returns PRIMAL_INFEASIBLE / DUAL_INFEASIBLE
+    // (the ray replaces y / x of sol) or STILL_RUNNING.
+    int32_t infeasibility_check() {
+        ProblemT<T>& P = *PT;
+        cudaStream_t s = h->stream;
+        const int64_t m = P.m, n = P.n;
+        const size_t nz = (size_t)std::max<int64_t>(n, 1), mz = (size_t)std::max<int64_t>(m, 1);
+        if (!xprev.p) {
+            xprev.alloc(nz); yprev.alloc(mz); rx.alloc(nz); ry.alloc(mz);
+            if (P.pm1) { rxs.alloc(nz); rys.alloc(mz); }
+            rpart_A.alloc((size_t)std::max(P.planA.npieces, 1));
+            rpart_At.alloc((size_t)std::max(P.planAt.npieces, 1));
+        }
+        auto keep = [&] {
+            CK(cudaMemcpyAsync(xprev.p, x[cur].p, sizeof(T) * nz, cudaMemcpyDeviceToDevice, s));
+            CK(cudaMemcpyAsync(yprev.p, y[cur].p, sizeof(T) * mz, cudaMemcpyDeviceToDevice, s));
+        };
+        if (!have_prev) {
+            keep();
+            have_prev = true;
+            return CPDLP_STILL_RUNNING;
+        }
+        k_ray<T><<<red_grid(*h, std::max(m, n)), RED_THREADS, 0, s>>>(
+            x[cur].p, xprev.p, P.lv.p, P.uv.p, rx.p, P.pm1 ? rxs.p : nullptr, P.D2.p, n,
+            y[cur].p, yprev.p, P.lc.p, P.uc.p, ry.p, P.pm1 ? rys.p : nullptr, P.D1.p, m);
+        CK_LAUNCH();
+        keep();
+        const unsigned gA = tiles_grid(P.planA), gAt = tiles_grid(P.planAt);
+        double* const rblk = P.red_rows.p;
+        double* const cblk = P.red_cols.p;
+        if (P.pm1) {
+            const CsrView<Pm1, double> A1{P.a_ptr.p, P.a_idx.p, nullptr, P.planA.tasks.p,
+                                          P.planA.ntasks, P.planA.ltasks.p, P.planA.nltasks,
+                                          P.planA.counters.p, rpart_A.p};
+            const CsrView<Pm1, double> At1{P.at_ptr.p, P.at_idx.p, nullptr, P.planAt.tasks.p,
+                                           P.planAt.ntasks, P.planAt.ltasks.p, P.planAt.nltasks,
+                                           P.planAt.counters.p, rpart_At.p};
+            launch_tiles<1>(P.planA, A1, VecSet<double, 1>{{rxs.p}},
+                            RayRowEpi<T, true>{P.lc.p, P.uc.p, ry.p, P.D1.p, rblk, rblk + (size_t)gA * 2}, s);
+            launch_tiles<1>(P.planAt, At1, VecSet<double, 1>{{rys.p}},
+                            RayColEpi<T, true>{P.c.p, P.lv.p, P.uv.p, rx.p, P.D2.p, cblk,
+                                               cblk + (size_t)gAt * 3}, s);
+        } else {
+            const CsrView<T, double> A{P.a_ptr.p, P.a_idx.p, P.a_val.p, P.planA.tasks.p,
+                                       P.planA.ntasks, P.planA.ltasks.p, P.planA.nltasks,
+                                       P.planA.counters.p, rpart_A.p};
+            const CsrView<T, double> At{P.at_ptr.p, P.at_idx.p, P.at_val.p, P.planAt.tasks.p,
+                                        P.planAt.ntasks, P.planAt.ltasks.p, P.planAt.nltasks,
+                                        P.planAt.counters.p, rpart_At.p};
+            launch_tiles<1>(P.planA, A, VecSet<double, 1>{{rx.p}},
+                            RayRowEpi<T>{P.lc.p, P.uc.p, ry.p, nullptr, rblk, rblk + (size_t)gA * 2}, s);
+            launch_tiles<1>(P.planAt, At, VecSet<double, 1>{{ry.p}},
+                            RayColEpi<T>{P.c.p, P.lv.p, P.uv.p, rx.p, nullptr, cblk,
+                                         cblk + (size_t)gAt * 3}, s);
+        }
+        reduce_partials(rblk, P.rows_A_partials, 2, P.red_out.p, s);
+        reduce_partials(cblk, P.rows_At_partials, 3, P.red_out.p + 2, s);
+        launches += 3 + tiles_launches(P.planA) + tiles_launches(P.planAt) + 2;
+        double* pin = h->pinned_area(sizeof(double) * 64);
+        CK(cudaMemcpyAsync(pin, P.red_out.p, sizeof(double) * 5, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        const double ep = std::sqrt(pin[0]), yrow = pin[1], ed = std::sqrt(pin[2]),
+                     ycol = pin[3], cx = pin[4];
+        const double tol = prm.infeasibility_tol, bobj = yrow + ycol;
+        if (bobj > 0.0 && ed <= tol * bobj) {
+            if (m > 0) {
+                k_narrow<T><<<grid_for(m, 256), 256, 0, s>>>(ry.p, y[cur].p, m);
+                CK_LAUNCH();
+            }
+            return CPDLP_PRIMAL_INFEASIBLE;
+        }
+        if (cx < 0.0 && ep <= tol * (-cx)) {
+            if (n > 0) {
+                k_narrow<T><<<grid_for(n, 256), 256, 0, s>>>(rx.p, x[cur].p, n);
+                CK_LAUNCH();
+            }
+            return CPDLP_DUAL_INFEASIBLE;
+        }
+        return CPDLP_STILL_RUNNING;
+    }
+
     void push_history() {
         if (!prm.record_error_history) return;
         hist_passes.push_back(kkt_passes);
@@ -1097,6 +1212,10 @@ struct StateT : StateBase {
                 cpdlp_kkt_errors e;
                 kkt(CPDLP_VEC_SOL, &e);
                 if (termination_check_with(e)) break;
+                if (prm.infeasibility_tol > 0) {
+                    const int32_t inf = infeasibility_check();
+                    if (inf != CPDLP_STILL_RUNNING) { status = inf; break; }
+                }
             }
             return status;
         }
@@ -1114,6 +1233,10 @@ struct StateT : StateBase {
                 // the outer loop's second termination_check! (pdlp.jl:88) re-evaluates sol
                 termination_check_with(e4[0]);
                 break;
+            }
+            if (prm.infeasibility_tol > 0) {
+                const int32_t inf = infeasibility_check();
+                if (inf != CPDLP_STILL_RUNNING) { status = inf; break; }
             }
             if (restart_check(e4)) restart();
         }
@@ -1469,6 +1592,7 @@ RefineResult refine_residual(Handle& h, ProblemT<float>& P32, ProblemT<double>& 
         pr.float_type = CPDLP_VAL_F32;
         pr.termination_reltol = 0.0;  // the rounds' own rule below decides
         pr.max_kkt_passes = passes_left;
+        pr.infeasibility_tol = 0.0;   // rays of the residual LP would need its shifted cones
         std::unique_ptr<StateBase> SB(
             make_state<float>(h, &P32, &pr, nullptr, nullptr, eta, R.omega * dd / dp));
         auto& S = static_cast<StateT<float>&>(*SB);

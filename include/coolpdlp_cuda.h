@@ -51,7 +51,10 @@ enum {
     CPDLP_OPTIMAL = 0,
     CPDLP_TIME_LIMIT = 1,
     CPDLP_ITERATION_LIMIT = 2,
-    CPDLP_STILL_RUNNING = 3
+    CPDLP_STILL_RUNNING = 3,
+    /* EXT (infeasibility_tol > 0; the reference has no detection): */
+    CPDLP_PRIMAL_INFEASIBLE = 4, /* a dual ray certifies that no x is feasible */
+    CPDLP_DUAL_INFEASIBLE = 5    /* a primal ray certifies that the objective is unbounded */
 };
 
 /* Algorithm{:PDLP} / Algorithm{:PDHG} (src/algorithms/pdlp.jl:6-11, pdhg.jl:6-16) */
@@ -132,6 +135,17 @@ typedef struct cpdlp_params {
     int32_t tile_nnz;
     /* EXT: storage flags (CPDLP_TILE_*); 0 = defaults. */
     int32_t tile_flags;
+    /* EXT: infeasibility detection of the single-LP solve (0 = off, as in the
+     * reference; 1e-8 is a typical value).  At every check the change of the
+     * iterates since the previous check is tested as a certificate: a dual ray
+     * y (signs projected onto the row bounds' cone) with reduced costs
+     * g = -A'y, r = its part the variable bounds allow, and positive ray
+     * objective b(y, r) proves primal infeasibility when |g - r| <=
+     * infeasibility_tol * b(y, r); a primal ray x (projected onto the bounds'
+     * recession cone) with c'x < 0 proves unboundedness when the distance of
+     * A x to the row bounds' recession cone is <= infeasibility_tol * |c'x|.
+     * Both tests run in the scaled problem, where they are equivalent. */
+    double infeasibility_tol;
 } cpdlp_params;
 
 /* tile_flags bits.  By default a single-LP solve with FP32 iterates whose
