@@ -76,3 +76,31 @@ def test_feasible_lps_unchanged(handle, ft):
         assert s1.termination_status == s0.termination_status == A.OPTIMAL
         assert s1.kkt_passes == s0.kkt_passes
         assert np.array_equal(x1, x0) and np.array_equal(y1, y0)
+
+
+def test_moi_statuses(cuda_lib):
+    from coolpdlp import moi
+    # infeasible: x + y >= 3 with x, y in [0, 1]
+    m = moi.Model()
+    x = m.add_variable(lower=0.0, upper=1.0)
+    y = m.add_variable(lower=0.0, upper=1.0)
+    m.add_constraint({x: 1.0, y: 1.0}, moi.GreaterThan(3.0))
+    m.set_objective({x: 1.0, y: 1.0}, sense=moi.Sense.MIN)
+    opt = moi.Optimizer()
+    opt.set_silent()
+    opt.set_attribute("infeasibility_tol", 1e-8)
+    opt.optimize(m)
+    assert opt.termination_status == moi.TerminationStatusCode.INFEASIBLE
+    assert opt.get_dual_status() == moi.ResultStatusCode.INFEASIBILITY_CERTIFICATE
+    # unbounded: max x + y with x - y <= 1, x, y >= 0
+    m2 = moi.Model()
+    a = m2.add_variable(lower=0.0)
+    b = m2.add_variable(lower=0.0)
+    m2.add_constraint({a: 1.0, b: -1.0}, moi.LessThan(1.0))
+    m2.set_objective({a: 1.0, b: 1.0}, sense=moi.Sense.MAX)
+    opt2 = moi.Optimizer()
+    opt2.set_silent()
+    opt2.set_attribute("infeasibility_tol", 1e-8)
+    opt2.optimize(m2)
+    assert opt2.termination_status == moi.TerminationStatusCode.DUAL_INFEASIBLE
+    assert opt2.get_primal_status() == moi.ResultStatusCode.INFEASIBILITY_CERTIFICATE
