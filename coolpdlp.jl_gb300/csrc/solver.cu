@@ -1229,6 +1229,8 @@ struct StateT : StateBase {
             const T* const xs[4] = {x[cur].p, xa[cur].p, x[cur ^ 1].p, xa[cur ^ 1].p};
             const T* const ys[4] = {y[cur].p, ya[cur].p, y[cur ^ 1].p, ya[cur ^ 1].p};
             kkt_multi<4>(xs, ys, e4);
+            err_avg = e4[1];
+            restarted_at_check = false;
             if (termination_check_with(e4[0])) {
                 // the outer loop's second termination_check! (pdlp.jl:88) re-evaluates sol
                 termination_check_with(e4[0]);
@@ -1238,7 +1240,10 @@ struct StateT : StateBase {
                 const int32_t inf = infeasibility_check();
                 if (inf != CPDLP_STILL_RUNNING) { status = inf; break; }
             }
-            if (restart_check(e4)) restart();
+            if (restart_check(e4)) {
+                restart();
+                restarted_at_check = true;
+            }
         }
         return status;
     }
@@ -1552,6 +1557,7 @@ RefineResult refine_residual(Handle& h, ProblemT<float>& P32, ProblemT<double>& 
     const size_t nz = (size_t)std::max<int64_t>(n, 1), mz = (size_t)std::max<int64_t>(m, 1);
     DBuf<double> Ax0(mz), Aty0(nz), cx[4], cy[4];
     DBuf<double> yoff(mz);
+    DBuf<float> bdx(nz), bdy(mz);  // the round's best correction
     for (int q = 0; q < 4; q++) {
         cx[q].alloc(nz);
         cy[q].alloc(mz);
@@ -1629,17 +1635,32 @@ RefineResult refine_residual(Handle& h, ProblemT<float>& P32, ProblemT<double>& 
         };
         const double target = jl_max(prm.refine_reltol, REFINE_ROUND_DECAY * r0);
         // a round counts as stalled once it gained a factor 100 and stopped
-        // halving, or after FP32_STALL_LONG windows without halving
+        // halving, or after FP32_STALL_LONG windows without halving (a round
+        // restarts PDLP cold, and its first halving can take 20,000 passes)
         StallWatch watch;
         const char* why = "limit";
+        // the best correction seen at a check (sol or its average), kept so that
+        // the base point never gets worse; the base itself (dx = 0) has r0
+        double best_rel = r0;
+        bool have_best = false;
         int64_t outer_before = S.outer;
-        bool use_avg = false;
         while (S.solve_blocks(1) == CPDLP_STILL_RUNNING) {
-            // the better of sol and its average (unless the check restarted, which
-            // moved the chosen candidate into sol)
-            use_avg = S.pdlp() && S.outer == outer_before && rel_err(e_avg) < rel_err(e_cur);
+            // candidates: sol and its average; a restart at the check moved the
+            // chosen one (the average if restart_from_avg) into sol
+            const bool restarted = S.outer != outer_before;
             outer_before = S.outer;
-            const double rc = jl_min(rel_err(e_cur), use_avg ? rel_err(e_avg) : INFINITY);
+            const double r_sol = restarted && S.restart_from_avg ? rel_err(e_avg) : rel_err(e_cur);
+            const double r_avg = (S.pdlp() && !restarted) ? rel_err(e_avg) : INFINITY;
+            const bool use_avg = r_avg < r_sol;
+            const double rc = jl_min(r_sol, r_avg);
+            if (rc < best_rel) {
+                best_rel = rc;
+                have_best = true;
+                CK(cudaMemcpyAsync(bdx.p, use_avg ? S.xa[S.cur].p : S.x[S.cur].p,
+                                   sizeof(float) * nz, cudaMemcpyDeviceToDevice, s));
+                CK(cudaMemcpyAsync(bdy.p, use_avg ? S.ya[S.cur].p : S.y[S.cur].p,
+                                   sizeof(float) * mz, cudaMemcpyDeviceToDevice, s));
+            }
             if (trace_level() > 1)
                 fprintf(stderr, "[cpdlp refine]   %lld: rel %.3e (p %.2e d %.2e g %.2e) omega %.3g\n",
                         (long long)S.kkt_passes, rc, e_cur.primal / e_cur.primal_scale,
@@ -1651,14 +1672,14 @@ RefineResult refine_residual(Handle& h, ProblemT<float>& P32, ProblemT<double>& 
                 break;
             }
         }
-        // the new base point: the round's solution (sol, or its average when
-        // that was better at the last check) added in FP64
-        const float* dxp = use_avg ? S.xa[S.cur].p : S.x[S.cur].p;
-        const float* dyp = use_avg ? S.ya[S.cur].p : S.y[S.cur].p;
-        k_refine_combine<float><<<gc, RED_THREADS, 0, s>>>(x0.p, dxp, 1.0 / dp, P64.lv.p, P64.uv.p,
-                                                          x0.p, n, y0.p, dyp, 1.0 / dd, P64.lc.p,
-                                                          P64.uc.p, y0.p, m);
-        CK_LAUNCH();
+        // the new base point: the best correction added in FP64 (none: the base
+        // stays)
+        if (have_best) {
+            k_refine_combine<float><<<gc, RED_THREADS, 0, s>>>(x0.p, bdx.p, 1.0 / dp, P64.lv.p,
+                                                              P64.uv.p, x0.p, n, y0.p, bdy.p,
+                                                              1.0 / dd, P64.lc.p, P64.uc.p, y0.p, m);
+            CK_LAUNCH();
+        }
         R.launches += S.launches + 1;
         R.passes += S.kkt_passes;
         passes_left -= S.kkt_passes;
@@ -1734,6 +1755,8 @@ void solve_full(Handle& h, const cpdlp_lp* lp, const cpdlp_params* params, const
     S->starting_time = t0;
     const bool mixed = params->float_type == CPDLP_VAL_F32 && params->refine_reltol > 0;
     bool stalled = false;
+    double fp32_best = INFINITY;      // mixed: the FP32 phase's best point
+    DBuf<float> best_x, best_y;
     if (P->m == 0 && P->zero_cost) {
         S->early_exit_zero_problem();  // common.jl:194-198
     } else if (mixed) {
@@ -1744,10 +1767,28 @@ void solve_full(Handle& h, const cpdlp_lp* lp, const cpdlp_params* params, const
                                              params->refine_reltol > 0 ? params->refine_reltol
                                                                        : INFINITY);
         const int64_t win = FP32_STALL_CHECKS * (int64_t)params->check_every;
+        auto& S32 = static_cast<StateT<float>&>(*S);
+        const size_t nz1 = (size_t)std::max<int64_t>(P->n, 1), mz1 = (size_t)std::max<int64_t>(P->m, 1);
         while (S->solve_blocks(1) == CPDLP_STILL_RUNNING) {
             const cpdlp_kkt_errors& e = S->err;
-            const double rel = std::max(std::max(e.primal / e.primal_scale, e.dual / e.dual_scale),
-                                        e.gap / e.gap_scale);
+            // candidates: sol and its average (the current iterate's error is
+            // noisy); a restart at the check moved the chosen one into sol
+            const bool rs = S32.restarted_at_check;
+            const double r_sol = rs && S32.restart_from_avg ? rel_err(S32.err_avg) : rel_err(e);
+            const double r_avg = (S32.pdlp() && !rs) ? rel_err(S32.err_avg) : INFINITY;
+            const double rel = jl_min(r_sol, r_avg);
+            if (rel < fp32_best) {  // the refinement starts from the best point
+                fp32_best = rel;
+                if (!best_x.p) {
+                    best_x.alloc(nz1);
+                    best_y.alloc(mz1);
+                }
+                const bool ua = r_avg < r_sol;
+                CK(cudaMemcpyAsync(best_x.p, ua ? S32.xa[S32.cur].p : S32.x[S32.cur].p,
+                                   sizeof(float) * nz1, cudaMemcpyDeviceToDevice, h.stream));
+                CK(cudaMemcpyAsync(best_y.p, ua ? S32.ya[S32.cur].p : S32.y[S32.cur].p,
+                                   sizeof(float) * mz1, cudaMemcpyDeviceToDevice, h.stream));
+            }
             if (trace_level() > 1)
                 fprintf(stderr, "[cpdlp refine]   FP32 %lld: rel %.3e (p %.2e d %.2e g %.2e)\n",
                         (long long)S->kkt_passes, rel, e.primal / e.primal_scale,
@@ -1761,8 +1802,8 @@ void solve_full(Handle& h, const cpdlp_lp* lp, const cpdlp_params* params, const
         S->solve();
     }
     if (mixed && trace_on())
-        fprintf(stderr, "[cpdlp refine] FP32 phase: rel %.3e after %lld passes%s\n",
-                rel_err(S->err), (long long)S->kkt_passes, stalled ? " (stalled)" : "");
+        fprintf(stderr, "[cpdlp refine] FP32 phase: rel %.3e (best %.3e) after %lld passes%s\n",
+                rel_err(S->err), fp32_best, (long long)S->kkt_passes, stalled ? " (stalled)" : "");
     // refinement: the FP32 iterates stalled before the tolerance
     const bool refine = mixed && stalled;
     if (!refine) {
@@ -1782,9 +1823,12 @@ void solve_full(Handle& h, const cpdlp_lp* lp, const cpdlp_params* params, const
     const size_t nz = (size_t)std::max<int64_t>(n, 1), mz = (size_t)std::max<int64_t>(m, 1);
     DBuf<double> bx(nz), by(mz);
     {
+        // the base point: the FP32 phase's best point at a check
         auto& S32 = static_cast<StateT<float>&>(*S);
-        if (n > 0) k_widen<float><<<grid_for(n, 256), 256, 0, h.stream>>>(S32.x[S32.cur].p, bx.p, n);
-        if (m > 0) k_widen<float><<<grid_for(m, 256), 256, 0, h.stream>>>(S32.y[S32.cur].p, by.p, m);
+        const float* xb = best_x.p ? best_x.p : S32.x[S32.cur].p;
+        const float* yb = best_y.p ? best_y.p : S32.y[S32.cur].p;
+        if (n > 0) k_widen<float><<<grid_for(n, 256), 256, 0, h.stream>>>(xb, bx.p, n);
+        if (m > 0) k_widen<float><<<grid_for(m, 256), 256, 0, h.stream>>>(yb, by.p, m);
         CK_LAUNCH();
     }
     S.reset();

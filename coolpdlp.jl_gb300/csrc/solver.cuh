@@ -70,6 +70,10 @@ struct StateBase {
     int32_t status = CPDLP_STILL_RUNNING;
     int32_t restart_from_avg = 0;
     cpdlp_kkt_errors err{}, err_cand{}, err_cand_last{}, err_restart{};
+    // PDLP: errors of the average at the last check, and whether that check
+    // restarted (which moved the chosen candidate into sol and reset the average)
+    cpdlp_kkt_errors err_avg{};
+    bool restarted_at_check = false;
     bool err_restart_valid = false;
     double starting_time = 0, time_elapsed = 0, setup_seconds = 0;
     int64_t power_iterations = 0;
