@@ -1666,6 +1666,12 @@ RefineResult refine_residual(Handle& h, ProblemT<float>& P32, ProblemT<double>& 
                         (long long)S.kkt_passes, rc, e_cur.primal / e_cur.primal_scale,
                         e_cur.dual / e_cur.dual_scale, e_cur.gap / e_cur.gap_scale, S.omega);
             if (rc <= target) { why = "target"; break; }
+            // a later round (the error already small) that has not improved at
+            // all after 3 windows ends
+            if (R.rounds > 0 && best_rel >= r0 && S.kkt_passes >= 3 * FP32_STALL_CHECKS * (int64_t)ce) {
+                why = "no gain";
+                break;
+            }
             if (watch.stalled(rc, S.kkt_passes, FP32_STALL_CHECKS * (int64_t)ce,
                               FP32_STALL_LONG * FP32_STALL_CHECKS * (int64_t)ce, 1e-2 * r0)) {
                 why = "stall";
@@ -1878,10 +1884,9 @@ void solve_full(Handle& h, const cpdlp_lp* lp, const cpdlp_params* params, const
     S64.reset();
     P.reset();
     p64.max_kkt_passes = std::max<int64_t>(params->max_kkt_passes - passes, 1);
-    // the primal weight starts cold (primal_weight_init): the FP32 run's and
-    // the rounds' weights belong to iterates that stopped making progress
+    // the primal weight continues from the rounds'
     std::unique_ptr<StateBase> C64(
-        state_create(h, P64.get(), &p64, xs.data(), ys.data(), eta32, 0.0));
+        state_create(h, P64.get(), &p64, xs.data(), ys.data(), eta32, R.omega));
     C64->starting_time = t0;
     C64->solve();
     C64->solution(x_out, y_out);
