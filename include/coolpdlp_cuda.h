@@ -367,7 +367,8 @@ int cpdlp_spmv_csr_noalloc(cpdlp_handle* h, int64_t m, int64_t n, int64_t nnz,
  * targets a smaller refine_reltol, or whose FP32 iterates stall (error not
  * halved over 30 checks), continues in FP64 warm-started from its FP32
  * solution (as cpdlp_solve does for one LP).  The power method runs in FP64
- * for both iterate types. */
+ * for both iterate types.  infeasibility_tol is not applied to batched LPs
+ * (they run into their limits, as in the reference). */
 int cpdlp_batch_solve(cpdlp_handle* h, int64_t count, const cpdlp_lp* lps,
                       const cpdlp_params* params, double* const* x_out,
                       double* const* y_out, cpdlp_stats* stats);
