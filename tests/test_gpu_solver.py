@@ -201,3 +201,33 @@ def test_fp32_with_fp64_refinement_reaches_1e8(handle, oracle):
     x, y, s = native.solve_lp(handle, L, p)
     assert s.termination_status == 0 and s.refine_kkt_passes > 0
     assert abs(float(lp.c @ x) - oo) <= 1e-6 * max(1.0, abs(oo))
+
+
+def test_pdhg_fp32_refinement_runs(handle):
+    """PDHG (no restarts, no averages) through the mixed-precision path: FP32
+    phase, refinement rounds on the residual LP, FP64 continuation if needed.
+    PDHG converges sublinearly, so the check is the plumbing: a consistent
+    status, and at OPTIMAL the tolerance met and the Float64 path's objective."""
+    from coolpdlp import native, _abi as A
+    from coolpdlp import generators as G
+    lp = G.random_sparse_lp(120, 240, 5, seed=21)
+    L = native.LPStruct(lp.m, lp.n, lp.colptr, lp.rowval, lp.nzval, lp.c, lp.lv, lp.uv, lp.lc,
+                        lp.uc)
+    p = A.default_params_py(A.ALGO_PDHG)
+    p.float_type = A.VAL_F32
+    p.refine_reltol = 1e-5
+    p.max_kkt_passes = 100000
+    x, y, st = native.solve_lp(handle, L, p)
+    e = st.err
+    rel = max(e.primal / e.primal_scale, e.dual / e.dual_scale, e.gap / e.gap_scale)
+    assert st.termination_status in (A.OPTIMAL, A.ITERATION_LIMIT)
+    if st.termination_status == A.ITERATION_LIMIT:
+        assert st.kkt_passes >= p.max_kkt_passes
+        return
+    assert rel <= 1e-5
+    p64 = A.default_params_py(A.ALGO_PDHG)
+    p64.termination_reltol = 1e-5
+    x64, _, st64 = native.solve_lp(handle, L, p64)
+    if st64.termination_status == A.OPTIMAL:
+        o, o64 = float(lp.c @ x), float(lp.c @ x64)
+        assert abs(o - o64) <= 1e-3 * max(1.0, abs(o64))
