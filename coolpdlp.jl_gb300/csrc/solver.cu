@@ -1667,7 +1667,7 @@ RefineResult refine_residual(Handle& h, ProblemT<float>& P32, ProblemT<double>& 
                         e_cur.dual / e_cur.dual_scale, e_cur.gap / e_cur.gap_scale, S.omega);
             if (rc <= target) { why = "target"; break; }
             // a later round (the error already small) that has not improved at
-            // all after 3 windows ends
+            // all after 3 stall windows (90 checks) ends
             if (R.rounds > 0 && best_rel >= r0 && S.kkt_passes >= 3 * FP32_STALL_CHECKS * (int64_t)ce) {
                 why = "no gain";
                 break;
