@@ -156,3 +156,15 @@ def test_narrow_flow_solves_match_highs(handle, refine):
             assert abs(o - obj) <= tol * max(1.0, abs(obj)), (narrow, o, obj)
         if not refine:
             assert abs(got[True] - got[False]) <= 1e-2 * max(1.0, abs(obj))
+
+
+def test_unknown_tile_flags_rejected(handle):
+    from coolpdlp import native, _abi as A
+    from coolpdlp import generators as G
+    lp = G.two_variable_lp()
+    L = native.LPStruct(lp.m, lp.n, lp.colptr, lp.rowval, lp.nzval, lp.c, lp.lv, lp.uv, lp.lc,
+                        lp.uc)
+    p = _params(True)
+    p.tile_flags = 2
+    with pytest.raises(A.ArgumentError):
+        native.solve_lp(handle, L, p)
