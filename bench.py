@@ -20,7 +20,7 @@ LP with K=16: FP32 iterations/s with the narrow +-1 storage and with scaled
 values, and solves to 1e-4 and, with refinement rounds, to 1e-8), `batch`
 (4,096 random LPs in persistent launches against the one-at-a-time FP64
 path) and `serving` (a Poisson stream through the continuous-batching
-server, p50/p99).
+server, p50/p99, then the same requests arriving at once for throughput).
 
 --impl reference times the CPU restatement of the reference algorithm
 (oracle/, Float64, all host threads) on the same LP.
