@@ -15,19 +15,33 @@
 // shuffle tree).  A row that crosses warp ranges leaves one partial sum per
 // warp in the scratch array below; a second, thread-per-row pass adds those
 // partials in warp order (deterministic) and also writes the rows without
-// nonzeros.
+// nonzeros.  A warp skips a run of empty rows with one binary search, so its
+// work does not grow with the number of empty rows.
 //
 // Scratch: a file-scope device array of NA_MAX_WARPS * 2 doubles (1 MiB),
 // resident on every GPU that loads this library until the process exits.  It
 // bounds nnz at NA_MAX_WARPS * 512 = 33,554,432 nonzeros; larger matrices are
 // rejected with CPDLP_ERR_UNSUPPORTED.  Host code cannot use the array's name
 // as a device address, so the address is looked up with cudaGetSymbolAddress
-// once per device, on that device's first call (which should therefore come
-// before any stream capture).  Every call shares the array and it keeps the
-// last call's contents; no part needs clearing, because every slot a call
-// reads is written earlier in the same call.  Calls that overlap on the GPU
-// (different streams or handles at the same time) race on the array.
+// once per device (thread-safe), on that device's first call, with the device
+// current.  That first call should therefore come before any stream capture;
+// with CUDA's lazy module loading it is also the call that makes the array
+// resident, so make it before the device-memory budget is fixed.  Every call
+// shares the array and it keeps the last call's contents; no part needs
+// clearing, because every slot a call reads is written earlier in the same
+// call.
+//
+// Validation flag: a second file-scope device word records invalid CSR input.
+// Each call clears it on its stream before its kernels and reads it back after
+// them, so every call blocks until its product is done.
+//
+// Calls that overlap on the GPU (different streams or handles at the same
+// time) race on both the scratch array and the validation flag: their
+// results can be wrong, and an invalid-input error of one call can be
+// reported by, or lost to, a call that overlaps it.  Serialise them.
 #include "noalloc.cuh"
+
+#include <mutex>
 
 namespace cpdlp {
 namespace {
@@ -61,10 +75,21 @@ __global__ void __launch_bounds__(NA_WARPS_PER_BLOCK * 32)
         const int64_t mid = (rlo + rhi) >> 1;
         if ((int64_t)rowptr1[mid] - 1 <= lo) rlo = mid; else rhi = mid;
     }
-    for (int64_t r = rlo; r < m; r++) {
+    for (int64_t r = rlo; r < m;) {
         const int64_t ra = (int64_t)rowptr1[r] - 1, rb = (int64_t)rowptr1[r + 1] - 1;
         if (ra >= hi) break;
-        if (rb <= ra) continue;  // empty rows are written by the second pass
+        // the next row to visit: the last q in (r, m] with rowptr0[q] <= rb,
+        // so a run of empty rows (written by the second pass) costs one
+        // binary search; q always advances, whatever the input
+        int64_t nlo = r + 1, nhi = m;
+        if ((int64_t)rowptr1[nlo] - 1 <= rb) {
+            while (nhi > nlo) {
+                const int64_t mid = (nlo + nhi + 1) >> 1;
+                if ((int64_t)rowptr1[mid] - 1 <= rb) nlo = mid; else nhi = mid - 1;
+            }
+        }
+        const int64_t next = nlo;
+        if (rb <= ra) { r = next; continue; }
         const int64_t a = max(ra, lo), e = min(rb, hi);
         T s = T(0);
         for (int64_t k = a + lane; k < e; k += 32) {
@@ -88,6 +113,7 @@ __global__ void __launch_bounds__(NA_WARPS_PER_BLOCK * 32)
                 scratch[2 * w + 1] = (double)s;
             }
         }
+        r = next;
     }
 }
 
@@ -118,18 +144,28 @@ __global__ void k_na_fixup(int64_t m, int64_t nnz, const int32_t* __restrict__ r
     c[r] = v;
 }
 
-// device address of the scratch array, looked up once per device
-double* scratch_address(int device) {
-    static double* addr[64] = {nullptr};
+// device addresses of the scratch array and of the validation flag, looked up
+// once per device (the device is current: every entry point sets the handle's
+// device first)
+struct NaSymbols {
+    double* scratch = nullptr;
+    int* bad = nullptr;
+};
+NaSymbols symbols(int device) {
+    static std::once_flag once[64];
+    static NaSymbols addr[64];
     if (device < 0 || device >= 64) fail(CPDLP_ERR_UNSUPPORTED, "device ordinal above 63");
-    if (!addr[device]) {
+    std::call_once(once[device], [device] {
         void* p = nullptr;
+        void* q = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_spmv_noalloc_scratch);
+        if (e == cudaSuccess) e = cudaGetSymbolAddress(&q, g_spmv_noalloc_bad);
         if (e != cudaSuccess)
             fail(CPDLP_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch) failed: ") +
                                      cudaGetErrorString(e));
-        addr[device] = static_cast<double*>(p);
-    }
+        addr[device].scratch = static_cast<double*>(p);
+        addr[device].bad = static_cast<int*>(q);
+    });
     return addr[device];
 }
 
@@ -137,7 +173,9 @@ template <class T>
 void run(Handle& h, int64_t m, int64_t n, int64_t nnz, const int32_t* rowptr1,
          const int32_t* colval1, const void* nzval, const void* b, void* c, double alpha,
          double beta) {
-    double* scratch = scratch_address(h.device);
+    const NaSymbols sym = symbols(h.device);
+    double* scratch = sym.scratch;
+    CK(cudaMemsetAsync(sym.bad, 0, sizeof(int), h.stream));
     const int use_beta = beta != 0.0;
     const int64_t warps = (nnz + NA_CHUNK - 1) / NA_CHUNK;
     if (warps > 0) {
@@ -174,12 +212,14 @@ void spmv_csr_noalloc(Handle& h, int64_t m, int64_t n, int64_t nnz, const int32_
         run<float>(h, m, n, nnz, rowptr1, colval1, nzval, b, c, alpha, beta);
     else
         fail(CPDLP_ERR_ARGUMENT, "value_type must be CPDLP_VAL_F64 or CPDLP_VAL_F32");
-    CK(cudaStreamSynchronize(h.stream));
+    // stream-ordered read of the flag on the handle's stream (the legacy
+    // default stream is not touched); a copy into pageable memory returns
+    // once it is done
     int bad = 0;
-    CK(cudaMemcpyFromSymbol(&bad, g_spmv_noalloc_bad, sizeof(int)));
+    CK(cudaMemcpyAsync(&bad, symbols(h.device).bad, sizeof(int), cudaMemcpyDeviceToHost,
+                       h.stream));
+    CK(cudaStreamSynchronize(h.stream));
     if (bad) {
-        const int zero = 0;
-        CK(cudaMemcpyToSymbol(g_spmv_noalloc_bad, &zero, sizeof(int)));
         fail(CPDLP_ERR_ARGUMENT,
              "cpdlp_spmv_csr_noalloc: arrays are not a valid 1-based CSR (column outside 1..n "
              "or row pointer outside 1..nnz+1); offending entries were skipped");
