@@ -255,7 +255,7 @@ def solve(milp: MILP, *args):
         lp = native.LPStruct(milp.A.m, milp.A.n, milp.A.colptr, milp.A.rowval, milp.A.nzval,
                              milp.c, milp.lv, milp.uv, milp.lc, milp.uc)
         x, y, st = native.solve_lp(handle, lp, p, sol.x, sol.y)
-        return PrimalDualSolution(x, y), _stats_from(st, [], t0)
+        return PrimalDualSolution(x, y), _stats_from(st, native.solve_history(handle), t0)
     dmilp, sol = preprocess(milp, sol, algo)
     state = initialize(dmilp, sol, algo, starting_time=t0)
     solve_inplace(state)

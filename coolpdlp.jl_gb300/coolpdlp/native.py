@@ -240,6 +240,18 @@ def solve_lp(handle: Handle, lp: LPStruct, params: A.ParamsC, x0=None, y0=None):
     return x, y, st
 
 
+def solve_history(handle: Handle):
+    """cpdlp_solve_history: the error history of the last cpdlp_solve on the
+    handle, as [(kkt_passes, KKTErrorsC)]."""
+    cnt = c_int64()
+    handle.check(handle.lib.cpdlp_solve_history(handle.h, None, None, 0, byref(cnt)))
+    k = cnt.value
+    passes = np.empty(max(k, 1), dtype=np.int64)
+    errs = (A.KKTErrorsC * max(k, 1))()
+    handle.check(handle.lib.cpdlp_solve_history(handle.h, _p64(passes), errs, k, byref(cnt)))
+    return [(int(passes[i]), errs[i]) for i in range(k)]
+
+
 def batch_solve(handle: Handle, lps: list, params: A.ParamsC):
     """cpdlp_batch_solve over LPStructs; returns lists of x, y and StatsC."""
     k = len(lps)

@@ -342,6 +342,20 @@ int cpdlp_state_history(const cpdlp_state* s, int64_t* kkt_passes, cpdlp_kkt_err
     return CPDLP_OK;
 }
 
+int cpdlp_solve_history(const cpdlp_handle* h, int64_t* kkt_passes, cpdlp_kkt_errors* errs,
+                        int64_t capacity, int64_t* count) {
+    if (!h) return CPDLP_ERR_ARGUMENT;
+    const Handle& H0 = *static_cast<const Handle*>(h);
+    const int64_t len = (int64_t)H0.solve_hist_passes.size();
+    const int64_t k = capacity < len ? capacity : len;
+    for (int64_t t = 0; t < k; t++) {
+        if (kkt_passes) kkt_passes[t] = H0.solve_hist_passes[(size_t)t];
+        if (errs) errs[t] = H0.solve_hist_err[(size_t)t];
+    }
+    if (count) *count = len;
+    return CPDLP_OK;
+}
+
 int cpdlp_solve(cpdlp_handle* h, const cpdlp_lp* lp, const cpdlp_params* params,
                 const double* x0, const double* y0, double* x_out, double* y_out,
                 cpdlp_stats* stats) {

@@ -176,6 +176,10 @@ struct Handle {
     cudaStream_t stream = nullptr;
     std::string last_error;
     int num_sms = 0;
+    // error history of the last cpdlp_solve on this handle (every phase of a
+    // mixed-precision solve, passes counted from the start of the solve)
+    std::vector<int64_t> solve_hist_passes;
+    std::vector<cpdlp_kkt_errors> solve_hist_err;
     // reusable small host-pinned area for reductions read back each check
     double* pinned = nullptr;
     size_t pinned_bytes = 0;

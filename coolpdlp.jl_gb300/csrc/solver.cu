@@ -1538,8 +1538,13 @@ struct RefineResult {
     bool progress = true;  // false: a round did not halve the error (continue in FP64)
     int rounds = 0;
     int64_t passes = 0, launches = 0;
+    int64_t first_gain = 0;  // passes the last round needed to first beat its base
     double omega = 1.0;    // primal weight in the original scaling
     cpdlp_kkt_errors err{};
+    // the combined point's errors at every check of every round (original
+    // units), passes counted from the start of the solve
+    std::vector<int64_t> hist_passes;
+    std::vector<cpdlp_kkt_errors> hist_err;
 };
 
 // Rounds from the base point (x0, y0) (FP64, scaled space) until refine_reltol,
@@ -1549,7 +1554,7 @@ struct RefineResult {
 RefineResult refine_residual(Handle& h, ProblemT<float>& P32, ProblemT<double>& P64,
                              StateT<double>& S64, DBuf<double>& x0, DBuf<double>& y0,
                              const cpdlp_params& prm, double t0, double eta, double omega,
-                             int64_t passes_left) {
+                             int64_t passes_left, int64_t passes_before) {
     RefineResult R;
     R.omega = omega;
     cudaStream_t s = h.stream;
@@ -1643,8 +1648,15 @@ RefineResult refine_residual(Handle& h, ProblemT<float>& P32, ProblemT<double>& 
         // the base point never gets worse; the base itself (dx = 0) has r0
         double best_rel = r0;
         bool have_best = false;
+        int64_t first_gain = -1;  // the round's passes when it first beat r0
         int64_t outer_before = S.outer;
-        while (S.solve_blocks(1) == CPDLP_STILL_RUNNING) {
+        for (;;) {
+            const int32_t st = S.solve_blocks(1);
+            if (prm.record_error_history) {
+                R.hist_passes.push_back(passes_before + R.passes + S.kkt_passes);
+                R.hist_err.push_back(e_cur);
+            }
+            if (st != CPDLP_STILL_RUNNING) break;
             // candidates: sol and its average; a restart at the check moved the
             // chosen one (the average if restart_from_avg) into sol
             const bool restarted = S.outer != outer_before;
@@ -1654,6 +1666,7 @@ RefineResult refine_residual(Handle& h, ProblemT<float>& P32, ProblemT<double>& 
             const bool use_avg = r_avg < r_sol;
             const double rc = jl_min(r_sol, r_avg);
             if (rc < best_rel) {
+                if (first_gain < 0) first_gain = S.kkt_passes;
                 best_rel = rc;
                 have_best = true;
                 CK(cudaMemcpyAsync(bdx.p, use_avg ? S.xa[S.cur].p : S.x[S.cur].p,
@@ -1667,8 +1680,13 @@ RefineResult refine_residual(Handle& h, ProblemT<float>& P32, ProblemT<double>& 
                         e_cur.dual / e_cur.dual_scale, e_cur.gap / e_cur.gap_scale, S.omega);
             if (rc <= target) { why = "target"; break; }
             // a later round (the error already small) that has not improved at
-            // all after 3 stall windows (90 checks) ends
-            if (R.rounds > 0 && best_rel >= r0 && S.kkt_passes >= 3 * FP32_STALL_CHECKS * (int64_t)ce) {
+            // all ends after 3 stall windows (90 checks), or after twice the
+            // passes the previous round needed for its first gain if that is
+            // longer (a cold PDLP start on a hard residual LP can take
+            // thousands of checks to beat its base point)
+            if (R.rounds > 0 && best_rel >= r0 &&
+                S.kkt_passes >= std::max<int64_t>(3 * FP32_STALL_CHECKS * (int64_t)ce,
+                                                  2 * R.first_gain)) {
                 why = "no gain";
                 break;
             }
@@ -1689,6 +1707,7 @@ RefineResult refine_residual(Handle& h, ProblemT<float>& P32, ProblemT<double>& 
         R.launches += S.launches + 1;
         R.passes += S.kkt_passes;
         passes_left -= S.kkt_passes;
+        R.first_gain = first_gain > 0 ? first_gain : 0;
         R.omega = S.omega * dp / dd;
         R.rounds++;
         kkt_base(&e);
@@ -1703,6 +1722,10 @@ RefineResult refine_residual(Handle& h, ProblemT<float>& P32, ProblemT<double>& 
             R.progress = false;
             break;
         }
+    }
+    if (prm.record_error_history) {  // the final base point
+        R.hist_passes.push_back(passes_before + R.passes);
+        R.hist_err.push_back(R.err);
     }
     R.launches += S64.launches;
     return R;
@@ -1757,6 +1780,15 @@ double problem_spectral_norm(Handle& h, ProblemBase* P, const cpdlp_params* prm,
 void solve_full(Handle& h, const cpdlp_lp* lp, const cpdlp_params* params, const double* x0,
                 const double* y0, double* x_out, double* y_out, cpdlp_stats* stats) {
     const double t0 = now_seconds();
+    h.solve_hist_passes.clear();
+    h.solve_hist_err.clear();
+    // appends a state's history, its passes offset by `base`
+    auto keep_history = [&h](const StateBase& S, int64_t base) {
+        for (size_t t = 0; t < S.hist_passes.size(); t++) {
+            h.solve_hist_passes.push_back(base + S.hist_passes[t]);
+            h.solve_hist_err.push_back(S.hist_err[t]);
+        }
+    };
     std::unique_ptr<ProblemBase> P(problem_create(h, lp, params));
     std::unique_ptr<StateBase> S(state_create(h, P.get(), params, x0, y0));
     S->starting_time = t0;
@@ -1813,9 +1845,13 @@ void solve_full(Handle& h, const cpdlp_lp* lp, const cpdlp_params* params, const
                 rel_err(S->err), fp32_best, (long long)S->kkt_passes, stalled ? " (stalled)" : "");
     // refinement: the FP32 iterates stalled before the tolerance
     const bool refine = mixed && stalled;
+    keep_history(*S, 0);
     if (!refine) {
         S->solution(x_out, y_out);
-        if (stats) S->stats(stats);
+        if (stats) {
+            S->stats(stats);
+            stats->history_length = (int64_t)h.solve_hist_passes.size();
+        }
         return;
     }
     // Refinement on the residual LP: FP32 rounds from the FP32 solution, with
@@ -1847,7 +1883,11 @@ void solve_full(Handle& h, const cpdlp_lp* lp, const cpdlp_params* params, const
     std::unique_ptr<StateBase> S64(state_create(h, P64.get(), &p64, nullptr, nullptr, eta32, omega32));
     auto& T64 = static_cast<StateT<double>&>(*S64);
     const RefineResult R = refine_residual(h, P32, Q64, T64, bx, by, *params, t0, eta32, omega32,
-                                           params->max_kkt_passes - st32.kkt_passes);
+                                           params->max_kkt_passes - st32.kkt_passes,
+                                           st32.kkt_passes);
+    h.solve_hist_passes.insert(h.solve_hist_passes.end(), R.hist_passes.begin(),
+                               R.hist_passes.end());
+    h.solve_hist_err.insert(h.solve_hist_err.end(), R.hist_err.begin(), R.hist_err.end());
     int64_t passes = st32.kkt_passes + R.passes;
     int64_t launches = st32.kernel_launches + R.launches;
     if (R.progress || R.status != CPDLP_STILL_RUNNING) {
@@ -1868,6 +1908,7 @@ void solve_full(Handle& h, const cpdlp_lp* lp, const cpdlp_params* params, const
             stats->omega = R.omega;
             stats->time_elapsed = now_seconds() - t0;
             stats->kernel_launches = launches;
+            stats->history_length = (int64_t)h.solve_hist_passes.size();
         }
         return;
     }
@@ -1890,13 +1931,33 @@ void solve_full(Handle& h, const cpdlp_lp* lp, const cpdlp_params* params, const
         state_create(h, P64.get(), &p64, xs.data(), ys.data(), eta32, R.omega));
     C64->starting_time = t0;
     C64->solve();
-    C64->solution(x_out, y_out);
+    keep_history(*C64, passes);
+    // the continuation can end at a limit with a worse current iterate than
+    // the refined point it started from (PDLP's iterate error is not
+    // monotone): the refined point is returned then
+    const bool keep_base = C64->status != CPDLP_OPTIMAL && !(rel_err(C64->err) <= rel_err(R.err));
+    if (keep_base) {
+        if (x_out && n > 0) memcpy(x_out, xs.data(), sizeof(double) * n);
+        if (y_out && m > 0) memcpy(y_out, ys.data(), sizeof(double) * m);
+        if (params->record_error_history) {  // the returned point's errors close the history
+            h.solve_hist_passes.push_back(passes + C64->kkt_passes);
+            h.solve_hist_err.push_back(R.err);
+        }
+    } else {
+        C64->solution(x_out, y_out);
+    }
     if (stats) {
         C64->stats(stats);
+        if (keep_base) stats->err = R.err;
         stats->refine_kkt_passes = R.passes + C64->kkt_passes;
         stats->kkt_passes = passes + C64->kkt_passes;
         stats->kernel_launches += launches;
+        stats->history_length = (int64_t)h.solve_hist_passes.size();
     }
+    if (trace_on())
+        fprintf(stderr, "[cpdlp refine] FP64 continuation: rel %.3e after %lld passes%s\n",
+                rel_err(C64->err), (long long)C64->kkt_passes,
+                keep_base ? " (worse than the refined point, which is returned)" : "");
 }
 
 void problem_scaling(Handle& h, ProblemBase* P, double* d1, double* d2) {

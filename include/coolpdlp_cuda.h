@@ -334,6 +334,18 @@ int cpdlp_solve(cpdlp_handle* h, const cpdlp_lp* lp, const cpdlp_params* params,
                 const double* x0, const double* y0, double* x_out, double* y_out,
                 cpdlp_stats* stats);
 
+/* stats.error_history (termination.jl:44-76, pushed at common.jl:226-228) of
+ * the last cpdlp_solve on this handle: copies up to `capacity` entries,
+ * `count` receives the full length.  With mixed precision (FP32 iterates and
+ * refine_reltol > 0) it holds every phase in order, passes counted from the
+ * start of the solve: the FP32 run's checks, the combined point's errors at
+ * every check of the refinement rounds plus the final refined point, then the
+ * FP64 continuation's checks if one ran (and the returned point's errors if
+ * the continuation ended worse than it).  Empty when record_error_history is
+ * 0 or the problem took the empty-problem early exit (common.jl:194-198). */
+int cpdlp_solve_history(const cpdlp_handle* h, int64_t* kkt_passes, cpdlp_kkt_errors* errs,
+                        int64_t capacity, int64_t* count);
+
 /* spectral_norm(A, A') (linalg.jl:86-96) of the problem's scaled matrix in its
  * float type, with the power-method settings of `params`. */
 int cpdlp_problem_spectral_norm(cpdlp_handle* h, cpdlp_problem* p, const cpdlp_params* params,

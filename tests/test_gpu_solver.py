@@ -193,6 +193,19 @@ def test_fp32_with_fp64_refinement_reaches_1e8(handle, oracle):
     assert st.refine_kkt_passes > 0 and st.kkt_passes > st.refine_kkt_passes
     og, oo = float(lp.c @ sol.x), float(lp.c @ xo)
     assert abs(og - oo) <= 1e-6 * max(1.0, abs(oo)), (og, oo)
+    # error_history covers every phase (common.jl:226-228): FP32 checks at
+    # multiples of check_every, then the refinement checks; passes never
+    # decrease, the last entry is the final error
+    hist = st.error_history
+    assert len(hist) >= 2
+    passes = [p for p, _ in hist]
+    assert passes == sorted(passes) and passes[-1] == st.kkt_passes
+    assert passes[0] % 100 == 0 and passes[0] > 0
+    assert cp.relative(hist[-1][1]) == cp.relative(st.err)
+    assert any(p > st.kkt_passes - st.refine_kkt_passes for p in passes)
+    _, st_nohist = cp.solve(milp, cp.PDLP(np.float32, refine_reltol=1e-8, max_kkt_passes=200000,
+                                          record_error_history=0))
+    assert st_nohist.error_history == []
     # the same through the C ABI (cpdlp_solve)
     from coolpdlp import native, _abi as A
     L = native.LPStruct(lp.m, lp.n, lp.colptr, lp.rowval, lp.nzval, lp.c, lp.lv, lp.uv, lp.lc, lp.uc)
