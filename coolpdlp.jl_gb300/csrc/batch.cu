@@ -131,6 +131,7 @@ struct BatchArgs {
     CsrView<T, T> A, At;
     const T *c, *lv, *uv, *lc, *uc;
     const double *invD1, *invD2, *D1, *D2;
+    const T *invD1t, *invD2t;   // 1 ./ D1, 1 ./ D2 in T (the KKT terms)
     T *x[2], *y[2], *xa[2], *ya[2], *xr, *yr, *xbar;
     const double* theta;     // per LP: the power method's estimate of |A|^2
     const int64_t* power_iters;
@@ -292,7 +293,7 @@ __device__ __forceinline__ void lp_kkt(const BatchArgs<T>& g, const BatchCtl& C,
     double rs[2], cs[3];
     {
         KktRowEpi<T, 1> re;
-        re.lc = g.lc; re.uc = g.uc; re.invD1 = g.invD1; re.y[0] = yv;
+        re.lc = g.lc; re.uc = g.uc; re.invD1 = g.invD1t; re.y[0] = yv;
         re.block_out = nullptr; re.long_out = g.longA;
         typename KktRowEpi<T, 1>::Acc a;
         re.init(a);
@@ -302,7 +303,7 @@ __device__ __forceinline__ void lp_kkt(const BatchArgs<T>& g, const BatchCtl& C,
     }
     {
         KktColEpi<T, 1> ce;
-        ce.c = g.c; ce.lv = g.lv; ce.uv = g.uv; ce.invD2 = g.invD2; ce.x[0] = xv;
+        ce.c = g.c; ce.lv = g.lv; ce.uv = g.uv; ce.invD2 = g.invD2t; ce.x[0] = xv;
         ce.block_out = nullptr; ce.long_out = g.longAt;
         typename KktColEpi<T, 1>::Acc a;
         ce.init(a);
@@ -1088,6 +1089,7 @@ struct Run : RunBase {
                              planAt.ltasks.p, planAt.nltasks, planAt.counters.p, partAt.p};
         g.c = P.c.p; g.lv = P.lv.p; g.uv = P.uv.p; g.lc = P.lc.p; g.uc = P.uc.p;
         g.invD1 = P.invD1.p; g.invD2 = P.invD2.p; g.D1 = P.D1.p; g.D2 = P.D2.p;
+        g.invD1t = P.invD1_T(); g.invD2t = P.invD2_T();
         for (int b = 0; b < 2; b++) { g.x[b] = bx[b].p; g.y[b] = by[b].p; g.xa[b] = bxa[b].p; g.ya[b] = bya[b].p; }
         g.xr = bxr.p; g.yr = byr.p; g.xbar = bxbar.p;
         g.theta = d_theta.p;

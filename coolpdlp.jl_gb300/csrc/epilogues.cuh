@@ -160,13 +160,22 @@ struct DualEpi {
     __device__ void finish(Acc&) {}
 };
 
+// The KKT pass evaluates NV (1 or 4) iterates (x_p, y_p) in one launch per
+// side (four: packed gathers, short_tile4, whose iterate index is a constant
+// at every epilogue call, so the accumulators stay in registers).  A block of
+// W warps reduces its threads' FP64 sums in a fixed order; an iterate's sums
+// do not depend on the other iterates of the launch.
+// Each row's terms are computed in the iterate type T (FP64 arithmetic is
+// scarce on GB300, and a term's own rounding is relative to that term) and
+// accumulated in FP64: the squares from the T value widened, so they cannot
+// overflow.  With T = double this is the FP64 evaluation of errors.jl.
 // KKT row side (errors.jl:73-80, 87-89): s = (A x_p)_i (SCALED: the product
 // gathered D2 x_p and s is multiplied by d1_i)
-template <class T, int NV, bool SCALED = false>
+template <class T, int NV, bool SCALED = false, int W = TILE_WARPS>
 struct KktRowEpi {
     const T* __restrict__ lc;
     const T* __restrict__ uc;
-    const double* __restrict__ invD1;
+    const T* __restrict__ invD1;   // 1 ./ D1 in T
     const T* y[NV];
     double* block_out;
     double* long_out;
@@ -182,12 +191,11 @@ struct KktRowEpi {
     __device__ __forceinline__ Pre pre_global(int) const { return Pre{}; }
     __device__ __forceinline__ void terms(int p, int i, T s, double& pr2, double& pc) const {
         if (SCALED) s = mul_rn(dsc[i], s);
-        const double l = (double)lc[i], u = (double)uc[i];
-        const double sd = (double)s;
-        const double d = __dmul_rn(invD1[i], __dsub_rn(sd, proj_box(sd, l, u)));
+        const T l = lc[i], u = uc[i];
+        const double d = (double)mul_rn(invD1[i], sub_rn(s, proj_box(s, l, u)));
         pr2 = __dmul_rn(d, d);
-        const double yy = (double)y[p][i];  // y[] is not restrict: a coherent load
-        pc = __dsub_rn(safeprod_left(u, pos_part(-yy)), safeprod_left(l, neg_part(-yy)));
+        const T yy = pick(y, p)[i];  // y[] is not restrict: a coherent load
+        pc = (double)sub_rn(safeprod_left(u, pos_part(-yy)), safeprod_left(l, neg_part(-yy)));
     }
     __device__ __forceinline__ void row(int p, int i, T s, const Pre&, Acc& a) {
         double pr2, pc;
@@ -201,17 +209,17 @@ struct KktRowEpi {
         long_out[(size_t)lid * 2 * NV + 2 * p] = pr2;
         long_out[(size_t)lid * 2 * NV + 2 * p + 1] = pc;
     }
-    __device__ void finish(Acc& a) { block_reduce_store<2 * NV>(a.v, block_out); }
+    __device__ void finish(Acc& a) { block_reduce_store<2 * NV, W>(a.v, block_out); }
 };
 
 // KKT column side (errors.jl:74-75, 82-95): s = (A' y_p)_j (SCALED: the
 // product gathered D1 y_p and s is multiplied by d2_j)
-template <class T, int NV, bool SCALED = false>
+template <class T, int NV, bool SCALED = false, int W = TILE_WARPS>
 struct KktColEpi {
     const T* __restrict__ c;
     const T* __restrict__ lv;
     const T* __restrict__ uv;
-    const double* __restrict__ invD2;
+    const T* __restrict__ invD2;   // 1 ./ D2 in T
     const T* x[NV];
     double* block_out;
     double* long_out;
@@ -226,13 +234,13 @@ struct KktColEpi {
     __device__ __forceinline__ void terms(int p, int j, T s, double& du2, double& pv,
                                           double& cx) const {
         if (SCALED) s = mul_rn(dsc[j], s);
-        const double cj = (double)c[j], l = (double)lv[j], u = (double)uv[j];
-        const double g = __dsub_rn(cj, (double)s);
-        const double r = proj_multiplier(g, l, u);
-        const double d = __dmul_rn(invD2[j], __dsub_rn(g, r));
+        const T cj = c[j], l = lv[j], u = uv[j];
+        const T g = sub_rn(cj, s);
+        const T r = proj_multiplier(g, l, u);
+        const double d = (double)mul_rn(invD2[j], sub_rn(g, r));
         du2 = __dmul_rn(d, d);
-        pv = __dsub_rn(safeprod_left(u, pos_part(-r)), safeprod_left(l, neg_part(-r)));
-        cx = __dmul_rn(cj, (double)x[p][j]);
+        pv = (double)sub_rn(safeprod_left(u, pos_part(-r)), safeprod_left(l, neg_part(-r)));
+        cx = (double)mul_rn(cj, pick(x, p)[j]);
     }
     __device__ __forceinline__ void row(int p, int j, T s, const Pre&, Acc& a) {
         double du2, pv, cx;
@@ -249,7 +257,7 @@ struct KktColEpi {
         o[1] = pv;
         o[2] = cx;
     }
-    __device__ void finish(Acc& a) { block_reduce_store<3 * NV>(a.v, block_out); }
+    __device__ void finish(Acc& a) { block_reduce_store<3 * NV, W>(a.v, block_out); }
 };
 
 // Infeasibility certificates (an extension; the reference has no detection).

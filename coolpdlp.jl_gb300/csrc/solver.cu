@@ -151,6 +151,29 @@ __global__ void k_mul_vec(const T* __restrict__ a, const T* __restrict__ b, T* _
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < len) out[i] = mul_rn(a[i], b[i]);
 }
+// The gathered vectors of a KKT pass: NV iterates interleaved (X[NV*j + p] =
+// x_p[j]), times the narrow matrix's column scale d (D2 for x, D1 for y) when
+// d is non-null; y alike.  With NV = 4 one request per nonzero gathers all four.
+template <class T, int NV>
+struct PackSrc {
+    const T* v[NV];
+};
+template <class T, int NV>
+__global__ void k_pack(PackSrc<T, NV> xs, const T* __restrict__ dx, int64_t n, T* __restrict__ X,
+                       PackSrc<T, NV> ys, const T* __restrict__ dy, int64_t m,
+                       T* __restrict__ Y) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
+        const T d = dx ? dx[j] : T(1);
+#pragma unroll
+        for (int p = 0; p < NV; p++) X[NV * j + p] = dx ? mul_rn(xs.v[p][j], d) : xs.v[p][j];
+    }
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += stride) {
+        const T d = dy ? dy[i] : T(1);
+#pragma unroll
+        for (int p = 0; p < NV; p++) Y[NV * i + p] = dy ? mul_rn(ys.v[p][i], d) : ys.v[p][i];
+    }
+}
 // Infeasibility certificates (an extension): the rays are the change of the
 // iterates since the previous check, x projected onto the recession cone of
 // [lv, uv] and y onto the multiplier cone of [lc, uc] (>= 0 with only lc
@@ -548,6 +571,13 @@ ProblemBase* make_problem(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm
         k_narrow<T><<<gn, 256, 0, s>>>(D2.p, P->d2t.p, n);
         CK_LAUNCH();
     }
+    if constexpr (!std::is_same<T, double>::value) {
+        P->invD1t.alloc(mz);
+        P->invD2t.alloc(nzv);
+        k_narrow<T><<<gm, 256, 0, s>>>(P->invD1.p, P->invD1t.p, m);
+        k_narrow<T><<<gn, 256, 0, s>>>(P->invD2.p, P->invD2t.p, n);
+        CK_LAUNCH();
+    }
     P->D1 = std::move(D1);
     P->D2 = std::move(D2);
     if (!plans) {  // the batched solver partitions the matrices itself
@@ -609,8 +639,11 @@ ProblemBase* make_problem(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm
     P->partAt.alloc((size_t)(P->planAt.npieces > 0 ? P->planAt.npieces : 1) * 4);
     P->rows_A_partials = (int64_t)tiles_grid(P->planA) + P->planA.nlong;
     P->rows_At_partials = (int64_t)tiles_grid(P->planAt) + P->planAt.nlong;
+    P->rows_A_kkt = (int64_t)tiles_grid(P->planA, kkt_warps<T>()) + P->planA.nlong;
+    P->rows_At_kkt = (int64_t)tiles_grid(P->planAt, kkt_warps<T>()) + P->planAt.nlong;
     int64_t rows_max = std::max<int64_t>(std::max(P->rows_A_partials, P->rows_At_partials),
                                          (int64_t)h.num_sms * 4 + 8);
+    rows_max = std::max<int64_t>(rows_max, std::max(P->rows_A_kkt, P->rows_At_kkt));
     P->red_rows.alloc((size_t)rows_max * 12);
     P->red_cols.alloc((size_t)rows_max * 12);
     P->red_out.alloc(64);
@@ -785,9 +818,10 @@ struct StateT : StateBase {
     DBuf<T> x[2], y[2], xa[2], ya[2], xr, yr, xbar;
     int cur = 0;  // sol = (x[cur], y[cur]); sol_last = (x[cur^1], y[cur^1]); same for averages
     // narrow +-1 storage: ys[b] = D1 .* y[b] (the primal product's gather; the
-    // dual step writes it beside y), xbar holds D2 .* xbar, and the KKT
-    // products gather the scratch copies kx = D2 .* x, ky = D1 .* y
-    DBuf<T> ys[2], kx[4], ky[4];
+    // dual step writes it beside y), xbar holds D2 .* xbar
+    DBuf<T> ys[2];
+    // the KKT pass's packed (and, for a narrow matrix, scaled) gathered vectors
+    DBuf<T> kx4, ky4;
     // refinement round on the residual LP: the dual step's activity offset
     // (scaled base multipliers), and the KKT evaluation of the combined iterate
     // (base + correction) that replaces the state's own
@@ -939,43 +973,68 @@ struct StateT : StateBase {
         CK(cudaStreamSynchronize(h->stream));
     }
 
-    // KKT errors (errors.jl:65-109) of NV (x, y) pairs: one row-side and one
-    // column-side tile pass per pair, each pair's FP64 block partials in its
-    // own segment, one segmented reduction per side and one read-back.  A
-    // pair's result does not depend on its slot (same kernels, same order).
-    void enqueue_kkt_pair(int p, const T* xp, const T* yp) {
+    // KKT errors (errors.jl:65-109) of NV (1 or 4) (x, y) pairs in ONE
+    // row-side and ONE column-side tile pass.  Four pairs are packed first
+    // (x4[4j + p], y4[4i + p]: one request per nonzero gathers all four, and
+    // the tile's indices and values are read once); a narrow matrix's pack
+    // also applies D2 / D1, the scales its products need.  Each pass leaves
+    // FP64 block partials (2 NV row-side, 3 NV column-side values per block);
+    // a pair's sums do not depend on the other pairs of the pass.
+    template <int NV>
+    void enqueue_kkt(const T* const (&xs)[NV], const T* const (&ys)[NV]) {
+        static_assert(NV == 1 || NV == 4, "one or four iterates per KKT pass");
         ProblemT<T>& P = *PT;
         cudaStream_t s = h->stream;
-        if (P.pm1) {
-            if (P.n > 0) k_mul_vec<T><<<grid_for(P.n, 256), 256, 0, s>>>(xp, P.d2t.p, kx[p].p, P.n);
-            if (P.m > 0) k_mul_vec<T><<<grid_for(P.m, 256), 256, 0, s>>>(yp, P.d1t.p, ky[p].p, P.m);
+        const size_t nz = (size_t)std::max<int64_t>(P.n, 1), mz = (size_t)std::max<int64_t>(P.m, 1);
+        const T* gx = xs[0];
+        const T* gy = ys[0];
+        if (NV == 4 || P.pm1) {
+            if (!kx4.p) {
+                kx4.alloc(4 * nz);
+                ky4.alloc(4 * mz);
+            }
+            PackSrc<T, NV> px, py;
+            for (int p = 0; p < NV; p++) {
+                px.v[p] = xs[p];
+                py.v[p] = ys[p];
+            }
+            k_pack<T, NV><<<red_grid(*h, std::max(P.m, P.n)), RED_THREADS, 0, s>>>(
+                px, P.pm1 ? P.d2t.p : nullptr, P.n, kx4.p, py, P.pm1 ? P.d1t.p : nullptr, P.m,
+                ky4.p);
             CK_LAUNCH();
-            kkt_pair_impl<true>(p, xp, yp, kx[p].p, ky[p].p, view_A_pm1(P), view_At_pm1(P), s);
-        } else {
-            kkt_pair_impl<false>(p, xp, yp, xp, yp, view_A(P), view_At(P), s);
+            launches += 1;
+            gx = kx4.p;
+            gy = ky4.p;
         }
+        if (P.pm1) kkt_impl<true, NV>(xs, ys, gx, gy, view_A_pm1(P), view_At_pm1(P));
+        else kkt_impl<false, NV>(xs, ys, gx, gy, view_A(P), view_At(P));
     }
-    // gx / gy: the vectors the two products gather (x, y, or their D2 / D1
-    // pre-scaled copies for a narrow matrix)
-    template <bool SC, class VA, class VAt>
-    void kkt_pair_impl(int p, const T* xp, const T* yp, const T* gx, const T* gy, const VA& vA,
-                       const VAt& vAt, cudaStream_t s) {
+    template <bool SC, int NV, class VA, class VAt>
+    void kkt_impl(const T* const (&xs)[NV], const T* const (&ys)[NV], const T* gx, const T* gy,
+                  const VA& vA, const VAt& vAt) {
         ProblemT<T>& P = *PT;
-        const unsigned gA = tiles_grid(P.planA), gAt = tiles_grid(P.planAt);
-        KktRowEpi<T, 1, SC> re;
-        re.lc = P.lc.p; re.uc = P.uc.p; re.invD1 = P.invD1.p;
-        re.y[0] = yp;
-        re.block_out = P.red_rows.p + (size_t)p * P.rows_A_partials * 2;
-        re.long_out = re.block_out + (size_t)gA * 2;
+        cudaStream_t s = h->stream;
+        constexpr int W = kkt_warps<T>();
+        const unsigned gA = tiles_grid(P.planA, W), gAt = tiles_grid(P.planAt, W);
+        KktRowEpi<T, NV, SC, W> re;
+        re.lc = P.lc.p; re.uc = P.uc.p; re.invD1 = P.invD1_T();
+        for (int p = 0; p < NV; p++) re.y[p] = ys[p];
+        re.block_out = P.red_rows.p;
+        re.long_out = re.block_out + (size_t)gA * 2 * NV;
         re.dsc = SC ? P.d1t.p : nullptr;
-        launch_tiles<1>(P.planA, vA, VecSet<T, 1>{{gx}}, re, s);
-        KktColEpi<T, 1, SC> ce;
-        ce.c = P.c.p; ce.lv = P.lv.p; ce.uv = P.uv.p; ce.invD2 = P.invD2.p;
-        ce.x[0] = xp;
-        ce.block_out = P.red_cols.p + (size_t)p * P.rows_At_partials * 3;
-        ce.long_out = ce.block_out + (size_t)gAt * 3;
+        KktColEpi<T, NV, SC, W> ce;
+        ce.c = P.c.p; ce.lv = P.lv.p; ce.uv = P.uv.p; ce.invD2 = P.invD2_T();
+        for (int p = 0; p < NV; p++) ce.x[p] = xs[p];
+        ce.block_out = P.red_cols.p;
+        ce.long_out = ce.block_out + (size_t)gAt * 3 * NV;
         ce.dsc = SC ? P.d2t.p : nullptr;
-        launch_tiles<1>(P.planAt, vAt, VecSet<T, 1>{{gy}}, ce, s);
+        if constexpr (NV == 4) {
+            launch_tiles4<W>(P.planA, vA, gx, re, s);
+            launch_tiles4<W>(P.planAt, vAt, gy, ce, s);
+        } else {
+            launch_tiles_w<W>(P.planA, vA, VecSet<T, 1>{{gx}}, re, s);
+            launch_tiles_w<W>(P.planAt, vAt, VecSet<T, 1>{{gy}}, ce, s);
+        }
     }
 
     template <int NV>
@@ -986,11 +1045,10 @@ struct StateT : StateBase {
         }
         ProblemT<T>& P = *PT;
         cudaStream_t s = h->stream;
-        for (int p = 0; p < NV; p++) enqueue_kkt_pair(p, xs[p], ys[p]);
-        reduce_partials(P.red_rows.p, P.rows_A_partials, 2, P.red_out.p, s, NV);
-        reduce_partials(P.red_cols.p, P.rows_At_partials, 3, P.red_out.p + 2 * NV, s, NV);
-        launches += NV * (tiles_launches(P.planA) + tiles_launches(P.planAt)) + 2 +
-                    (P.pm1 ? NV * ((P.n > 0) + (P.m > 0)) : 0);
+        enqueue_kkt<NV>(xs, ys);
+        reduce_partials(P.red_rows.p, P.rows_A_kkt, 2 * NV, P.red_out.p, s);
+        reduce_partials(P.red_cols.p, P.rows_At_kkt, 3 * NV, P.red_out.p + 2 * NV, s);
+        launches += tiles_launches(P.planA) + tiles_launches(P.planAt) + 2;
         double* pin = h->pinned_area(sizeof(double) * 64);
         CK(cudaMemcpyAsync(pin, P.red_out.p, sizeof(double) * 5 * NV, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
@@ -1277,10 +1335,9 @@ struct StateT : StateBase {
             launch_dual(y[o].p, ty.p, P.pm1 ? tys.p : nullptr, ya[o].p, tya.p, xbar.p, coef1.p, s);
         });
         ms[2] = timed([&] {
-            enqueue_kkt_pair(0, x[cur].p, y[cur].p);
-            enqueue_kkt_pair(1, xa[cur].p, ya[cur].p);
-            enqueue_kkt_pair(2, x[cur ^ 1].p, y[cur ^ 1].p);
-            enqueue_kkt_pair(3, xa[cur ^ 1].p, ya[cur ^ 1].p);
+            const T* const xs4[4] = {x[cur].p, xa[cur].p, x[cur ^ 1].p, xa[cur ^ 1].p};
+            const T* const ys4[4] = {y[cur].p, ya[cur].p, y[cur ^ 1].p, ya[cur ^ 1].p};
+            enqueue_kkt<4>(xs4, ys4);
         });
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
@@ -1299,14 +1356,14 @@ struct StateT : StateBase {
         // write y+ (+ avg read/write); narrow: no values, read d1, write D1 y+
         bytes[1] = nnz * (sv + si) + (m + 1) * si + sf * (n + (avg ? 6 : 4) * m) +
                    (P.pm1 ? 2 * sf * m : 0.0);
-        // KKT of 4 pairs: both matrices once (the minimum; the kernels read
-        // them once per pair), 4 gathered vectors per side, bounds, the 4
-        // epilogue vectors per side, D1/D2 inverses (FP64); narrow: the scale
-        // reads per pair and the pre-scaling passes (read x, d2, write D2 x;
-        // the same for y)
+        // KKT of 4 pairs in one pass per side: both matrices once, the 4
+        // gathered vectors per side (packed: counted once), bounds, the 4
+        // epilogue vectors per side, D1/D2 inverses (in T); narrow: the row
+        // scales and the column scales of the pack, once each.  The pack
+        // itself (read 4 vectors, write them interleaved) is not counted.
         bytes[2] = 2 * nnz * (sv + si) + (m + n + 2) * si + sf * (4 * n + 4 * m) +
-                   sf * (2 * m + 4 * m) + sf * (3 * n + 4 * n) + 8.0 * (m + n) +
-                   (P.pm1 ? sf * (4 * (m + n) + 12 * (m + n)) : 0.0);
+                   sf * (2 * m + 4 * m) + sf * (3 * n + 4 * n) + sf * (m + n) +
+                   (P.pm1 ? sf * 2 * (m + n) : 0.0);
     }
 
     void early_exit_zero_problem() override {
@@ -1390,10 +1447,6 @@ StateBase* make_state(Handle& h, ProblemT<T>* P, const cpdlp_params* prm, const 
     CK(cudaMemsetAsync(S->xbar.p, 0, sizeof(T) * nz, s));
     if (P->pm1) {
         for (int b = 0; b < 2; b++) S->ys[b].alloc(mz);
-        for (int q = 0; q < 4; q++) {
-            S->kx[q].alloc(nz);
-            S->ky[q].alloc(mz);
-        }
         CK(cudaMemsetAsync(S->ys[1].p, 0, sizeof(T) * mz, s));
         if (m > 0) {
             k_mul_vec<T><<<grid_for(m, 256), 256, 0, s>>>(S->y[0].p, P->d1t.p, S->ys[0].p, m);

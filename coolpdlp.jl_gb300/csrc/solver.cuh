@@ -1,6 +1,8 @@
 // solver.cuh -- single-LP PDLP / PDHG on the device.
 #pragma once
 
+#include <type_traits>
+
 #include "cpdlp_common.cuh"
 #include "sparse_build.cuh"
 #include "tiles.cuh"
@@ -48,6 +50,8 @@ struct ProblemBase {
     // reduction scratch (FP64 block partials) sized for NVEC = 4
     DBuf<double> red_rows, red_cols, red_out;
     int64_t rows_A_partials = 0, rows_At_partials = 0;
+    // block-partial rows of the KKT pass (kkt_warps<T>() per block)
+    int64_t rows_A_kkt = 0, rows_At_kkt = 0;
 };
 
 template <class T>
@@ -59,6 +63,17 @@ struct ProblemT : ProblemBase {
     // value arrays are empty, and the products apply d1 / d2 (as T)
     bool pm1 = false;
     DBuf<T> d1t, d2t;
+    // 1 ./ D1 and 1 ./ D2 in T for the KKT terms (FP32 problems keep a copy;
+    // FP64 problems use invD1 / invD2 themselves)
+    DBuf<T> invD1t, invD2t;
+    const T* invD1_T() const {
+        if constexpr (std::is_same<T, double>::value) return invD1.p;
+        else return invD1t.p;
+    }
+    const T* invD2_T() const {
+        if constexpr (std::is_same<T, double>::value) return invD2.p;
+        else return invD2t.p;
+    }
 };
 
 struct StateBase {

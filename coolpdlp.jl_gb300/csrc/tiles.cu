@@ -87,33 +87,49 @@ void build_tile_plan(const std::vector<int32_t>& ptr, int32_t rows, int items, T
 }
 
 namespace {
-// block b reduces segment b: rows [b*nrows, (b+1)*nrows) -> out[b*q + j]
+constexpr int RED_MAX_Q = 12;
+// block b reduces segment b: rows [b*nrows, (b+1)*nrows) -> out[b*q + j].
+// Each thread adds whole rows (q contiguous values) in row order, then the
+// block sums its threads' values in a fixed tree: the result depends only on
+// the data and the block size.
 __global__ void k_reduce_partials(const double* __restrict__ part, int64_t nrows, int q,
                                   double* __restrict__ out) {
-    __shared__ double red[32];
+    __shared__ double red[32][RED_MAX_Q];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     part += (size_t)blockIdx.x * nrows * q;
     out += (size_t)blockIdx.x * q;
-    for (int j = 0; j < q; j++) {
-        double s = 0.0;
-        for (int64_t r = threadIdx.x; r < nrows; r += blockDim.x) s += part[r * q + j];
+    double acc[RED_MAX_Q];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (lane == 0) red[w] = s;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double t = 0.0;
-            for (int ww = 0; ww < (int)(blockDim.x >> 5); ww++) t += red[ww];
-            out[j] = t;
-        }
-        __syncthreads();
+    for (int j = 0; j < RED_MAX_Q; j++) acc[j] = 0.0;
+    for (int64_t r = threadIdx.x; r < nrows; r += blockDim.x) {
+        const double* row = part + r * q;
+#pragma unroll
+        for (int j = 0; j < RED_MAX_Q; j++)
+            if (j < q) acc[j] += row[j];
+    }
+#pragma unroll
+    for (int j = 0; j < RED_MAX_Q; j++) {
+        if (j >= q) break;
+        double x = acc[j];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if (lane == 0) red[w][j] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < q) {
+        double t = 0.0;
+        for (int ww = 0; ww < (int)(blockDim.x >> 5); ww++) t += red[ww][threadIdx.x];
+        out[threadIdx.x] = t;
     }
 }
 }  // namespace
 
 void reduce_partials(const double* partials, int64_t nrows, int q, double* out, cudaStream_t s,
                      int nseg) {
-    k_reduce_partials<<<nseg, 1024, 0, s>>>(partials, nrows, q, out);
+    if (q < 1 || q > RED_MAX_Q) fail(CPDLP_ERR_ARGUMENT, "reduce_partials: 1..12 values per row");
+    // fewer threads for short inputs (the launch cost dominates there)
+    const int threads = nrows >= 8192 ? 1024 : nrows >= 1024 ? 256 : 64;
+    k_reduce_partials<<<nseg, threads, 0, s>>>(partials, nrows, q, out);
     CK_LAUNCH();
 }
 

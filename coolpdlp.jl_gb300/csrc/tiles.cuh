@@ -99,6 +99,17 @@ struct VecSet {
     const T* v[NVEC];
 };
 
+// v[p] for a runtime p without indexing a parameter array dynamically (which
+// would copy it to local memory)
+template <class T, int N>
+__device__ __forceinline__ const T* pick(const T* const (&v)[N], int p) {
+    const T* r = v[0];
+#pragma unroll
+    for (int q = 1; q < N; q++)
+        if (p == q) r = v[q];
+    return r;
+}
+
 // ---- 4-element chunk loads (the chunk start is a multiple of 4 elements) ----
 // Streaming (evict-first) loads written as volatile PTX: they keep their
 // program order, so a batch of them is issued back to back before the first
@@ -140,6 +151,15 @@ __device__ __forceinline__ double gather(const double* p) {
     else asm volatile("ld.global.nc.f64 %0, [%1];" : "=d"(v) : "l"(p));
     return v;
 }
+// 16-byte asynchronous global -> shared copy (both addresses 16-byte aligned):
+// a gather that holds no registers while in flight
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.wait_all;" ::: "memory");
+}
 template <class V, class T>
 __device__ __forceinline__ T load1v(const V* p) {
     return (T)__ldcs(p);
@@ -158,6 +178,13 @@ __device__ __forceinline__ uint64_t global_ns() {
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
 }
+
+constexpr int TILE_WARPS = 8;
+// Warps per block of the KKT pass: the four iterates' gathered values of a
+// whole tile live in shared memory, within the static 48 KB (4 warps for FP32
+// iterates, 2 for FP64).
+template <class T>
+constexpr int kkt_warps() { return sizeof(T) == 4 ? 4 : 2; }
 
 // One warp, one short tile.  All loads of a phase are volatile PTX issued back
 // to back, so they are in flight together: (1) the tile's indices and values
@@ -202,6 +229,7 @@ __device__ __forceinline__ void short_tile(const CsrView<V, T>& A, const VecSet<
     // pass) this keeps one batch of gathers in registers instead of all of them
 #pragma unroll 1
     for (int p = 0; p < NVEC; p++) {
+        const T* xv = pick(xs.v, p);
         T xg[NV4][4];
 #pragma unroll
         for (int j = 0; j < NV4; j++) {
@@ -209,7 +237,7 @@ __device__ __forceinline__ void short_tile(const CsrView<V, T>& A, const VecSet<
 #pragma unroll
             for (int q = 0; q < 4; q++)
                 xg[j][q] = (e + q >= nz0 && e + q < nz1)
-                               ? gather<COH>(xs.v[p] + (is_pm1<V>::value ? pm1_col(cc[j][q]) : cc[j][q]))
+                               ? gather<COH>(xv + (is_pm1<V>::value ? pm1_col(cc[j][q]) : cc[j][q]))
                                : T(0);
         }
 #pragma unroll
@@ -235,34 +263,65 @@ __device__ __forceinline__ void short_tile(const CsrView<V, T>& A, const VecSet<
     }
 }
 
-// One warp, one TILE-sized piece of a row longer than LONG_ROW: lane-strided
-// coalesced loads, lane partial sums, a fixed shuffle tree.  Multi-piece rows
-// combine through scratch slots: the warp that completes the row (atomic
-// counter, no waiting) adds the partials in piece order and applies the
-// epilogue.
+// One warp, one TILE-sized piece of a row longer than LONG_ROW.  The piece's
+// indices and values are loaded with 128-bit loads over the 4-element-aligned
+// window and its gathers are issued in one batch, as in a short tile; each
+// lane sums its own elements in ascending order, then a fixed shuffle tree
+// adds the lanes.  Multi-piece rows combine through scratch slots: the warp
+// that completes the row (atomic counter, no waiting) adds the partials in
+// piece order and applies the epilogue.
 template <int ITEMS, int NVEC, class V, class T, class Epi, bool COH>
 __device__ __forceinline__ void long_piece(const CsrView<V, T>& A, const VecSet<T, NVEC, COH>& xs,
                                            Epi& epi, typename Epi::Acc& acc, int4 t, int lane) {
     constexpr int TILE = 32 * ITEMS;
+    constexpr int NV4 = ITEMS / 4 + 1;
     const int row = t.x, piece = -t.y - 1, lid = t.z, base_slot = t.w;
     const int rb = ld_keep(A.ptr + row), re = ld_keep(A.ptr + row + 1);
     const int npieces = (re - rb + TILE - 1) / TILE;
     const int a = rb + piece * TILE;
     const int b = min(a + TILE, re);
-    T s[NVEC];
+    const int base = a & ~3;
+    int cc[NV4][4];
+    T vv[NV4][4];
 #pragma unroll
-    for (int p = 0; p < NVEC; p++) s[p] = T(0);
-    for (int e = a + lane; e < b; e += 32) {
-        const int cc = __ldcs(A.idx + e);
-        if constexpr (is_pm1<V>::value) {
-#pragma unroll
-            for (int p = 0; p < NVEC; p++)
-                s[p] = add_rn(s[p], pm1_apply(cc, gather<COH>(xs.v[p] + pm1_col(cc))));
+    for (int j = 0; j < NV4; j++) {
+        const int e = base + 4 * (lane + 32 * j);
+        if (e < b) {
+            load4(A.idx + e, cc[j]);
+            if constexpr (!is_pm1<V>::value) load4v<T>(A.val + e, vv[j]);
+            else vv[j][0] = vv[j][1] = vv[j][2] = vv[j][3] = T(0);
         } else {
-            const T vv = load1v<V, T>(A.val + e);
 #pragma unroll
-            for (int p = 0; p < NVEC; p++) s[p] = add_rn(s[p], mul_rn(vv, gather<COH>(xs.v[p] + cc)));
+            for (int q = 0; q < 4; q++) { cc[j][q] = 0; vv[j][q] = T(0); }
         }
+    }
+    T s[NVEC];
+#pragma unroll 1
+    for (int p = 0; p < NVEC; p++) {
+        const T* xv = pick(xs.v, p);
+        T xg[NV4][4];
+#pragma unroll
+        for (int j = 0; j < NV4; j++) {
+            const int e = base + 4 * (lane + 32 * j);
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                xg[j][q] = (e + q >= a && e + q < b)
+                               ? gather<COH>(xv + (is_pm1<V>::value ? pm1_col(cc[j][q]) : cc[j][q]))
+                               : T(0);
+        }
+        T acc_p = T(0);
+#pragma unroll
+        for (int j = 0; j < NV4; j++) {
+            const int e = base + 4 * (lane + 32 * j);
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                if (e + q >= a && e + q < b)
+                    acc_p = add_rn(acc_p, is_pm1<V>::value ? pm1_apply(cc[j][q], xg[j][q])
+                                                           : mul_rn(vv[j][q], xg[j][q]));
+        }
+#pragma unroll
+        for (int q = 0; q < NVEC; q++)
+            if (q == p) s[q] = acc_p;
     }
 #pragma unroll
     for (int p = 0; p < NVEC; p++) s[p] = warp_sum_tree(s[p]);
@@ -298,8 +357,14 @@ __device__ __forceinline__ void long_piece(const CsrView<V, T>& A, const VecSet<
 
 // One launch covers both kinds of work: the first warps take the long-row
 // pieces (so they start early), the rest the short tiles.
+// FP64 iterates: at least CPDLP_F64_MIN_BLOCKS resident blocks per SM (a
+// register cap; unbounded, the FP64 step kernels took up to 159 registers and
+// one 8-warp block per SM)
+#ifndef CPDLP_F64_MIN_BLOCKS
+#define CPDLP_F64_MIN_BLOCKS 2
+#endif
 template <int ITEMS, int WARPS, int NVEC, class V, class T, class Epi>
-__global__ void __launch_bounds__(WARPS * 32)
+__global__ void __launch_bounds__(WARPS * 32, sizeof(T) == 8 ? CPDLP_F64_MIN_BLOCKS : 1)
     k_tiles(CsrView<V, T> A, VecSet<T, NVEC> xs, Epi epi) {
     __shared__ T prod[WARPS][32 * ITEMS];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -315,20 +380,237 @@ __global__ void __launch_bounds__(WARPS * 32)
     epi.finish(acc);
 }
 
-constexpr int TILE_WARPS = 8;
-
-// Launches the tile kernel on `s`.  Reducing epilogues write one row of
-// block partials per block.
+// Launches the tile kernel on `s` with WARPS warps per block.  Reducing
+// epilogues write one row of block partials per block.
+template <int WARPS, int NVEC, class V, class T, class Epi>
+void launch_tiles_w(const TilePlan& plan, const CsrView<V, T>& view, const VecSet<T, NVEC>& xs,
+                    const Epi& epi, cudaStream_t s) {
+    const int64_t tasks = (int64_t)plan.ntasks + plan.nltasks;
+    if (tasks == 0) return;
+    const unsigned grid = (unsigned)((tasks + WARPS - 1) / WARPS);
+    switch (plan.items) {
+        case 4: k_tiles<4, WARPS, NVEC, V, T, Epi><<<grid, WARPS * 32, 0, s>>>(view, xs, epi); break;
+        case 8: k_tiles<8, WARPS, NVEC, V, T, Epi><<<grid, WARPS * 32, 0, s>>>(view, xs, epi); break;
+        default: k_tiles<16, WARPS, NVEC, V, T, Epi><<<grid, WARPS * 32, 0, s>>>(view, xs, epi); break;
+    }
+    CK_LAUNCH();
+}
 template <int NVEC, class V, class T, class Epi>
 void launch_tiles(const TilePlan& plan, const CsrView<V, T>& view, const VecSet<T, NVEC>& xs,
                   const Epi& epi, cudaStream_t s) {
+    launch_tiles_w<TILE_WARPS>(plan, view, xs, epi, s);
+}
+
+// ---- four iterates per pass (the KKT evaluation) ------------------------------
+// x4 holds the four gathered vectors interleaved (x4[4*col + p]), so one
+// request per nonzero fetches all four.  The gathers are asynchronous copies
+// (cp.async) straight into the warp's shared buffer g[k][0..3] (k = the
+// nonzero's place in the tile): they hold no registers, so all of a lane's
+// gathers are in flight at once.  Each lane then multiplies its own nonzeros'
+// four values in place, and every lane reduces its rows for the four iterates
+// side by side, each in ascending column order: iterate p's row sums are the
+// ones a one-iterate pass over x_p computes.
+template <int ITEMS, class V, class T, class Epi, int RPL = ROWS_PER_LANE>
+__device__ __forceinline__ void short_tile4(const CsrView<V, T>& A, const T* __restrict__ x4,
+                                            Epi& epi, typename Epi::Acc& acc, int r0, int r1,
+                                            int nz0, int nz1, int lane, T* g) {
+    constexpr int NV4 = ITEMS / 4 + 1;
+    const int base = nz0 & ~3;
+    int ra[RPL], rb[RPL];
+#pragma unroll
+    for (int k = 0; k < RPL; k++) {
+        const int r = r0 + lane + 32 * k;
+        if (r < r1) {
+            ra[k] = ld_keep(A.ptr + r);
+            rb[k] = ld_keep(A.ptr + r + 1);
+        } else {
+            ra[k] = rb[k] = 0;
+        }
+    }
+    int cc[NV4][4];
+    T vv[NV4][4];
+#pragma unroll
+    for (int j = 0; j < NV4; j++) {
+        const int e = base + 4 * (lane + 32 * j);
+        if (e < nz1) {
+            load4(A.idx + e, cc[j]);
+            if constexpr (!is_pm1<V>::value) load4v<T>(A.val + e, vv[j]);
+            else vv[j][0] = vv[j][1] = vv[j][2] = vv[j][3] = T(0);
+        } else {
+#pragma unroll
+            for (int q = 0; q < 4; q++) { cc[j][q] = 0; vv[j][q] = T(0); }
+        }
+    }
+    // the gathers: 4 values of T per nonzero, 16 bytes per copy
+#pragma unroll
+    for (int j = 0; j < NV4; j++) {
+        const int e = base + 4 * (lane + 32 * j);
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            if (e + q >= nz0 && e + q < nz1) {
+                const int col = is_pm1<V>::value ? pm1_col(cc[j][q]) : cc[j][q];
+                const T* src = x4 + 4 * (size_t)col;
+                T* dst = g + 4 * (e + q - nz0);
+#pragma unroll
+                for (int h = 0; h < (int)(4 * sizeof(T)) / 16; h++)
+                    cp_async16(dst + h * (16 / sizeof(T)), src + h * (16 / sizeof(T)));
+            }
+    }
+    cp_async_wait_all();
+    // products in place (each lane its own nonzeros)
+#pragma unroll
+    for (int j = 0; j < NV4; j++) {
+        const int e = base + 4 * (lane + 32 * j);
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            if (e + q >= nz0 && e + q < nz1) {
+                T* gk = g + 4 * (e + q - nz0);
+#pragma unroll
+                for (int p = 0; p < 4; p++)
+                    gk[p] = is_pm1<V>::value ? pm1_apply(cc[j][q], gk[p]) : mul_rn(vv[j][q], gk[p]);
+            }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < RPL; k++) {
+        const int r = r0 + lane + 32 * k;
+        if (r < r1) {
+            T s0 = T(0), s1 = T(0), s2 = T(0), s3 = T(0);
+            for (int i = ra[k] - nz0; i < rb[k] - nz0; i++) {
+                const T* gi = g + 4 * i;
+                s0 = add_rn(s0, gi[0]);
+                s1 = add_rn(s1, gi[1]);
+                s2 = add_rn(s2, gi[2]);
+                s3 = add_rn(s3, gi[3]);
+            }
+            const typename Epi::Pre pre{};
+            epi.row(0, r, s0, pre, acc);
+            epi.row(1, r, s1, pre, acc);
+            epi.row(2, r, s2, pre, acc);
+            epi.row(3, r, s3, pre, acc);
+        }
+    }
+    __syncwarp();
+}
+
+// one TILE-sized piece of a long row, four packed iterates (see long_piece):
+// the gathers are asynchronous copies into the warp's buffer g, and each lane
+// sums its own elements' products for the four iterates
+template <int ITEMS, class V, class T, class Epi>
+__device__ __forceinline__ void long_piece4(const CsrView<V, T>& A, const T* __restrict__ x4,
+                                            Epi& epi, typename Epi::Acc& acc, int4 t, int lane,
+                                            T* g) {
+    constexpr int TILE = 32 * ITEMS;
+    constexpr int NV4 = ITEMS / 4 + 1;
+    const int row = t.x, piece = -t.y - 1, lid = t.z, base_slot = t.w;
+    const int rb = ld_keep(A.ptr + row), re = ld_keep(A.ptr + row + 1);
+    const int npieces = (re - rb + TILE - 1) / TILE;
+    const int a = rb + piece * TILE;
+    const int b = min(a + TILE, re);
+    const int base = a & ~3;
+    int cc[NV4][4];
+    T vv[NV4][4];
+#pragma unroll
+    for (int j = 0; j < NV4; j++) {
+        const int e = base + 4 * (lane + 32 * j);
+        if (e < b) {
+            load4(A.idx + e, cc[j]);
+            if constexpr (!is_pm1<V>::value) load4v<T>(A.val + e, vv[j]);
+            else vv[j][0] = vv[j][1] = vv[j][2] = vv[j][3] = T(0);
+        } else {
+#pragma unroll
+            for (int q = 0; q < 4; q++) { cc[j][q] = 0; vv[j][q] = T(0); }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < NV4; j++) {
+        const int e = base + 4 * (lane + 32 * j);
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            if (e + q >= a && e + q < b) {
+                const int col = is_pm1<V>::value ? pm1_col(cc[j][q]) : cc[j][q];
+                const T* src = x4 + 4 * (size_t)col;
+                T* dst = g + 4 * (e + q - a);
+#pragma unroll
+                for (int h = 0; h < (int)(4 * sizeof(T)) / 16; h++)
+                    cp_async16(dst + h * (16 / sizeof(T)), src + h * (16 / sizeof(T)));
+            }
+    }
+    cp_async_wait_all();
+    T s[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll
+    for (int j = 0; j < NV4; j++) {
+        const int e = base + 4 * (lane + 32 * j);
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            if (e + q >= a && e + q < b) {
+                const T* gk = g + 4 * (e + q - a);
+#pragma unroll
+                for (int p = 0; p < 4; p++)
+                    s[p] = add_rn(s[p], is_pm1<V>::value ? pm1_apply(cc[j][q], gk[p])
+                                                         : mul_rn(vv[j][q], gk[p]));
+            }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int p = 0; p < 4; p++) s[p] = warp_sum_tree(s[p]);
+    if (npieces == 1) {
+        if (lane == 0) {
+#pragma unroll
+            for (int p = 0; p < 4; p++) epi.row_long(p, row, s[p], lid, acc);
+        }
+        return;
+    }
+    int done = 0;
+    if (lane == 0) {
+#pragma unroll
+        for (int p = 0; p < 4; p++) A.partials[(size_t)(base_slot + piece) * 4 + p] = s[p];
+        __threadfence();
+        done = atomicAdd(&A.counters[lid], 1);
+    }
+    done = __shfl_sync(FULL_MASK, done, 0);
+    if (done == npieces - 1) {
+        __threadfence();
+        if (lane == 0) {
+#pragma unroll
+            for (int p = 0; p < 4; p++) {
+                T tot = T(0);
+                for (int q = 0; q < npieces; q++)
+                    tot = add_rn(tot, __ldcg(A.partials + (size_t)(base_slot + q) * 4 + p));
+                epi.row_long(p, row, tot, lid, acc);
+            }
+            A.counters[lid] = 0;
+        }
+    }
+}
+
+template <int ITEMS, int WARPS, class V, class T, class Epi>
+__global__ void __launch_bounds__(WARPS * 32)
+    k_tiles4(CsrView<V, T> A, const T* __restrict__ x4, Epi epi) {
+    __shared__ __align__(16) T prod[WARPS][4 * 32 * ITEMS];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int task = blockIdx.x * WARPS + w;
+    typename Epi::Acc acc;
+    epi.init(acc);
+    if (task < A.nltasks) {
+        long_piece4<ITEMS>(A, x4, epi, acc, A.ltasks[task], lane, prod[w]);
+    } else if (task - A.nltasks < A.ntasks) {
+        const int4 t = A.tasks[task - A.nltasks];
+        short_tile4<ITEMS>(A, x4, epi, acc, t.x, t.y, t.z, t.w, lane, prod[w]);
+    }
+    epi.finish(acc);
+}
+
+template <int WARPS, class V, class T, class Epi>
+void launch_tiles4(const TilePlan& plan, const CsrView<V, T>& view, const T* x4, const Epi& epi,
+                   cudaStream_t s) {
     const int64_t tasks = (int64_t)plan.ntasks + plan.nltasks;
     if (tasks == 0) return;
-    const unsigned grid = (unsigned)((tasks + TILE_WARPS - 1) / TILE_WARPS);
+    const unsigned grid = (unsigned)((tasks + WARPS - 1) / WARPS);
     switch (plan.items) {
-        case 4: k_tiles<4, TILE_WARPS, NVEC, V, T, Epi><<<grid, TILE_WARPS * 32, 0, s>>>(view, xs, epi); break;
-        case 8: k_tiles<8, TILE_WARPS, NVEC, V, T, Epi><<<grid, TILE_WARPS * 32, 0, s>>>(view, xs, epi); break;
-        default: k_tiles<16, TILE_WARPS, NVEC, V, T, Epi><<<grid, TILE_WARPS * 32, 0, s>>>(view, xs, epi); break;
+        case 4: k_tiles4<4, WARPS, V, T, Epi><<<grid, WARPS * 32, 0, s>>>(view, x4, epi); break;
+        case 8: k_tiles4<8, WARPS, V, T, Epi><<<grid, WARPS * 32, 0, s>>>(view, x4, epi); break;
+        default: k_tiles4<16, WARPS, V, T, Epi><<<grid, WARPS * 32, 0, s>>>(view, x4, epi); break;
     }
     CK_LAUNCH();
 }
@@ -336,17 +618,17 @@ void launch_tiles(const TilePlan& plan, const CsrView<V, T>& view, const VecSet<
 // number of kernels launch_tiles issues for this plan
 inline int tiles_launches(const TilePlan& plan) { return (plan.ntasks + plan.nltasks) ? 1 : 0; }
 
-// block-partial rows written by a reducing epilogue
-inline unsigned tiles_grid(const TilePlan& plan) {
-    return (unsigned)(((int64_t)plan.ntasks + plan.nltasks + TILE_WARPS - 1) / TILE_WARPS);
+// block-partial rows written by a reducing epilogue (WARPS warps per block)
+inline unsigned tiles_grid(const TilePlan& plan, int warps = TILE_WARPS) {
+    return (unsigned)(((int64_t)plan.ntasks + plan.nltasks + warps - 1) / warps);
 }
 
 // ---- block reduction of per-thread FP64 accumulators -------------------------
 // Every thread of a TILE_WARPS*32 block calls it; thread 0..Q-1 of the block
 // write the block's sums to out[blockIdx.x * Q + q].
-template <int Q>
+template <int Q, int W = TILE_WARPS>
 __device__ __forceinline__ void block_reduce_store(const double (&v)[Q], double* out) {
-    __shared__ double red[TILE_WARPS][Q];
+    __shared__ double red[W][Q];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
     for (int q = 0; q < Q; q++) {
@@ -359,7 +641,7 @@ __device__ __forceinline__ void block_reduce_store(const double (&v)[Q], double*
     if (threadIdx.x < Q) {
         double s = 0.0;
 #pragma unroll
-        for (int ww = 0; ww < TILE_WARPS; ww++) s += red[ww][threadIdx.x];
+        for (int ww = 0; ww < W; ww++) s += red[ww][threadIdx.x];
         out[(size_t)blockIdx.x * Q + threadIdx.x] = s;
     }
 }
