@@ -913,6 +913,16 @@ ORC_EXPORT int32_t orc_solve(const cpdlp_lp* lp, const cpdlp_params* prm, const 
     return status;
 }
 
+/* Thread count of the OpenMP row loops (the CPU baselines time 1 thread, as
+ * the reference's single-threaded CPU path, and all host threads). */
+ORC_EXPORT void orc_set_num_threads(int32_t n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
 ORC_EXPORT int32_t orc_num_threads(void) {
 #ifdef _OPENMP
     return (int32_t)omp_get_max_threads();

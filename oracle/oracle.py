@@ -81,6 +81,7 @@ def lib():
             "orc_solve": (c_int32, [POINTER(A.LPC), POINTER(A.ParamsC), PD, PD, PD, PD,
                                     POINTER(A.StatsC), POINTER(c_void_p)]),
             "orc_num_threads": (c_int32, []),
+            "orc_set_num_threads": (None, [c_int32]),
             "orc_lp_preconditioner": (None, [POINTER(A.LPC), c_int32, c_double, c_int32, PD, PD]),
         }
         for name, (res, args) in sig.items():

@@ -7,12 +7,13 @@
   test/moi.jl:38-53 for the two-variable LP, optimal objective 205);
 * optimal objectives from an independent solver (HiGHS through scipy's
   linprog) for seeded LPs of the single-LP, batched and multicommodity-flow
-  workloads: these pin the oracle and the device path to an answer that does
-  not come from this repository's code;
+  workloads, the requests of the serving test's stream and a scaled-down
+  power-law LP of the large single-LP workload: these pin the oracle and the
+  device path to an answer that does not come from this repository's code;
 * outputs of the CPU oracle (oracle/) on small seeded inputs: the CSR / ELL /
   COO fields of matrix conversions, the Ruiz + Pock-Chambolle diagonals, KKT
-  errors at fixed points and whole solve trajectories (KKT passes, status,
-  objective).  The oracle is a restatement of the reference's algorithm, not
+  errors at fixed points, whole solve trajectories (KKT passes, status,
+  objective) and the scaled-down power-law LP solved to 1e-4 and 1e-8.  The oracle is a restatement of the reference's algorithm, not
   the reference itself (Julia is not available), so these fixtures pin
   regressions of the oracle and give the device tests bit-exact targets; they
   are not an independent check.
@@ -63,6 +64,25 @@ def lp_sets():
     return {"single": single, "batch": batch, "flow": flows}
 
 
+def served_requests():
+    """The small served stream of tests/test_gpu_serving.py (36 requests,
+    seed 11: random sparse LPs m in [60, 1500], grid flows side 6..14, K 2..4,
+    tolerance 1e-4 or 1e-8)."""
+    from coolpdlp import generators as G
+    reqs = G.served_stream(36, 400.0, seed=11, m_lo=60, m_hi=1500, side_lo=6, side_hi=14,
+                           k_lo=2, k_hi=4)
+    return reqs, [G.request_lp(r) for r in reqs]
+
+
+def powerlaw_small():
+    """The large single LP's generator scaled down to m = 5,000, n = 10,000,
+    60,000 nonzeros (power-law rows with tail 1.5 and the cap at 20,000, so
+    76 rows exceed 64 nonzeros and 4 exceed 512; row factors log-U[1e-3,
+    1e3]; seed 1)."""
+    from coolpdlp import generators as G
+    return G.powerlaw_lp(5000, 10000, 60000, seed=1, cap=20000)
+
+
 def main():
     import oracle as O
     from coolpdlp import generators as G
@@ -82,6 +102,23 @@ def main():
     meta["highs"] = {}
     for kind, lps in sets.items():
         meta["highs"][kind] = [{"name": lp.name, "objective": highs_objective(lp)} for lp in lps]
+
+    # ---- HiGHS objectives of the served requests of the serving test
+    reqs, rlps = served_requests()
+    meta["served"] = [{"rid": r.rid, "name": lp.name, "reltol": r.reltol,
+                       "objective": highs_objective(lp)} for r, lp in zip(reqs, rlps)]
+
+    # ---- the scaled-down large single LP: HiGHS, and the oracle (FP64 PDLP)
+    # to 1e-4 and to 1e-8 relative KKT
+    lpp = powerlaw_small()
+    meta["powerlaw"] = {"name": lpp.name, "m": lpp.m, "n": lpp.n, "nnz": lpp.nnz,
+                        "highs_objective": highs_objective(lpp)}
+    for tol in (1e-4, 1e-8):
+        x, y, st = O.solve(lpp, O.params(termination_reltol=tol, max_kkt_passes=2_000_000,
+                                         time_limit=3600.0))
+        meta["powerlaw"][f"oracle_{tol:.0e}"] = {
+            "termination_status": st["termination_status"], "kkt_passes": st["kkt_passes"],
+            "objective": float(np.dot(lpp.c, x)), "err": st["err"]}
 
     # ---- oracle: conversions of a small matrix with an empty row and column
     lp = G.random_sparse_lp(40, 60, 3, seed=5)

@@ -1,7 +1,13 @@
 """The continuous-batching server (coolpdlp.serving): requests that arrive
 while others run are admitted as slots and HBM budget free up, their work
 overlaps on the GPU, and every result equals the result of the same request
-solved alone (bit-identical: an LP's arithmetic does not depend on the mix)."""
+solved alone (bit-identical: an LP's arithmetic does not depend on the mix).
+Every served result is also checked against HiGHS's optimal objective for its
+LP (committed fixture, tests/golden/): within 1e-6 relative for requests at
+1e-8 relative KKT, within 1e-2 for requests at 1e-4."""
+import json
+import os
+
 import numpy as np
 import pytest
 
@@ -34,9 +40,17 @@ def test_served_stream_equals_alone(float_type):
     assert out["p99_ms"] >= out["p50_ms"] > 0
     overlapped = 0
     h = native.Handle(0)
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                           "golden.json")) as f:
+        highs = {d["rid"]: d for d in json.load(f)["served"]}
     for r in reqs:
         res = server.results[r.rid]
         assert _rel(res.stats) <= r.reltol, (r.rid, _rel(res.stats), r.reltol)
+        want = highs[r.rid]
+        assert want["name"] == lps[r.rid].name and want["reltol"] == r.reltol
+        obj, ref = float(lps[r.rid].c @ res.x), want["objective"]
+        tol = 1e-6 if r.reltol < 1e-6 else 1e-2
+        assert abs(obj - ref) <= tol * max(1.0, abs(ref)), (r.rid, r.reltol, obj, ref)
         lp = lps[r.rid]
         S = native.LPStruct(lp.m, lp.n, lp.colptr, lp.rowval, lp.nzval, lp.c, lp.lv, lp.uv,
                             lp.lc, lp.uc)
