@@ -253,7 +253,7 @@ __device__ __forceinline__ void lp_tiles(const CsrView<V, T>& A, int t0, int t1,
     for (int t = l0 + gw; t < l1; t += BW * CS) long_piece<ITEMS, 1>(A, xs, epi, acc, A.ltasks[t], lane);
     for (int t = t0 + gw; t < t1; t += BW * CS) {
         const int4 tk = A.tasks[t];
-        short_tile<ITEMS, 1, V, T, Epi, true, BATCH_RPL>(A, xs, epi, acc, tk.x, tk.y, tk.z, tk.w,
+        short_tile<ITEMS, 1, V, T, Epi, true, BATCH_RPL, true>(A, xs, epi, acc, tk.x, tk.y, tk.z, tk.w,
                                                        lane, prod + w * 32 * ITEMS);
     }
 }

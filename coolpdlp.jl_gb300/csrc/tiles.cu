@@ -28,6 +28,16 @@ void build_tile_plan(const std::vector<int32_t>& ptr, int32_t rows, int items, T
     plan.rows = rows;
     plan.items = items;
     const int tile = 32 * items;
+    // rows of LONG_ROW+1 .. tile nonzeros stay in short tiles (summed by the
+    // whole warp); with the default row cap their tiles hold at most 64 rows
+    bool medium = false;
+    for (int32_t r = 0; r < rows && !medium; r++) {
+        const int32_t len = ptr[r + 1] - ptr[r];
+        medium = len > LONG_ROW && len <= tile;
+    }
+    if (medium && max_rows == MAX_TILE_ROWS) max_rows = 64;
+    plan.medium = medium;
+    plan.rpl = max_rows / 32;
     std::vector<int4> longs, shorts;
     plan.long_rows.clear();
     int32_t slot = 0;
@@ -45,7 +55,7 @@ void build_tile_plan(const std::vector<int32_t>& ptr, int32_t rows, int items, T
         int32_t r = (int32_t)segs[k];
         while (r < end) {
             int32_t len = ptr[r + 1] - ptr[r];
-            if (len > LONG_ROW) {
+            if (len > tile) {
                 // warp path: one piece per TILE nonzeros; only multi-piece rows use slots
                 int32_t lid = (int32_t)plan.long_rows.size();
                 int32_t np = (len + tile - 1) / tile;
@@ -58,7 +68,7 @@ void build_tile_plan(const std::vector<int32_t>& ptr, int32_t rows, int items, T
             int32_t r0 = r, nz = 0;
             while (r < end && r - r0 < max_rows) {
                 int32_t l = ptr[r + 1] - ptr[r];
-                if (l > LONG_ROW || nz + l > tile) break;
+                if (l > tile || nz + l > tile) break;
                 nz += l;
                 r++;
             }

@@ -2,17 +2,18 @@
 //
 // Work partition (built once per matrix on the host from its row pointer):
 //  * short tile {r0, r1, nz0, nz1}: consecutive rows [r0, r1), each at most
-//    LONG_ROW nonzeros, together at most TILE = 32*ITEMS nonzeros and at most
+//    TILE = 32*ITEMS nonzeros, together at most TILE nonzeros and at most
 //    MAX_TILE_ROWS rows.  One warp
 //      1. prefetches the row pointers and the epilogue inputs of its rows,
 //      2. loads the tile's values and column indices with 128-bit loads
 //         (window aligned down to 4 elements), all issued before any use,
 //      3. gathers x[col] for the whole tile in one batch,
 //      4. writes value*x products to shared memory, and
-//      5. lets every lane reduce whole rows in ascending column order (the
-//         reference's order) and apply the fused epilogue.
+//      5. lets every lane reduce its rows of at most LONG_ROW nonzeros in
+//         ascending column order (the reference's order), while longer rows
+//         are reduced by the whole warp; the fused epilogue follows.
 //  * long-row piece {row, -(piece+1), long_id, slot_base}: a row longer than
-//    LONG_ROW is cut into TILE-sized pieces, one warp each, reduced with warp
+//    TILE is cut into TILE-sized pieces, one warp each, reduced with warp
 //    shuffles.  A row of several pieces writes each partial to a scratch slot;
 //    the warp that completes the row (atomic counter, no waiting) adds the
 //    partials in piece order and applies the epilogue, so results do not
@@ -43,6 +44,8 @@ struct TilePlan {
     int32_t nlong = 0;      // rows that take the warp path
     int32_t npieces = 0;    // pieces of all long rows
     int32_t nltasks = 0;    // long-row pieces (tasks of the long-row kernel)
+    int32_t rpl = ROWS_PER_LANE;  // rows per lane of a short tile (row cap / 32)
+    bool medium = false;    // some short tile holds a row longer than LONG_ROW
     DBuf<int4> tasks;       // short tiles
     DBuf<int4> ltasks;      // long-row pieces
     DBuf<int32_t> counters; // per long row, zero between launches
@@ -55,7 +58,10 @@ struct TilePlan {
 // start, and seg_tasks / seg_ltasks / seg_lids receive, per segment, the first
 // short task, long task and long-row id (one extra final entry = totals).
 // max_rows caps the rows of a short tile (a multiple of 32, at most
-// MAX_TILE_ROWS): kernels built for max_rows / 32 rows per lane.
+// MAX_TILE_ROWS): kernels built for max_rows / 32 rows per lane.  With the
+// default cap, a matrix with rows of LONG_ROW+1 .. TILE nonzeros (which short
+// tiles sum with the whole warp) gets tiles of at most 64 rows: the kernels
+// that handle such rows keep two rows per lane in registers instead of four.
 void build_tile_plan(const std::vector<int32_t>& ptr, int32_t rows, int items, TilePlan& plan,
                      cudaStream_t s, const std::vector<int64_t>* seg_rows = nullptr,
                      std::vector<int32_t>* seg_tasks = nullptr,
@@ -192,7 +198,8 @@ constexpr int kkt_warps() { return sizeof(T) == 4 ? 4 : 2; }
 // and epilogue inputs of this lane's rows, (2) one batch of gathers.  Then
 // products go to shared memory and every lane reduces whole rows in column
 // order before the fused epilogue.  RPL: rows per lane, the plan's row cap / 32.
-template <int ITEMS, int NVEC, class V, class T, class Epi, bool COH, int RPL = ROWS_PER_LANE>
+template <int ITEMS, int NVEC, class V, class T, class Epi, bool COH, int RPL = ROWS_PER_LANE,
+          bool MED = false>
 __device__ __forceinline__ void short_tile(const CsrView<V, T>& A, const VecSet<T, NVEC, COH>& xs,
                                            Epi& epi, typename Epi::Acc& acc, int r0, int r1,
                                            int nz0, int nz1, int lane, T* prod) {
@@ -225,8 +232,8 @@ __device__ __forceinline__ void short_tile(const CsrView<V, T>& A, const VecSet<
             for (int q = 0; q < 4; q++) { cc[j][q] = 0; vv[j][q] = T(0); }
         }
     }
-    // one input vector at a time (not unrolled): with several vectors (the KKT
-    // pass) this keeps one batch of gathers in registers instead of all of them
+    // one input vector at a time (not unrolled): with several vectors this
+    // keeps one batch of gathers in registers instead of all of them
 #pragma unroll 1
     for (int p = 0; p < NVEC; p++) {
         const T* xv = pick(xs.v, p);
@@ -253,9 +260,26 @@ __device__ __forceinline__ void short_tile(const CsrView<V, T>& A, const VecSet<
 #pragma unroll
         for (int k = 0; k < RPL; k++) {
             const int r = r0 + lane + 32 * k;
+            const int len = rb[k] - ra[k];
+            T sum = T(0);
+            if constexpr (MED) {
+                // rows longer than LONG_ROW: the whole warp, lane-strided
+                // partial sums and a fixed shuffle tree (a long-row piece's order)
+                unsigned med = __ballot_sync(FULL_MASK, r < r1 && len > LONG_ROW);
+                while (med) {
+                    const int l = __ffs(med) - 1;
+                    med &= med - 1;
+                    const int a = __shfl_sync(FULL_MASK, ra[k], l) - nz0;
+                    const int b = __shfl_sync(FULL_MASK, rb[k], l) - nz0;
+                    T part = T(0);
+                    for (int i = a + lane; i < b; i += 32) part = add_rn(part, prod[i]);
+                    part = warp_sum_tree(part);
+                    if (lane == l) sum = part;
+                }
+            }
             if (r < r1) {
-                T sum = T(0);
-                for (int i = ra[k] - nz0; i < rb[k] - nz0; i++) sum = add_rn(sum, prod[i]);
+                if (len <= LONG_ROW)
+                    for (int i = ra[k] - nz0; i < rb[k] - nz0; i++) sum = add_rn(sum, prod[i]);
                 epi.row(p, r, sum, pre[k], acc);
             }
         }
@@ -263,65 +287,34 @@ __device__ __forceinline__ void short_tile(const CsrView<V, T>& A, const VecSet<
     }
 }
 
-// One warp, one TILE-sized piece of a row longer than LONG_ROW.  The piece's
-// indices and values are loaded with 128-bit loads over the 4-element-aligned
-// window and its gathers are issued in one batch, as in a short tile; each
-// lane sums its own elements in ascending order, then a fixed shuffle tree
-// adds the lanes.  Multi-piece rows combine through scratch slots: the warp
-// that completes the row (atomic counter, no waiting) adds the partials in
-// piece order and applies the epilogue.
+// One warp, one TILE-sized piece of a row longer than TILE: lane-strided
+// coalesced loads, lane partial sums, a fixed shuffle tree.  Multi-piece rows
+// combine through scratch slots: the warp that completes the row (atomic
+// counter, no waiting) adds the partials in piece order and applies the
+// epilogue.
 template <int ITEMS, int NVEC, class V, class T, class Epi, bool COH>
 __device__ __forceinline__ void long_piece(const CsrView<V, T>& A, const VecSet<T, NVEC, COH>& xs,
                                            Epi& epi, typename Epi::Acc& acc, int4 t, int lane) {
     constexpr int TILE = 32 * ITEMS;
-    constexpr int NV4 = ITEMS / 4 + 1;
     const int row = t.x, piece = -t.y - 1, lid = t.z, base_slot = t.w;
     const int rb = ld_keep(A.ptr + row), re = ld_keep(A.ptr + row + 1);
     const int npieces = (re - rb + TILE - 1) / TILE;
     const int a = rb + piece * TILE;
     const int b = min(a + TILE, re);
-    const int base = a & ~3;
-    int cc[NV4][4];
-    T vv[NV4][4];
-#pragma unroll
-    for (int j = 0; j < NV4; j++) {
-        const int e = base + 4 * (lane + 32 * j);
-        if (e < b) {
-            load4(A.idx + e, cc[j]);
-            if constexpr (!is_pm1<V>::value) load4v<T>(A.val + e, vv[j]);
-            else vv[j][0] = vv[j][1] = vv[j][2] = vv[j][3] = T(0);
-        } else {
-#pragma unroll
-            for (int q = 0; q < 4; q++) { cc[j][q] = 0; vv[j][q] = T(0); }
-        }
-    }
     T s[NVEC];
-#pragma unroll 1
-    for (int p = 0; p < NVEC; p++) {
-        const T* xv = pick(xs.v, p);
-        T xg[NV4][4];
 #pragma unroll
-        for (int j = 0; j < NV4; j++) {
-            const int e = base + 4 * (lane + 32 * j);
+    for (int p = 0; p < NVEC; p++) s[p] = T(0);
+    for (int e = a + lane; e < b; e += 32) {
+        const int cc = __ldcs(A.idx + e);
+        if constexpr (is_pm1<V>::value) {
 #pragma unroll
-            for (int q = 0; q < 4; q++)
-                xg[j][q] = (e + q >= a && e + q < b)
-                               ? gather<COH>(xv + (is_pm1<V>::value ? pm1_col(cc[j][q]) : cc[j][q]))
-                               : T(0);
+            for (int p = 0; p < NVEC; p++)
+                s[p] = add_rn(s[p], pm1_apply(cc, gather<COH>(xs.v[p] + pm1_col(cc))));
+        } else {
+            const T vv = load1v<V, T>(A.val + e);
+#pragma unroll
+            for (int p = 0; p < NVEC; p++) s[p] = add_rn(s[p], mul_rn(vv, gather<COH>(xs.v[p] + cc)));
         }
-        T acc_p = T(0);
-#pragma unroll
-        for (int j = 0; j < NV4; j++) {
-            const int e = base + 4 * (lane + 32 * j);
-#pragma unroll
-            for (int q = 0; q < 4; q++)
-                if (e + q >= a && e + q < b)
-                    acc_p = add_rn(acc_p, is_pm1<V>::value ? pm1_apply(cc[j][q], xg[j][q])
-                                                           : mul_rn(vv[j][q], xg[j][q]));
-        }
-#pragma unroll
-        for (int q = 0; q < NVEC; q++)
-            if (q == p) s[q] = acc_p;
     }
 #pragma unroll
     for (int p = 0; p < NVEC; p++) s[p] = warp_sum_tree(s[p]);
@@ -359,11 +352,12 @@ __device__ __forceinline__ void long_piece(const CsrView<V, T>& A, const VecSet<
 // pieces (so they start early), the rest the short tiles.
 // FP64 iterates: at least CPDLP_F64_MIN_BLOCKS resident blocks per SM (a
 // register cap; unbounded, the FP64 step kernels took up to 159 registers and
-// one 8-warp block per SM)
+// one 8-warp block per SM).  FP32 kernels are left to the compiler (56-64
+// registers; a cap of 64 made it spill).
 #ifndef CPDLP_F64_MIN_BLOCKS
 #define CPDLP_F64_MIN_BLOCKS 2
 #endif
-template <int ITEMS, int WARPS, int NVEC, class V, class T, class Epi>
+template <int ITEMS, int WARPS, int NVEC, class V, class T, class Epi, int RPL, bool MED>
 __global__ void __launch_bounds__(WARPS * 32, sizeof(T) == 8 ? CPDLP_F64_MIN_BLOCKS : 1)
     k_tiles(CsrView<V, T> A, VecSet<T, NVEC> xs, Epi epi) {
     __shared__ T prod[WARPS][32 * ITEMS];
@@ -375,7 +369,8 @@ __global__ void __launch_bounds__(WARPS * 32, sizeof(T) == 8 ? CPDLP_F64_MIN_BLO
         long_piece<ITEMS, NVEC>(A, xs, epi, acc, A.ltasks[task], lane);
     } else if (task - A.nltasks < A.ntasks) {
         const int4 t = A.tasks[task - A.nltasks];
-        short_tile<ITEMS, NVEC>(A, xs, epi, acc, t.x, t.y, t.z, t.w, lane, prod[w]);
+        short_tile<ITEMS, NVEC, V, T, Epi, false, RPL, MED>(A, xs, epi, acc, t.x, t.y, t.z, t.w,
+                                                            lane, prod[w]);
     }
     epi.finish(acc);
 }
@@ -388,11 +383,24 @@ void launch_tiles_w(const TilePlan& plan, const CsrView<V, T>& view, const VecSe
     const int64_t tasks = (int64_t)plan.ntasks + plan.nltasks;
     if (tasks == 0) return;
     const unsigned grid = (unsigned)((tasks + WARPS - 1) / WARPS);
-    switch (plan.items) {
-        case 4: k_tiles<4, WARPS, NVEC, V, T, Epi><<<grid, WARPS * 32, 0, s>>>(view, xs, epi); break;
-        case 8: k_tiles<8, WARPS, NVEC, V, T, Epi><<<grid, WARPS * 32, 0, s>>>(view, xs, epi); break;
-        default: k_tiles<16, WARPS, NVEC, V, T, Epi><<<grid, WARPS * 32, 0, s>>>(view, xs, epi); break;
+#define CPDLP_TILES(IT, R, M) k_tiles<IT, WARPS, NVEC, V, T, Epi, R, M><<<grid, WARPS * 32, 0, s>>>(view, xs, epi)
+    if (plan.medium) {
+        if (plan.rpl != 2) fail(CPDLP_ERR_ARGUMENT, "tile plan with long rows needs 64-row tiles");
+        switch (plan.items) {
+            case 4: CPDLP_TILES(4, 2, true); break;
+            case 8: CPDLP_TILES(8, 2, true); break;
+            default: CPDLP_TILES(16, 2, true); break;
+        }
+    } else {
+        if (plan.rpl != ROWS_PER_LANE && plan.rpl != 2 && plan.rpl != 1)
+            fail(CPDLP_ERR_ARGUMENT, "tile plan row cap");
+        switch (plan.items) {
+            case 4: CPDLP_TILES(4, ROWS_PER_LANE, false); break;
+            case 8: CPDLP_TILES(8, ROWS_PER_LANE, false); break;
+            default: CPDLP_TILES(16, ROWS_PER_LANE, false); break;
+        }
     }
+#undef CPDLP_TILES
     CK_LAUNCH();
 }
 template <int NVEC, class V, class T, class Epi>
@@ -410,7 +418,7 @@ void launch_tiles(const TilePlan& plan, const CsrView<V, T>& view, const VecSet<
 // four values in place, and every lane reduces its rows for the four iterates
 // side by side, each in ascending column order: iterate p's row sums are the
 // ones a one-iterate pass over x_p computes.
-template <int ITEMS, class V, class T, class Epi, int RPL = ROWS_PER_LANE>
+template <int ITEMS, class V, class T, class Epi, int RPL = ROWS_PER_LANE, bool MED = false>
 __device__ __forceinline__ void short_tile4(const CsrView<V, T>& A, const T* __restrict__ x4,
                                             Epi& epi, typename Epi::Acc& acc, int r0, int r1,
                                             int nz0, int nz1, int lane, T* g) {
@@ -471,10 +479,41 @@ __device__ __forceinline__ void short_tile4(const CsrView<V, T>& A, const T* __r
             }
     }
     __syncwarp();
+    // rows longer than LONG_ROW: the whole warp, lane-strided sums and a tree
+#pragma unroll
+    for (int k = 0; k < (MED ? RPL : 0); k++) {
+        const int r = r0 + lane + 32 * k;
+        unsigned med = __ballot_sync(FULL_MASK, r < r1 && rb[k] - ra[k] > LONG_ROW);
+        while (med) {
+            const int l = __ffs(med) - 1;
+            med &= med - 1;
+            const int a = __shfl_sync(FULL_MASK, ra[k], l) - nz0;
+            const int b = __shfl_sync(FULL_MASK, rb[k], l) - nz0;
+            T m0 = T(0), m1 = T(0), m2 = T(0), m3 = T(0);
+            for (int i = a + lane; i < b; i += 32) {
+                const T* gi = g + 4 * i;
+                m0 = add_rn(m0, gi[0]);
+                m1 = add_rn(m1, gi[1]);
+                m2 = add_rn(m2, gi[2]);
+                m3 = add_rn(m3, gi[3]);
+            }
+            m0 = warp_sum_tree(m0);
+            m1 = warp_sum_tree(m1);
+            m2 = warp_sum_tree(m2);
+            m3 = warp_sum_tree(m3);
+            if (lane == l) {
+                const typename Epi::Pre pre{};
+                epi.row(0, r, m0, pre, acc);
+                epi.row(1, r, m1, pre, acc);
+                epi.row(2, r, m2, pre, acc);
+                epi.row(3, r, m3, pre, acc);
+            }
+        }
+    }
 #pragma unroll
     for (int k = 0; k < RPL; k++) {
         const int r = r0 + lane + 32 * k;
-        if (r < r1) {
+        if (r < r1 && rb[k] - ra[k] <= LONG_ROW) {
             T s0 = T(0), s1 = T(0), s2 = T(0), s3 = T(0);
             for (int i = ra[k] - nz0; i < rb[k] - nz0; i++) {
                 const T* gi = g + 4 * i;
@@ -584,7 +623,7 @@ __device__ __forceinline__ void long_piece4(const CsrView<V, T>& A, const T* __r
     }
 }
 
-template <int ITEMS, int WARPS, class V, class T, class Epi>
+template <int ITEMS, int WARPS, class V, class T, class Epi, int RPL, bool MED>
 __global__ void __launch_bounds__(WARPS * 32)
     k_tiles4(CsrView<V, T> A, const T* __restrict__ x4, Epi epi) {
     __shared__ __align__(16) T prod[WARPS][4 * 32 * ITEMS];
@@ -596,7 +635,7 @@ __global__ void __launch_bounds__(WARPS * 32)
         long_piece4<ITEMS>(A, x4, epi, acc, A.ltasks[task], lane, prod[w]);
     } else if (task - A.nltasks < A.ntasks) {
         const int4 t = A.tasks[task - A.nltasks];
-        short_tile4<ITEMS>(A, x4, epi, acc, t.x, t.y, t.z, t.w, lane, prod[w]);
+        short_tile4<ITEMS, V, T, Epi, RPL, MED>(A, x4, epi, acc, t.x, t.y, t.z, t.w, lane, prod[w]);
     }
     epi.finish(acc);
 }
@@ -607,11 +646,22 @@ void launch_tiles4(const TilePlan& plan, const CsrView<V, T>& view, const T* x4,
     const int64_t tasks = (int64_t)plan.ntasks + plan.nltasks;
     if (tasks == 0) return;
     const unsigned grid = (unsigned)((tasks + WARPS - 1) / WARPS);
-    switch (plan.items) {
-        case 4: k_tiles4<4, WARPS, V, T, Epi><<<grid, WARPS * 32, 0, s>>>(view, x4, epi); break;
-        case 8: k_tiles4<8, WARPS, V, T, Epi><<<grid, WARPS * 32, 0, s>>>(view, x4, epi); break;
-        default: k_tiles4<16, WARPS, V, T, Epi><<<grid, WARPS * 32, 0, s>>>(view, x4, epi); break;
+#define CPDLP_TILES4(IT, R, M) k_tiles4<IT, WARPS, V, T, Epi, R, M><<<grid, WARPS * 32, 0, s>>>(view, x4, epi)
+    if (plan.medium) {
+        if (plan.rpl != 2) fail(CPDLP_ERR_ARGUMENT, "tile plan with long rows needs 64-row tiles");
+        switch (plan.items) {
+            case 4: CPDLP_TILES4(4, 2, true); break;
+            case 8: CPDLP_TILES4(8, 2, true); break;
+            default: CPDLP_TILES4(16, 2, true); break;
+        }
+    } else {
+        switch (plan.items) {
+            case 4: CPDLP_TILES4(4, ROWS_PER_LANE, false); break;
+            case 8: CPDLP_TILES4(8, ROWS_PER_LANE, false); break;
+            default: CPDLP_TILES4(16, ROWS_PER_LANE, false); break;
+        }
     }
+#undef CPDLP_TILES4
     CK_LAUNCH();
 }
 
