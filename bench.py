@@ -63,7 +63,12 @@ def parse_args():
                     help="LPs of the batch solved one at a time by the FP64 path")
     ap.add_argument("--serve-requests", type=int, default=160,
                     help="requests of the served stream (0 skips the serving measurement)")
-    ap.add_argument("--serve-rate", type=float, default=8.0, help="Poisson arrivals per second")
+    ap.add_argument("--serve-rates", type=str, default="8,16,32",
+                    help="Poisson arrival rates per second, comma separated")
+    ap.add_argument("--c1-solves", type=int, default=1,
+                    help="1: solve the large LP to 1e-4 and (refined) to 1e-8 in the line")
+    ap.add_argument("--c1-time-limit", type=float, default=150.0,
+                    help="time limit in seconds of each large-LP solve")
     ap.add_argument("--batch-m-hi", type=int, default=5000,
                     help="largest m of the batched LPs (5000 = the named workload)")
     ap.add_argument("--flow-side", type=int, default=256,
@@ -111,6 +116,35 @@ def load_peak():
             return float(json.load(f)["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+def rel_kkt(st) -> float:
+    e = st.err
+    return max(e.primal / e.primal_scale, e.dual / e.dual_scale, e.gap / e.gap_scale)
+
+
+def fp64_reference(h, lp, reltol: float = 1e-8, time_limit: float = 60.0):
+    """The plain FP64 path (cpdlp_solve, Float64 iterates) to `reltol`: the
+    FP64 reference objective that every reported result is compared with."""
+    from coolpdlp import native
+    p = native.default_params()
+    p.termination_reltol = reltol
+    p.max_kkt_passes = 1 << 40
+    p.time_limit = time_limit
+    L = native.LPStruct(lp.m, lp.n, lp.colptr, lp.rowval, lp.nzval, lp.c, lp.lv, lp.uv, lp.lc,
+                        lp.uc)
+    x, _, st = native.solve_lp(h, L, p)
+    return float(lp.c @ x), st
+
+
+def obj_err(obj: float, ref: float) -> float:
+    return abs(obj - ref) / max(1.0, abs(ref))
+
+
+def err_summary(errs) -> dict:
+    import numpy as np
+    a = np.asarray(errs, dtype=float)
+    return {"max": float(a.max()), "median": float(np.median(a)), "count": int(a.size)}
 
 
 class ClockSampler:
@@ -166,26 +200,59 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_baseline(lp, budget_s: float = 20.0) -> dict:
-    """The oracle (CPU restatement, FP64, all host threads) on the same LP:
-    preprocessing untimed, then whole 100-iteration blocks until ~budget_s."""
+def cpu_baseline(lp, budget_s: float = 16.0, single_core_s: float = 6.0, c0=None) -> dict:
+    """The oracle (CPU restatement, FP64) on the same LP: preprocessing
+    untimed, then 10-iteration steps until ~budget_s on all host threads
+    (OpenMP row loops), and a sample on 1 thread (the reference's CPU path is
+    single-threaded).  With `c0` (the GPU's FP64 C0 result), the C0 LP is also
+    solved by the oracle on 1 thread: iterations/s and parity (status, KKT
+    passes, objective)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
     import oracle as O
+    cores = int(O.lib().orc_num_threads())
     prm = O.params(termination_reltol=0.0, max_kkt_passes=1 << 60, time_limit=1e30)
     t0 = time.perf_counter()
     S = O.OracleState(lp, prm)
     t_setup = time.perf_counter() - t0
-    iters, t = 0, 0.0
-    while t < budget_s and iters < 100 * 50:
-        a = time.perf_counter()
-        S.step(10)
-        t += time.perf_counter() - a
-        iters += 10
+
+    def sample(limit_s, max_iters):
+        iters, t = 0, 0.0
+        while t < limit_s and iters < max_iters:
+            a = time.perf_counter()
+            S.step(10)
+            t += time.perf_counter() - a
+            iters += 10
+        return iters, t
+
+    iters, t = sample(budget_s, 100 * 50)
+    O.lib().orc_set_num_threads(1)
+    it1, t1 = sample(single_core_s, 100 * 50)
+    O.lib().orc_set_num_threads(cores)
     S.close()
-    return {"value": iters / t, "unit": UNIT, "cores": int(O.lib().orc_num_threads()),
-            "kind": "port",
-            "sample": (f"{iters} PDLP iterations (FP64) of the same LP after "
-                       f"{t_setup:.1f} s of untimed preprocessing"), "seconds": t}
+    out = {"value": iters / t, "unit": UNIT, "cores": cores, "kind": "port",
+           "precision": "FP64",
+           "sample": (f"{iters} PDLP iterations (FP64) of the same LP after "
+                      f"{t_setup:.1f} s of untimed preprocessing"), "seconds": t,
+           "single_core": {"value": it1 / t1, "unit": UNIT, "cores": 1,
+                           "sample": f"{it1} PDLP iterations (FP64) of the same LP"}}
+    if c0 is not None:
+        from coolpdlp import generators as G
+        lp0 = G.random_sparse_lp(1000, 2000, 5, seed=0)
+        O.lib().orc_set_num_threads(1)
+        a = time.perf_counter()
+        xo, _, so = O.solve(lp0, O.params())
+        dt = time.perf_counter() - a
+        O.lib().orc_set_num_threads(cores)
+        obj = float(lp0.c @ xo)
+        out["c0"] = {"iters_per_s": so["kkt_passes"] / dt, "cores": 1,
+                     "termination_status": so["termination_status"],
+                     "kkt_passes": so["kkt_passes"], "objective": obj,
+                     "parity_vs_gpu_fp64": {
+                         "same_status": so["termination_status"] == c0["status"],
+                         "same_kkt_passes": so["kkt_passes"] == c0["iterations"],
+                         "objective_rel_diff": obj_err(c0["objective"], obj)}}
+    return out
 
 
 def measure_batch(h, count: int, sample: int, m_hi: int = 5000, rank: int = 0, world: int = 1,
@@ -255,6 +322,17 @@ def measure_batch(h, count: int, sample: int, m_hi: int = 5000, rank: int = 0, w
                               "mean_passes": passes / len(idx)}
     out["speedup_fp32_refined_vs_sequential"] = out["fp32_refined"]["lps_per_s"] / seq
     out["speedup_fp64_batched_vs_sequential"] = out["fp64_batched"]["lps_per_s"] / seq
+    if world > 1:  # the sample's indices are global, the results are this rank's shard
+        return out
+    # every batched result of the sample against the FP64 path solved to 1e-8
+    errs = {"fp32_refined": [], "fp64_batched": []}
+    for k in idx:
+        ref, st = fp64_reference(h, all_lps[k])
+        for name in errs:
+            errs[name].append(obj_err(obj(k, res[name][k]), ref))
+    out["err_vs_fp64"] = {"reference": ("plain FP64 path (cpdlp_solve) to 1e-8 relative KKT on "
+                                        f"the same {len(idx)}-LP sample; relative objective error"),
+                          **{name: err_summary(v) for name, v in errs.items()}}
     return out
 
 
@@ -325,33 +403,121 @@ def measure_flow(h, side: int, K: int, blocks: int = 10, solves: bool = True) ->
         out[tag] = {"status": int(st.termination_status), "iterations": int(st.kkt_passes),
                     "refine_iterations": int(st.refine_kkt_passes), "rel_kkt": rel,
                     "seconds": dt, "objective": float(np.dot(lp.c, x))}
+    if solves:
+        out["err_vs_fp64"] = fp64_verified_errors(out)
     return out
 
 
-def measure_serving(requests: int, rate: float) -> dict:
+def fp64_verified_errors(sec: dict) -> dict:
+    """Objective error of the 1e-4 result against the 1e-8 result, whose KKT
+    error is evaluated in FP64 on the FP64 copy of the LP (the refinement's
+    FP64 residuals): the FP64 reference at sizes where the plain FP64 path
+    cannot reach 1e-8 within the bench."""
+    ref = sec["solve_1e-8"]
+    return {"reference": ("solve_1e-8 result (FP32 corrections accumulated in FP64, KKT "
+                          f"evaluated in FP64: relative KKT {ref['rel_kkt']:.2e}, status "
+                          f"{ref['status']})"),
+            "solve_1e-4": obj_err(sec["solve_1e-4"]["objective"], ref["objective"]),
+            "solve_1e-8": 0.0}
+
+
+def measure_c1_solves(h, lp, tl_1e4: float, tl_1e8: float) -> dict:
+    """cpdlp_solve of the large single LP from host memory: to 1e-4 relative
+    KKT with FP32 iterates, and to 1e-8 with FP32 iterates plus refinement
+    rounds (FP64 residuals and KKT errors); iterations, seconds, final relative
+    KKT error and objective, each within the stated time limit."""
+    import numpy as np
+    from coolpdlp import _abi as A
+    from coolpdlp import native
+    L = native.LPStruct(lp.m, lp.n, lp.colptr, lp.rowval, lp.nzval, lp.c, lp.lv, lp.uv, lp.lc,
+                        lp.uc)
+    out = {}
+    for tag, tol, refine, tl in (("solve_1e-4", 1e-4, 0.0, tl_1e4),
+                                 ("solve_1e-8", 1e-4, 1e-8, tl_1e8)):
+        prm = A.default_params_py(A.ALGO_PDLP)
+        prm.float_type = A.VAL_F32
+        prm.termination_reltol = tol
+        prm.refine_reltol = refine
+        prm.max_kkt_passes = 1 << 40
+        prm.time_limit = tl
+        t0 = time.perf_counter()
+        x, y, st = native.solve_lp(h, L, prm)
+        dt = time.perf_counter() - t0
+        e = st.err
+        out[tag] = {"status": int(st.termination_status), "iterations": int(st.kkt_passes),
+                    "refine_iterations": int(st.refine_kkt_passes), "rel_kkt": rel_kkt(st),
+                    "rel_primal": e.primal / e.primal_scale, "rel_dual": e.dual / e.dual_scale,
+                    "rel_gap": e.gap / e.gap_scale, "seconds": dt,
+                    "iters_per_s": st.kkt_passes / dt, "time_limit_s": tl,
+                    "objective": float(np.dot(lp.c, x))}
+    out["err_vs_fp64"] = fp64_verified_errors(out)
+    return out
+
+
+def measure_c0(h, reps: int = 5) -> dict:
+    """The 1,000 x 2,000 random sparse LP (5 nonzeros per column, seed 0) with
+    plain FP64 PDLP to 1e-4 through cpdlp_solve: iterations/s, kernel launches
+    per iteration and the result (its oracle parity is in cpu_baseline.c0)."""
+    import numpy as np
+    from coolpdlp import generators as G
+    from coolpdlp import native
+    lp = G.random_sparse_lp(1000, 2000, 5, seed=0)
+    L = native.LPStruct(lp.m, lp.n, lp.colptr, lp.rowval, lp.nzval, lp.c, lp.lv, lp.uv, lp.lc,
+                        lp.uc)
+    p = native.default_params()
+    native.solve_lp(h, L, p)  # warm-up (module load, allocator pools)
+    ts = []
+    for _ in range(reps):
+        a = time.perf_counter()
+        x, y, st = native.solve_lp(h, L, p)
+        ts.append(time.perf_counter() - a)
+    t = statistics.median(ts)
+    return {"workload": "random sparse LP m=1,000 n=2,000 5 nnz/column seed 0, FP64, 1e-4",
+            "status": int(st.termination_status), "iterations": int(st.kkt_passes),
+            "seconds": t, "iters_per_s": st.kkt_passes / t,
+            "launches_per_iter": st.kernel_launches / max(1, st.kkt_passes),
+            "objective": float(np.dot(lp.c, x)), "rel_kkt": rel_kkt(st)}
+
+
+def measure_serving(requests: int, rates, err_sample: int = 12) -> dict:
     """The served stream: Poisson arrivals, 80% random sparse LPs (m log-U[100,
     20000]) and 20% grid multicommodity flows (side U{32..128}, K U{2..8}),
     tolerance 1e-4 or 1e-8; replayed in real time through the continuous-
-    batching server with FP32+FP64-refined and with plain FP64 iterates."""
+    batching server with FP32+FP64-refined iterates at each arrival rate of
+    `rates` (the first also with plain FP64 iterates), then all requests
+    arriving at once (throughput when the GPU is the bottleneck).  A sample of
+    the served results is checked against the plain FP64 path to 1e-8."""
+    import numpy as np
     from coolpdlp import _abi as A
     from coolpdlp import generators as G
+    from coolpdlp import native
     from coolpdlp import serving
-    reqs = G.served_stream(requests, rate, seed=7)
-    t0 = time.perf_counter()
-    lps = [G.request_lp(r) for r in reqs]
-    gen_s = time.perf_counter() - t0
-    out = {"requests": requests, "rate_per_s": rate, "generation_s": gen_s,
-           "workload": (f"{requests} Poisson arrivals at {rate}/s: 80% random sparse LPs "
+    out = {"requests": requests, "rates_per_s": list(rates),
+           "workload": (f"{requests} Poisson arrivals per rate: 80% random sparse LPs "
                         "m log-U[100,20000] n=2m 5 nnz/col, 20% grid multicommodity flows "
                         "side U{32..128} K U{2..8}; tolerance 1e-4 or 1e-8; "
                         "150 GB admission budget")}
-    for name, ft in (("fp32_refined", A.VAL_F32), ("fp64", A.VAL_F64)):
-        srv = serving.Server(float_type=ft, hbm_budget=150e9)
-        r = serving.replay(srv, [q.arrival for q in reqs], lps, [q.reltol for q in reqs])
-        srv.close()
-        out[name] = r
-    # the plain FP64 one-LP-at-a-time path (cpdlp_solve) on an evenly spaced sample
-    from coolpdlp import native
+    t0 = time.perf_counter()
+    reqs = G.served_stream(requests, 1.0, seed=7)
+    lps = [G.request_lp(r) for r in reqs]
+    out["generation_s"] = time.perf_counter() - t0
+    base = np.array([q.arrival for q in reqs])   # arrival times at 1 request/s
+    tols = [q.reltol for q in reqs]
+    sweep = {}
+    kept = {}
+    for i, rate in enumerate(rates):
+        modes = (("fp32_refined", A.VAL_F32), ("fp64", A.VAL_F64)) if i == 0 else \
+            (("fp32_refined", A.VAL_F32),)
+        row = {}
+        for name, ft in modes:
+            srv = serving.Server(float_type=ft, hbm_budget=150e9)
+            row[name] = serving.replay(srv, list(base / rate), lps, tols)
+            if i == 0:
+                kept[name] = dict(srv.results)
+            srv.close()
+        sweep[f"{rate:g}/s"] = row
+    out["sweep"] = sweep
+    # the plain FP64 path one request at a time (cpdlp_solve), evenly spaced sample
     h = native.Handle(0)
     idx = list(range(0, requests, max(1, requests // 40)))[:40]
     t0 = time.perf_counter()
@@ -363,15 +529,29 @@ def measure_serving(requests: int, rate: float) -> dict:
                                            lp.lv, lp.uv, lp.lc, lp.uc), p)
     seq = len(idx) / (time.perf_counter() - t0)
     out["fp64_sequential"] = {"lps_per_s": seq, "sample": len(idx)}
-    for name in ("fp32_refined", "fp64"):
-        out[name]["throughput_vs_sequential"] = out[name]["throughput_lps_per_s"] / seq
-    # the same requests all arriving at once: throughput when the GPU is the
-    # bottleneck, not the arrival rate
+    for row in sweep.values():
+        for r in row.values():
+            r["throughput_vs_sequential"] = r["throughput_lps_per_s"] / seq
     srv = serving.Server(float_type=A.VAL_F32, hbm_budget=150e9)
-    r = serving.replay(srv, [0.0] * len(reqs), lps, [q.reltol for q in reqs])
+    r = serving.replay(srv, [0.0] * len(reqs), lps, tols)
     srv.close()
     r["throughput_vs_sequential"] = r["throughput_lps_per_s"] / seq
     out["fp32_refined_saturated"] = r
+    # served results (first rate) against the FP64 path to 1e-8, on the
+    # requests of the batched route (up to 40,000 nonzeros), evenly spaced
+    small = [i for i in range(requests) if lps[i].nnz <= 40_000]
+    pick = small[::max(1, len(small) // err_sample)][:err_sample]
+    errs = {name: {"1e-4": [], "1e-8": []} for name in kept}
+    for i in pick:
+        ref, _ = fp64_reference(h, lps[i])
+        key = "1e-8" if tols[i] < 1e-6 else "1e-4"
+        for name, res in kept.items():
+            errs[name][key].append(obj_err(float(lps[i].c @ res[i].x), ref))
+    out["err_vs_fp64"] = {
+        "reference": ("plain FP64 path (cpdlp_solve) to 1e-8 relative KKT; relative objective "
+                      f"error of {len(pick)} served results of the first rate, by requested "
+                      "tolerance"),
+        **{name: {k: err_summary(v) for k, v in d.items() if v} for name, d in errs.items()}}
     return out
 
 
@@ -567,15 +747,23 @@ def run_ours(args):
             "clocks": clocks,
             "wall_s_timed": wall, "setup_s": setup_s,
         }
+        line["precision"] = {"value": "FP32 iterates and SpMVs, FP64 KKT/restart sums",
+                             "e2e": "FP32 iterates and SpMVs, FP64 KKT/restart sums",
+                             "cpu_baseline": "FP64 (CPU restatement of the reference)"}
+        c0 = measure_c0(h)
+        line["c0"] = c0
         if not args.no_cpu_baseline:
-            line["cpu_baseline"] = cpu_baseline(lp)
+            line["cpu_baseline"] = cpu_baseline(lp, c0=c0)
+        if args.c1_solves:
+            line["c1"] = measure_c1_solves(h, lp, args.c1_time_limit, args.c1_time_limit)
         if args.flow_side > 0:
             line["flow"] = measure_flow(h, args.flow_side, args.flow_k,
                                         solves=not args.flow_no_solve)
         if batch is not None:
             line["batch"] = batch
         if args.serve_requests > 0:
-            line["serving"] = measure_serving(args.serve_requests, args.serve_rate)
+            rates = [float(r) for r in args.serve_rates.split(",") if r]
+            line["serving"] = measure_serving(args.serve_requests, rates)
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.barrier()
