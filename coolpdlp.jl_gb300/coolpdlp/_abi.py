@@ -34,7 +34,7 @@ ALGO_PDLP, ALGO_PDHG = 0, 1
 VAL_F64, VAL_F32, VAL_PM1 = 0, 1, 2
 # tile_flags bits: CPDLP_TILE_NO_NARROW keeps scaled values for a +-1 matrix
 TILE_NO_NARROW = 1
-FMT_CSR, FMT_ELL, FMT_COO = 0, 1, 2
+FMT_AUTO, FMT_CSR, FMT_ELL, FMT_COO = -1, 0, 1, 2
 VEC_SOL, VEC_SOL_LAST, VEC_SOL_AVG, VEC_SOL_AVG_LAST, VEC_SOL_RESTART = 0, 1, 2, 3, 4
 
 
@@ -68,6 +68,7 @@ class ParamsC(Structure):
         ("tile_nnz", c_int32),
         ("tile_flags", c_int32),
         ("infeasibility_tol", c_double),
+        ("matrix_type", c_int32),
     ]
 
 
@@ -126,6 +127,7 @@ def default_params_py(algorithm: int = ALGO_PDLP) -> ParamsC:
     p.tile_nnz = 0
     p.tile_flags = 0
     p.infeasibility_tol = 0.0
+    p.matrix_type = FMT_AUTO
     return p
 
 
@@ -165,6 +167,7 @@ EXPORTED_SYMBOLS = (
     "cpdlp_state_create", "cpdlp_state_destroy", "cpdlp_state_solve", "cpdlp_state_step",
     "cpdlp_state_kkt", "cpdlp_state_vectors", "cpdlp_state_solution", "cpdlp_state_stats",
     "cpdlp_state_history", "cpdlp_solve", "cpdlp_solve_history", "cpdlp_problem_spectral_norm",
+    "cpdlp_problem_layout",
     "cpdlp_batch_solve", "cpdlp_state_solve_blocks", "cpdlp_state_profile",
     "cpdlp_state_kernel_bytes", "cpdlp_spmv_csr_noalloc",
     "cpdlp_submit", "cpdlp_poll", "cpdlp_wait", "cpdlp_cancel", "cpdlp_collect",
@@ -208,6 +211,7 @@ def _declare(lib):
         "cpdlp_solve": (c_int32, [H, POINTER(LPC), POINTER(ParamsC), PD, PD, PD, PD,
                                   POINTER(StatsC)]),
         "cpdlp_solve_history": (c_int32, [H, P64, POINTER(KKTErrorsC), c_int64, P64]),
+        "cpdlp_problem_layout": (c_int32, [H, POINTER(c_int32), POINTER(c_int32), P64]),
         "cpdlp_problem_spectral_norm": (c_int32, [H, H, POINTER(ParamsC), PD, P64]),
         "cpdlp_batch_solve": (c_int32, [H, c_int64, POINTER(LPC), POINTER(ParamsC),
                                         POINTER(PD), POINTER(PD), POINTER(StatsC)]),

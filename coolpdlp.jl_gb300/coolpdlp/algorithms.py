@@ -101,8 +101,12 @@ class Algorithm:
 
     name: "PDLP" or "PDHG"; T: np.float64 / np.float32 (iterate precision);
     Ti: index type (the device always uses int32 indices, so only its range is
-    checked); M: matrix format name ("CSR", "ELL", "COO"; the solver itself
-    runs on the device CSR engine)."""
+    checked); M: the matrix type of the solve's products (conversion.jl:37-55):
+    "CSR" (the CSR tile engine), "ELL" (the reference's ELL layout, one thread
+    per row), "COO" (solved on the CSR engine: the reference's COO product
+    sums with atomics in a run-dependent order), a GPUSparseMatrix* class, or
+    None / "AUTO" (default): the autotuner picks per matrix among CSR tile
+    shapes and ELL for matrices of at least 2^21 nonzeros."""
 
     KEYWORDS = ("chambolle_pock_alpha", "ruiz_iter", "invnorm_scaling", "primal_weight_damping",
                 "zero_tol", "sufficient_decay", "necessary_decay", "artificial_decay",
@@ -110,7 +114,9 @@ class Algorithm:
                 "max_kkt_passes", "time_limit", "power_tol_override", "power_maxiter_override",
                 "power_seed", "refine_reltol", "tile_nnz", "tile_flags", "infeasibility_tol")
 
-    def __init__(self, name: str = "PDLP", T=np.float64, Ti=np.int64, M="CSR", *, device: int = 0,
+    FORMATS = {"AUTO": A.FMT_AUTO, "CSR": A.FMT_CSR, "ELL": A.FMT_ELL, "COO": A.FMT_COO}
+
+    def __init__(self, name: str = "PDLP", T=np.float64, Ti=np.int64, M=None, *, device: int = 0,
                  backend=None, **kw):
         name = name.upper()
         if name not in ("PDLP", "PDHG"):
@@ -121,11 +127,16 @@ class Algorithm:
             raise A.ArgumentError(A.ERR_ARGUMENT, "T must be Float64 or Float32")
         self.T = T
         self.Ti = Ti
-        self.M = M if isinstance(M, str) else getattr(M, "FORMAT", "CSR")
+        if M is None:
+            M = "AUTO"
+        self.M = (M if isinstance(M, str) else getattr(M, "FORMAT", "CSR")).upper()
+        if self.M not in self.FORMATS:
+            raise A.ArgumentError(A.ERR_ARGUMENT, f"unknown matrix type {M}")
         self.device = device if backend is None else int(getattr(backend, "device", backend))
         algo = A.ALGO_PDLP if name == "PDLP" else A.ALGO_PDHG
         p = A.default_params_py(algo)
         p.float_type = A.VAL_F32 if T is np.float32 else A.VAL_F64
+        p.matrix_type = self.FORMATS[self.M]
         for k, v in kw.items():
             if k not in self.KEYWORDS:
                 raise TypeError(f"unexpected keyword {k}")
@@ -140,12 +151,12 @@ class Algorithm:
         return f"{self.name} algorithm (T={self.T.__name__}, M={self.M}): {kw}"
 
 
-def PDLP(T=np.float64, Ti=np.int64, M="CSR", **kw) -> Algorithm:
+def PDLP(T=np.float64, Ti=np.int64, M=None, **kw) -> Algorithm:
     """pdlp.jl:6-11"""
     return Algorithm("PDLP", T, Ti, M, **kw)
 
 
-def PDHG(T=np.float64, Ti=np.int64, M="CSR", **kw) -> Algorithm:
+def PDHG(T=np.float64, Ti=np.int64, M=None, **kw) -> Algorithm:
     """pdhg.jl:6-16: ruiz_iter = 0 and NaN restart / primal-weight parameters."""
     kw.setdefault("ruiz_iter", 0)
     return Algorithm("PDHG", T, Ti, M, **kw)

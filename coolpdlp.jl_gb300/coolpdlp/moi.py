@@ -263,7 +263,7 @@ class Optimizer:
             warnings.warn(f"Got mismatched float type: solving in {float_type.__name__} but "
                           f"returning the solution in {self.T.__name__}.")
         int_type = opts.pop("int_type", np.int64)
-        matrix_type = opts.pop("matrix_type", "CSR")
+        matrix_type = opts.pop("matrix_type", None)
         device = int(opts.pop("backend", 0) or 0)
         kw = {"show_progress": not self.silent}
         kw.update(opts)

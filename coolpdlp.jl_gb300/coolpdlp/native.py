@@ -114,6 +114,17 @@ class Problem:
                                                      byref(p)), "cpdlp_problem_create")
         self.p = p
 
+    def layout(self) -> dict:
+        """cpdlp_problem_layout: format, CSR tile size and ELL width of the
+        products over the rows of A ("A") and of A' ("At")."""
+        fmt = (c_int32 * 2)()
+        tile = (c_int32 * 2)()
+        width = (c_int64 * 2)()
+        self.handle.check(self.handle.lib.cpdlp_problem_layout(self.p, fmt, tile, width))
+        names = {A.FMT_CSR: "CSR", A.FMT_ELL: "ELL"}
+        return {side: {"format": names.get(fmt[k], str(fmt[k])), "tile_nnz": int(tile[k]),
+                       "ell_width": int(width[k])} for k, side in enumerate(("A", "At"))}
+
     def scaling(self):
         d1 = np.empty(self.m)
         d2 = np.empty(self.n)

@@ -74,6 +74,7 @@ void cpdlp_params_default(cpdlp_params* p, int32_t algorithm) {
     p->refine_reltol = 0.0;
     p->tile_nnz = 0;
     p->infeasibility_tol = 0.0;
+    p->matrix_type = CPDLP_FMT_AUTO;
 }
 
 int cpdlp_create(int32_t device, cpdlp_handle** out) {
@@ -339,6 +340,19 @@ int cpdlp_state_history(const cpdlp_state* s, int64_t* kkt_passes, cpdlp_kkt_err
         if (errs) errs[t] = S->hist_err[(size_t)t];
     }
     if (count) *count = len;
+    return CPDLP_OK;
+}
+
+int cpdlp_problem_layout(const cpdlp_problem* p, int32_t* format, int32_t* tile_nnz,
+                         int64_t* width) {
+    if (!p) return CPDLP_ERR_ARGUMENT;
+    const ProblemBase* P = reinterpret_cast<const ProblemBase*>(p);
+    for (int sd = 0; sd < 2; sd++) {
+        const bool ell = P->fmt[sd] == CPDLP_FMT_ELL;
+        if (format) format[sd] = P->fmt[sd];
+        if (tile_nnz) tile_nnz[sd] = ell ? 0 : (sd == 0 ? P->planA : P->planAt).tile_nnz();
+        if (width) width[sd] = ell ? P->ell_width[sd] : 0;
+    }
     return CPDLP_OK;
 }
 

@@ -26,6 +26,7 @@
 #include <memory>
 #include <type_traits>
 
+#include "ell.cuh"
 #include "epilogues.cuh"
 #include "solver.cuh"
 
@@ -372,47 +373,164 @@ CsrView<Pm1, T> view_At_pm1(ProblemT<T>& P) {
                            P.planAt.ltasks.p, P.planAt.nltasks, P.planAt.counters.p, P.partAt.p};
 }
 
-// Autotuner of the tile shape (nonzeros per lane) of one CSR matrix: each
-// candidate's plan is built and the fused step kernel that uses the matrix (the
-// primal step for A', the dual step for A) is timed with CUDA events on the
-// handle's stream, on scratch vectors.  The heuristic's choice is kept unless
-// another candidate is at least 3% faster.  Decisions are cached per matrix
-// shape for the process.
+// ---- the product of one matrix of the problem (side 0: rows of A, the dual
+// step; side 1: rows of A', the primal step) in its chosen format ----------
+template <class T>
+int64_t side_rows(const ProblemT<T>& P, int side) { return side == 0 ? P.m : P.n; }
+
+// blocks of a launch over `side` with `warps` warps per block (the
+// block-partial rows of a reducing epilogue; its long-row outputs follow)
+template <class T>
+int64_t side_blocks(const ProblemT<T>& P, int side, int warps) {
+    if (P.fmt[side] == CPDLP_FMT_ELL) return side_rows(P, side) > 0 ? ell_grid(side_rows(P, side), warps) : 0;
+    return tiles_grid(side == 0 ? P.planA : P.planAt, warps);
+}
+// all partial rows a reducing epilogue writes over `side`
+template <class T>
+int64_t side_partials(const ProblemT<T>& P, int side, int warps) {
+    const int64_t longs = P.fmt[side] == CPDLP_FMT_ELL ? 0 : (side == 0 ? P.planA : P.planAt).nlong;
+    return side_blocks(P, side, warps) + longs;
+}
+
+template <class V, class VT, class T>
+EllView<V, VT> ell_view(const ProblemT<T>& P, int side, const int32_t* ptr) {
+    const V* val = nullptr;
+    if constexpr (!is_pm1<V>::value) val = P.ell_val[side].p;
+    return EllView<V, VT>{ptr, P.ell_idx[side].p, val, side_rows(P, side)};
+}
+
+// One product over `side` with the fused epilogue `epi`, in the side's
+// format: the CSR view's tile plan, or the ELL slabs (the view's row pointer
+// gives the row lengths).  W: warps per block (the epilogue's block size).
+template <int W = TILE_WARPS, int NVEC, class V, class VT, class Epi, class T>
+void launch_side(const ProblemT<T>& P, int side, const CsrView<V, VT>& view,
+                 const VecSet<VT, NVEC>& xs, const Epi& epi, cudaStream_t s) {
+    if (P.fmt[side] == CPDLP_FMT_ELL)
+        launch_ell<W>(ell_view<V, VT>(P, side, view.ptr), xs, epi, s);
+    else
+        launch_tiles_w<W>(side == 0 ? P.planA : P.planAt, view, xs, epi, s);
+}
+// four packed iterates (the KKT pass)
+template <int W, class V, class VT, class Epi, class T>
+void launch_side4(const ProblemT<T>& P, int side, const CsrView<V, VT>& view, const VT* x4,
+                  const Epi& epi, cudaStream_t s) {
+    if (P.fmt[side] == CPDLP_FMT_ELL)
+        launch_ell4<W>(ell_view<V, VT>(P, side, view.ptr), x4, epi, s);
+    else
+        launch_tiles4<W>(side == 0 ? P.planA : P.planAt, view, x4, epi, s);
+}
+
+// the ELL slabs of a CSR (0-based; narrow storage keeps the signed index):
+// entry k of row r at r + k*rows, padding index 0 and value 0 (never read)
+template <class T>
+__global__ void k_csr_to_ell(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+                             const T* __restrict__ val, int64_t rows, int64_t width,
+                             int32_t* __restrict__ eidx, T* __restrict__ eval) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    const int a = ptr[r], len = ptr[r + 1] - a;
+    for (int64_t k = 0; k < width; k++) {
+        const bool in = k < len;
+        eidx[r + k * rows] = in ? idx[a + k] : 0;
+        if (eval) eval[r + k * rows] = in ? val[a + k] : T(0);
+    }
+}
+template <class T>
+void build_ell(Handle& h, ProblemT<T>& P, int side, const std::vector<int32_t>& hp) {
+    const int64_t rows = side_rows(P, side);
+    int64_t width = 0;
+    for (int64_t r = 0; r < rows; r++) width = std::max<int64_t>(width, hp[r + 1] - hp[r]);
+    const size_t slots = (size_t)std::max<int64_t>(rows * width, 1);
+    P.ell_width[side] = width;
+    P.ell_idx[side].alloc(slots);
+    if (!P.pm1) P.ell_val[side].alloc(slots);
+    if (rows > 0 && width > 0) {
+        k_csr_to_ell<T><<<grid_for(rows, 256), 256, 0, h.stream>>>(
+            side == 0 ? P.a_ptr.p : P.at_ptr.p, side == 0 ? P.a_idx.p : P.at_idx.p,
+            P.pm1 ? nullptr : (side == 0 ? P.a_val.p : P.at_val.p), rows, width,
+            P.ell_idx[side].p, P.pm1 ? nullptr : P.ell_val[side].p);
+        CK_LAUNCH();
+    }
+}
+
+// Autotuner of one matrix's product (side 0: rows of A, side 1: rows of A'):
+// each candidate -- CSR tile shapes (nonzeros per lane) and, when allowed,
+// ELL -- runs the fused step kernel that uses the matrix (the primal step for
+// A', the dual step for A) on scratch vectors, timed with CUDA events on the
+// handle's stream.  The heuristic's tile shape is kept unless another
+// candidate is at least 3% faster.  Decisions are cached per matrix shape and
+// requested format for the process.  With ELL chosen the slabs stay in P.
 constexpr int64_t AUTOTUNE_MIN_NNZ = 1 << 21;
+// ELL is a candidate when its slabs hold at most this many times the nonzeros
+constexpr int64_t ELL_MAX_PADDING = 3;
+
+struct SideChoice {
+    int fmt;
+    int items;
+};
 
 template <class T, class Launch>
-int tune_items(Handle& h, const std::vector<int32_t>& hp, int32_t rows, int64_t cols, int64_t nnz,
-               int heuristic, int which, Launch&& launch) {
+SideChoice tune_side(Handle& h, ProblemT<T>& P, int side, const std::vector<int32_t>& hp,
+                     int heuristic, bool try_csr, bool try_ell, int which, Launch&& launch) {
     static std::mutex mu;
-    static std::map<std::tuple<int64_t, int64_t, int64_t, int, int, int>, int> cache;
-    const auto key = std::make_tuple((int64_t)rows, cols, nnz, (int)sizeof(T), h.device, which);
+    static std::map<std::tuple<int64_t, int64_t, int64_t, int, int, int, int>, SideChoice> cache;
+    const int64_t rows = side_rows(P, side), cols = side_rows(P, 1 - side);
+    const auto key = std::make_tuple(rows, cols, P.nnz, (int)sizeof(T), h.device, which,
+                                     (int)try_csr * 2 + (int)try_ell);
     {
         std::lock_guard<std::mutex> lock(mu);
         auto it = cache.find(key);
-        if (it != cache.end()) return it->second;
+        if (it != cache.end()) {
+            if (it->second.fmt == CPDLP_FMT_ELL) {
+                build_ell(h, P, side, hp);
+                P.fmt[side] = CPDLP_FMT_ELL;
+            }
+            return it->second;
+        }
     }
     cudaStream_t s = h.stream;
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
-    int best = heuristic;
+    SideChoice best{try_csr ? CPDLP_FMT_CSR : CPDLP_FMT_ELL, heuristic};
     float best_ms = INFINITY;
-    const int cands[3] = {heuristic, heuristic == 4 ? 8 : 4, heuristic == 16 ? 8 : 16};
+    auto timed = [&](int fmt, TilePlan& pl, T* part) {
+        launch(fmt, pl, part);
+        CK(cudaEventRecord(e0, s));
+        for (int r = 0; r < 4; r++) launch(fmt, pl, part);
+        CK(cudaEventRecord(e1, s));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        return ms;
+    };
     try {
-        for (int items : cands) {
-            TilePlan plan;
-            build_tile_plan(hp, rows, items, plan, s);
-            DBuf<T> part((size_t)std::max(plan.npieces, 1));
-            launch(plan, part.p);
-            CK(cudaEventRecord(e0, s));
-            for (int r = 0; r < 4; r++) launch(plan, part.p);
-            CK(cudaEventRecord(e1, s));
-            CK(cudaEventSynchronize(e1));
-            float ms = 0.f;
-            CK(cudaEventElapsedTime(&ms, e0, e1));
-            if (items == heuristic ? ms < best_ms : ms < 0.97f * best_ms) {
+        if (try_csr) {
+            const int cands[3] = {heuristic, heuristic == 4 ? 8 : 4, heuristic == 16 ? 8 : 16};
+            for (int items : cands) {
+                TilePlan plan;
+                build_tile_plan(hp, (int32_t)rows, items, plan, s);
+                DBuf<T> part((size_t)std::max(plan.npieces, 1));
+                const float ms = timed(CPDLP_FMT_CSR, plan, part.p);
+                if (items == heuristic ? ms < best_ms : ms < 0.97f * best_ms) {
+                    best_ms = ms;
+                    best = SideChoice{CPDLP_FMT_CSR, items};
+                }
+            }
+        }
+        if (try_ell) {
+            build_ell(h, P, side, hp);
+            P.fmt[side] = CPDLP_FMT_ELL;
+            TilePlan none;
+            const float ms = timed(CPDLP_FMT_ELL, none, nullptr);
+            if (!try_csr || ms < 0.97f * best_ms) {
                 best_ms = ms;
-                best = items;
+                best = SideChoice{CPDLP_FMT_ELL, heuristic};
+            } else {
+                P.fmt[side] = CPDLP_FMT_CSR;
+                P.ell_idx[side] = DBuf<int32_t>();
+                P.ell_val[side] = DBuf<T>();
+                P.ell_width[side] = 0;
             }
         }
     } catch (...) {
@@ -593,7 +711,27 @@ ProblemBase* make_problem(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm
     CK(cudaMemcpyAsync(hp1.data(), P->at_ptr.p, sizeof(int32_t) * (n + 1), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     int items_A = choose_items(nnz, m, prm->tile_nnz), items_At = choose_items(nnz, n, prm->tile_nnz);
-    if (prm->tile_nnz == 0 && nnz >= AUTOTUNE_MIN_NNZ) {
+    // the product format: matrix_type (COO solves on the CSR engine), or the
+    // autotuner's choice for large matrices
+    const int32_t mt = prm->matrix_type;
+    if (mt != CPDLP_FMT_AUTO && mt != CPDLP_FMT_CSR && mt != CPDLP_FMT_ELL && mt != CPDLP_FMT_COO)
+        fail(CPDLP_ERR_ARGUMENT, "matrix_type must be CPDLP_FMT_AUTO, _CSR, _ELL or _COO");
+    auto ell_fits = [&](const std::vector<int32_t>& hp, int64_t rows) {
+        int64_t w = 0;
+        for (int64_t r = 0; r < rows; r++) w = std::max<int64_t>(w, hp[r + 1] - hp[r]);
+        return rows * w <= ELL_MAX_PADDING * std::max<int64_t>(nnz, 1);
+    };
+    const bool tune = mt == CPDLP_FMT_AUTO ? nnz >= AUTOTUNE_MIN_NNZ
+                                           : (mt != CPDLP_FMT_ELL && prm->tile_nnz == 0 &&
+                                              nnz >= AUTOTUNE_MIN_NNZ);
+    if (mt == CPDLP_FMT_ELL) {
+        build_ell(h, *P, 0, hp2);
+        build_ell(h, *P, 1, hp1);
+        P->fmt[0] = P->fmt[1] = CPDLP_FMT_ELL;
+    } else if (tune) {
+        const bool try_csr = true;
+        const bool ell_A = mt == CPDLP_FMT_AUTO && ell_fits(hp2, m);
+        const bool ell_At = mt == CPDLP_FMT_AUTO && ell_fits(hp1, n);
         // scratch iterates (zeros) for the fused step kernels being timed
         DBuf<T> vx(nzv), vxn(nzv), vxb(nzv), vxa(nzv), vxa2(nzv), vy(mz), vyn(mz), vya(mz),
             vya2(mz), vys(pm1 ? mz : 1);
@@ -602,45 +740,52 @@ ProblemBase* make_problem(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm
         DBuf<StepCoef<T>> cf(1);
         CK(cudaMemsetAsync(cf.p, 0, sizeof(StepCoef<T>), s));
         ProblemT<T>* Q = P;
-        items_At = tune_items<T>(h, hp1, (int32_t)n, m, nnz, items_At, pm1 ? 3 : 1,
-                                 [&](TilePlan& pl, T* part) {
+        const SideChoice cAt = tune_side<T>(h, *P, 1, hp1, items_At, try_csr, ell_At, pm1 ? 3 : 1,
+                                            [&](int fmt, TilePlan& pl, T* part) {
             if (pm1) {
                 const CsrView<Pm1, T> V{Q->at_ptr.p, Q->at_idx.p, nullptr, pl.tasks.p, pl.ntasks,
                                         pl.ltasks.p, pl.nltasks, pl.counters.p, part};
                 PrimalEpi<T, false, true> pe{vx.p, Q->c.p, Q->lv.p, Q->uv.p, vxn.p, vxb.p,
                                              vxa.p, vxa2.p, {cf.p}, 1, Q->d2t.p};
-                launch_tiles<1>(pl, V, VecSet<T, 1>{{vy.p}}, pe, s);
+                if (fmt == CPDLP_FMT_ELL) launch_ell<TILE_WARPS>(ell_view<Pm1, T>(*Q, 1, Q->at_ptr.p), VecSet<T, 1>{{vy.p}}, pe, s);
+                else launch_tiles<1>(pl, V, VecSet<T, 1>{{vy.p}}, pe, s);
             } else {
                 const CsrView<T, T> V{Q->at_ptr.p, Q->at_idx.p, Q->at_val.p, pl.tasks.p, pl.ntasks,
                                       pl.ltasks.p, pl.nltasks, pl.counters.p, part};
                 PrimalEpi<T> pe{vx.p, Q->c.p, Q->lv.p, Q->uv.p, vxn.p, vxb.p, vxa.p, vxa2.p, {cf.p}, 1};
-                launch_tiles<1>(pl, V, VecSet<T, 1>{{vy.p}}, pe, s);
+                if (fmt == CPDLP_FMT_ELL) launch_ell<TILE_WARPS>(ell_view<T, T>(*Q, 1, Q->at_ptr.p), VecSet<T, 1>{{vy.p}}, pe, s);
+                else launch_tiles<1>(pl, V, VecSet<T, 1>{{vy.p}}, pe, s);
             }
         });
-        items_A = tune_items<T>(h, hp2, (int32_t)m, n, nnz, items_A, pm1 ? 2 : 0,
-                                [&](TilePlan& pl, T* part) {
+        const SideChoice cA = tune_side<T>(h, *P, 0, hp2, items_A, try_csr, ell_A, pm1 ? 2 : 0,
+                                           [&](int fmt, TilePlan& pl, T* part) {
             if (pm1) {
                 const CsrView<Pm1, T> V{Q->a_ptr.p, Q->a_idx.p, nullptr, pl.tasks.p, pl.ntasks,
                                         pl.ltasks.p, pl.nltasks, pl.counters.p, part};
                 DualEpi<T, false, true> de{vy.p, Q->lc.p, Q->uc.p, vyn.p, vya.p, vya2.p, {cf.p}, 1,
                                            Q->d1t.p, vys.p};
-                launch_tiles<1>(pl, V, VecSet<T, 1>{{vxb.p}}, de, s);
+                if (fmt == CPDLP_FMT_ELL) launch_ell<TILE_WARPS>(ell_view<Pm1, T>(*Q, 0, Q->a_ptr.p), VecSet<T, 1>{{vxb.p}}, de, s);
+                else launch_tiles<1>(pl, V, VecSet<T, 1>{{vxb.p}}, de, s);
             } else {
                 const CsrView<T, T> V{Q->a_ptr.p, Q->a_idx.p, Q->a_val.p, pl.tasks.p, pl.ntasks,
                                       pl.ltasks.p, pl.nltasks, pl.counters.p, part};
                 DualEpi<T> de{vy.p, Q->lc.p, Q->uc.p, vyn.p, vya.p, vya2.p, {cf.p}, 1};
-                launch_tiles<1>(pl, V, VecSet<T, 1>{{vxb.p}}, de, s);
+                if (fmt == CPDLP_FMT_ELL) launch_ell<TILE_WARPS>(ell_view<T, T>(*Q, 0, Q->a_ptr.p), VecSet<T, 1>{{vxb.p}}, de, s);
+                else launch_tiles<1>(pl, V, VecSet<T, 1>{{vxb.p}}, de, s);
             }
         });
+        items_A = cA.items;
+        items_At = cAt.items;
     }
+    // the CSR plans (also kept for an ELL side: the tuner and the exports use them)
     build_tile_plan(hp2, (int32_t)m, items_A, P->planA, s);
     build_tile_plan(hp1, (int32_t)n, items_At, P->planAt, s);
     P->partA.alloc((size_t)(P->planA.npieces > 0 ? P->planA.npieces : 1) * 4);
     P->partAt.alloc((size_t)(P->planAt.npieces > 0 ? P->planAt.npieces : 1) * 4);
-    P->rows_A_partials = (int64_t)tiles_grid(P->planA) + P->planA.nlong;
-    P->rows_At_partials = (int64_t)tiles_grid(P->planAt) + P->planAt.nlong;
-    P->rows_A_kkt = (int64_t)tiles_grid(P->planA, kkt_warps<T>()) + P->planA.nlong;
-    P->rows_At_kkt = (int64_t)tiles_grid(P->planAt, kkt_warps<T>()) + P->planAt.nlong;
+    P->rows_A_partials = side_partials(*P, 0, TILE_WARPS);
+    P->rows_At_partials = side_partials(*P, 1, TILE_WARPS);
+    P->rows_A_kkt = side_partials(*P, 0, kkt_warps<T>());
+    P->rows_At_kkt = side_partials(*P, 1, kkt_warps<T>());
     int64_t rows_max = std::max<int64_t>(std::max(P->rows_A_partials, P->rows_At_partials),
                                          (int64_t)h.num_sms * 4 + 8);
     rows_max = std::max<int64_t>(rows_max, std::max(P->rows_A_kkt, P->rows_At_kkt));
@@ -762,16 +907,15 @@ double spectral_norm_T(Handle& h, ProblemT<V>& P, const cpdlp_params* prm, int64
         cudaGraph_t g = nullptr;
         CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         double* const blk = P.red_cols.p;
-        double* const lng = P.red_cols.p + (size_t)tiles_grid(P.planAt) * 2;
+        double* const lng = P.red_cols.p + (size_t)side_blocks(P, 1, TILE_WARPS) * 2;
         if (P.pm1) {
-            launch_tiles<1>(P.planA, A1, VecSet<double, 1>{{xs.p}},
-                            ScaledStoreEpi<double>{sv.p, P.D1.p}, s);
+            launch_side(P, 0, A1, VecSet<double, 1>{{xs.p}}, ScaledStoreEpi<double>{sv.p, P.D1.p}, s);
             PowerEpi<double, true> pe{x.p, Ax.p, blk, lng, P.D2.p};
-            launch_tiles<1>(P.planAt, At1, VecSet<double, 1>{{sv.p}}, pe, s);
+            launch_side(P, 1, At1, VecSet<double, 1>{{sv.p}}, pe, s);
         } else {
-            launch_tiles<1>(P.planA, A, VecSet<double, 1>{{x.p}}, StoreEpi<double>{sv.p}, s);
+            launch_side(P, 0, A, VecSet<double, 1>{{x.p}}, StoreEpi<double>{sv.p}, s);
             PowerEpi<double> pe{x.p, Ax.p, blk, lng};
-            launch_tiles<1>(P.planAt, At, VecSet<double, 1>{{sv.p}}, pe, s);
+            launch_side(P, 1, At, VecSet<double, 1>{{sv.p}}, pe, s);
         }
         reduce_partials(P.red_cols.p, P.rows_At_partials, 2, P.red_out.p, s);
         k_power_theta<<<1, 32, 0, s>>>(P.red_out.p, scal.p, d_it.p, dring, DEPTH);
@@ -865,10 +1009,10 @@ struct StateT : StateBase {
         if (P.pm1) {
             PrimalEpi<T, false, true> pe{xo, P.c.p, P.lv.p, P.uv.p, xn, xb, xao, xan, {c}, avg,
                                          P.d2t.p};
-            launch_tiles<1>(P.planAt, view_At_pm1(P), VecSet<T, 1>{{yg}}, pe, s);
+            launch_side(P, 1, view_At_pm1(P), VecSet<T, 1>{{yg}}, pe, s);
         } else {
             PrimalEpi<T> pe{xo, P.c.p, P.lv.p, P.uv.p, xn, xb, xao, xan, {c}, avg};
-            launch_tiles<1>(P.planAt, view_At(P), VecSet<T, 1>{{yg}}, pe, s);
+            launch_side(P, 1, view_At(P), VecSet<T, 1>{{yg}}, pe, s);
         }
     }
     // dual step: y+ from A xbar (narrow storage: also writes ysn = D1 y+)
@@ -879,17 +1023,17 @@ struct StateT : StateBase {
         if (P.pm1 && yoff) {
             DualEpi<T, false, true, true> de{yo, P.lc.p, P.uc.p, yn, yao, yan, {c}, avg,
                                              P.d1t.p, ysn, yoff};
-            launch_tiles<1>(P.planA, view_A_pm1(P), VecSet<T, 1>{{xg}}, de, s);
+            launch_side(P, 0, view_A_pm1(P), VecSet<T, 1>{{xg}}, de, s);
         } else if (P.pm1) {
             DualEpi<T, false, true> de{yo, P.lc.p, P.uc.p, yn, yao, yan, {c}, avg, P.d1t.p, ysn};
-            launch_tiles<1>(P.planA, view_A_pm1(P), VecSet<T, 1>{{xg}}, de, s);
+            launch_side(P, 0, view_A_pm1(P), VecSet<T, 1>{{xg}}, de, s);
         } else if (yoff) {
             DualEpi<T, false, false, true> de{yo, P.lc.p, P.uc.p, yn, yao, yan, {c}, avg,
                                               nullptr, nullptr, yoff};
-            launch_tiles<1>(P.planA, view_A(P), VecSet<T, 1>{{xg}}, de, s);
+            launch_side(P, 0, view_A(P), VecSet<T, 1>{{xg}}, de, s);
         } else {
             DualEpi<T> de{yo, P.lc.p, P.uc.p, yn, yao, yan, {c}, avg};
-            launch_tiles<1>(P.planA, view_A(P), VecSet<T, 1>{{xg}}, de, s);
+            launch_side(P, 0, view_A(P), VecSet<T, 1>{{xg}}, de, s);
         }
     }
 
@@ -1015,7 +1159,7 @@ struct StateT : StateBase {
         ProblemT<T>& P = *PT;
         cudaStream_t s = h->stream;
         constexpr int W = kkt_warps<T>();
-        const unsigned gA = tiles_grid(P.planA, W), gAt = tiles_grid(P.planAt, W);
+        const int64_t gA = side_blocks(P, 0, W), gAt = side_blocks(P, 1, W);
         KktRowEpi<T, NV, SC, W> re;
         re.lc = P.lc.p; re.uc = P.uc.p; re.invD1 = P.invD1_T();
         for (int p = 0; p < NV; p++) re.y[p] = ys[p];
@@ -1029,11 +1173,11 @@ struct StateT : StateBase {
         ce.long_out = ce.block_out + (size_t)gAt * 3 * NV;
         ce.dsc = SC ? P.d2t.p : nullptr;
         if constexpr (NV == 4) {
-            launch_tiles4<W>(P.planA, vA, gx, re, s);
-            launch_tiles4<W>(P.planAt, vAt, gy, ce, s);
+            launch_side4<W>(P, 0, vA, gx, re, s);
+            launch_side4<W>(P, 1, vAt, gy, ce, s);
         } else {
-            launch_tiles_w<W>(P.planA, vA, VecSet<T, 1>{{gx}}, re, s);
-            launch_tiles_w<W>(P.planAt, vAt, VecSet<T, 1>{{gy}}, ce, s);
+            launch_side<W>(P, 0, vA, VecSet<T, 1>{{gx}}, re, s);
+            launch_side<W>(P, 1, vAt, VecSet<T, 1>{{gy}}, ce, s);
         }
     }
 
@@ -1112,7 +1256,7 @@ struct StateT : StateBase {
             y[cur].p, yprev.p, P.lc.p, P.uc.p, ry.p, P.pm1 ? rys.p : nullptr, P.D1.p, m);
         CK_LAUNCH();
         keep();
-        const unsigned gA = tiles_grid(P.planA), gAt = tiles_grid(P.planAt);
+        const int64_t gA = side_blocks(P, 0, TILE_WARPS), gAt = side_blocks(P, 1, TILE_WARPS);
         double* const rblk = P.red_rows.p;
         double* const cblk = P.red_cols.p;
         if (P.pm1) {
@@ -1122,9 +1266,9 @@ struct StateT : StateBase {
             const CsrView<Pm1, double> At1{P.at_ptr.p, P.at_idx.p, nullptr, P.planAt.tasks.p,
                                            P.planAt.ntasks, P.planAt.ltasks.p, P.planAt.nltasks,
                                            P.planAt.counters.p, rpart_At.p};
-            launch_tiles<1>(P.planA, A1, VecSet<double, 1>{{rxs.p}},
+            launch_side(P, 0, A1, VecSet<double, 1>{{rxs.p}},
                             RayRowEpi<T, true>{P.lc.p, P.uc.p, ry.p, P.D1.p, rblk, rblk + (size_t)gA * 2}, s);
-            launch_tiles<1>(P.planAt, At1, VecSet<double, 1>{{rys.p}},
+            launch_side(P, 1, At1, VecSet<double, 1>{{rys.p}},
                             RayColEpi<T, true>{P.c.p, P.lv.p, P.uv.p, rx.p, P.D2.p, cblk,
                                                cblk + (size_t)gAt * 3}, s);
         } else {
@@ -1134,9 +1278,9 @@ struct StateT : StateBase {
             const CsrView<T, double> At{P.at_ptr.p, P.at_idx.p, P.at_val.p, P.planAt.tasks.p,
                                         P.planAt.ntasks, P.planAt.ltasks.p, P.planAt.nltasks,
                                         P.planAt.counters.p, rpart_At.p};
-            launch_tiles<1>(P.planA, A, VecSet<double, 1>{{rx.p}},
+            launch_side(P, 0, A, VecSet<double, 1>{{rx.p}},
                             RayRowEpi<T>{P.lc.p, P.uc.p, ry.p, nullptr, rblk, rblk + (size_t)gA * 2}, s);
-            launch_tiles<1>(P.planAt, At, VecSet<double, 1>{{ry.p}},
+            launch_side(P, 1, At, VecSet<double, 1>{{ry.p}},
                             RayColEpi<T>{P.c.p, P.lv.p, P.uv.p, rx.p, nullptr, cblk,
                                          cblk + (size_t)gAt * 3}, s);
         }
@@ -1640,8 +1784,8 @@ RefineResult refine_residual(Handle& h, ProblemT<float>& P32, ProblemT<double>& 
                      eg = e.gap / e.gap_scale;
         const double dp = pow2_scale(jl_max(ep, eg)), dd = pow2_scale(jl_max(ed, eg));
         // the round's residual LP, in P32's vectors
-        launch_tiles<1>(P64.planA, view_A(P64), VecSet<double, 1>{{x0.p}}, StoreEpi<double>{Ax0.p}, s);
-        launch_tiles<1>(P64.planAt, view_At(P64), VecSet<double, 1>{{y0.p}},
+        launch_side(P64, 0, view_A(P64), VecSet<double, 1>{{x0.p}}, StoreEpi<double>{Ax0.p}, s);
+        launch_side(P64, 1, view_At(P64), VecSet<double, 1>{{y0.p}},
                         StoreEpi<double>{Aty0.p}, s);
         if (m > 0)
             k_refine_rows<<<grid_for(m, 256), 256, 0, s>>>(P64.lc.p, P64.uc.p, Ax0.p, y0.p, dp, dd,

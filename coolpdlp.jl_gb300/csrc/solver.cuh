@@ -42,6 +42,12 @@ struct ProblemBase {
     int64_t m = 0, n = 0, nnz = 0;
     DBuf<int32_t> a_ptr, a_idx, at_ptr, at_idx;
     TilePlan planA, planAt;
+    // product format per matrix ([0]: rows of A, [1]: rows of A'): CSR tiles
+    // or ELL (ell_idx rows x width column-major, 0-based; the values in
+    // ProblemT::ell_val; the CSR row pointer gives the row lengths)
+    int32_t fmt[2] = {CPDLP_FMT_CSR, CPDLP_FMT_CSR};
+    int64_t ell_width[2] = {0, 0};
+    DBuf<int32_t> ell_idx[2];
     DBuf<double> D1, D2, invD1, invD2;
     double primal_scale = 0, dual_scale = 0;
     bool zero_cost = false;
@@ -57,6 +63,7 @@ struct ProblemBase {
 template <class T>
 struct ProblemT : ProblemBase {
     DBuf<T> a_val, at_val;
+    DBuf<T> ell_val[2];   // ELL values of a matrix whose fmt is CPDLP_FMT_ELL
     DBuf<T> c, lv, uv, lc, uc;
     DBuf<T> partA, partAt;   // long-row piece partials, NVEC = 4
     // narrow +-1 storage: the index arrays carry the signs of A (Pm1), the

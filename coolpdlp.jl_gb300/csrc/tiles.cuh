@@ -157,6 +157,17 @@ __device__ __forceinline__ double gather(const double* p) {
     else asm volatile("ld.global.nc.f64 %0, [%1];" : "=d"(v) : "l"(p));
     return v;
 }
+// four interleaved values p[0..3] (16-byte aligned) in one request (two for
+// FP64): the packed iterates of the KKT pass
+__device__ __forceinline__ void gather4(const float* p, float (&o)[4]) {
+    asm volatile("ld.global.nc.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(o[0]), "=f"(o[1]), "=f"(o[2]), "=f"(o[3])
+                 : "l"(p));
+}
+__device__ __forceinline__ void gather4(const double* p, double (&o)[4]) {
+    asm volatile("ld.global.nc.v2.f64 {%0, %1}, [%2];" : "=d"(o[0]), "=d"(o[1]) : "l"(p));
+    asm volatile("ld.global.nc.v2.f64 {%0, %1}, [%2];" : "=d"(o[2]), "=d"(o[3]) : "l"(p + 2));
+}
 // 16-byte asynchronous global -> shared copy (both addresses 16-byte aligned):
 // a gather that holds no registers while in flight
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {

@@ -65,8 +65,10 @@ enum { CPDLP_ALGO_PDLP = 0, CPDLP_ALGO_PDHG = 1 };
  * the signs of the column indices (no value array, FP32 vectors, CSR). */
 enum { CPDLP_VAL_F64 = 0, CPDLP_VAL_F32 = 1, CPDLP_VAL_PM1 = 2 };
 
-/* matrix_type: GPUSparseMatrixCSR / ELL / COO (src/utils/mat_*.jl) */
-enum { CPDLP_FMT_CSR = 0, CPDLP_FMT_ELL = 1, CPDLP_FMT_COO = 2 };
+/* matrix_type: GPUSparseMatrixCSR / ELL / COO (src/utils/mat_*.jl).
+ * CPDLP_FMT_AUTO (solver parameter only, EXT): the autotuner picks the
+ * product format of each matrix of the solve by timing. */
+enum { CPDLP_FMT_AUTO = -1, CPDLP_FMT_CSR = 0, CPDLP_FMT_ELL = 1, CPDLP_FMT_COO = 2 };
 
 /* which iterate to read back from a solver state (src/algorithms/pdlp.jl:20-43) */
 enum {
@@ -146,6 +148,19 @@ typedef struct cpdlp_params {
      * A x to the row bounds' recession cone is <= infeasibility_tol * |c'x|.
      * Both tests run in the scaled problem, where they are equivalent. */
     double infeasibility_tol;
+    /* matrix_type M of Algorithm{A}(T, Ti, M) (src/components/conversion.jl:
+     * 37-55, src/problems/modify.jl:80-105): the product format of the
+     * single-LP solve's matrices A and A'.  CPDLP_FMT_CSR: the CSR tile
+     * engine (tile shape autotuned for large matrices); CPDLP_FMT_ELL: the
+     * reference's ELL layout (column-major, width = the longest row), one
+     * thread per row, each row summed in column order; CPDLP_FMT_COO: solved
+     * on the CSR engine (the reference's COO product accumulates with atomics
+     * in a run-dependent order; CSR sums each row in COO's column order);
+     * CPDLP_FMT_AUTO (default, EXT): for matrices of at least 2^21 nonzeros
+     * the autotuner times CSR tile shapes and ELL (when its padding is at
+     * most 3x the nonzeros) and keeps the fastest per matrix, otherwise CSR.
+     * Batched solves and jobs use the CSR engine. */
+    int32_t matrix_type;
 } cpdlp_params;
 
 /* tile_flags bits.  By default a single-LP solve with FP32 iterates whose
@@ -345,6 +360,13 @@ int cpdlp_solve(cpdlp_handle* h, const cpdlp_lp* lp, const cpdlp_params* params,
  * 0 or the problem took the empty-problem early exit (common.jl:194-198). */
 int cpdlp_solve_history(const cpdlp_handle* h, int64_t* kkt_passes, cpdlp_kkt_errors* errs,
                         int64_t capacity, int64_t* count);
+
+/* The product layout the solve of this problem uses, per matrix ([0]: rows
+ * of A, the dual step; [1]: rows of A', the primal step): format
+ * (CPDLP_FMT_CSR or CPDLP_FMT_ELL), CSR tile size in nonzeros (0 for ELL)
+ * and ELL width (0 for CSR).  Any pointer may be NULL.  EXT (measurement). */
+int cpdlp_problem_layout(const cpdlp_problem* p, int32_t* format, int32_t* tile_nnz,
+                         int64_t* width);
 
 /* spectral_norm(A, A') (linalg.jl:86-96) of the problem's scaled matrix in its
  * float type, with the power-method settings of `params`. */
