@@ -167,7 +167,7 @@ EXPORTED_SYMBOLS = (
     "cpdlp_state_create", "cpdlp_state_destroy", "cpdlp_state_solve", "cpdlp_state_step",
     "cpdlp_state_kkt", "cpdlp_state_vectors", "cpdlp_state_solution", "cpdlp_state_stats",
     "cpdlp_state_history", "cpdlp_solve", "cpdlp_solve_history", "cpdlp_problem_spectral_norm",
-    "cpdlp_problem_layout",
+    "cpdlp_problem_layout", "cpdlp_reduced_costs",
     "cpdlp_batch_solve", "cpdlp_state_solve_blocks", "cpdlp_state_profile",
     "cpdlp_state_kernel_bytes", "cpdlp_spmv_csr_noalloc",
     "cpdlp_submit", "cpdlp_poll", "cpdlp_wait", "cpdlp_cancel", "cpdlp_collect",
@@ -212,6 +212,7 @@ def _declare(lib):
                                   POINTER(StatsC)]),
         "cpdlp_solve_history": (c_int32, [H, P64, POINTER(KKTErrorsC), c_int64, P64]),
         "cpdlp_problem_layout": (c_int32, [H, POINTER(c_int32), POINTER(c_int32), P64]),
+        "cpdlp_reduced_costs": (c_int32, [H, POINTER(LPC), PD, PD, PD]),
         "cpdlp_problem_spectral_norm": (c_int32, [H, H, POINTER(ParamsC), PD, P64]),
         "cpdlp_batch_solve": (c_int32, [H, c_int64, POINTER(LPC), POINTER(ParamsC),
                                         POINTER(PD), POINTER(PD), POINTER(StatsC)]),

@@ -30,6 +30,7 @@ import warnings
 import numpy as np
 
 from . import algorithms as alg
+from . import native
 from .problems import CSCMatrix, MILP
 
 
@@ -272,14 +273,11 @@ class Optimizer:
         self.model = model
         self.x = np.asarray(sol.x, dtype=np.float64)
         self.y = np.asarray(sol.y, dtype=np.float64)
-        At = milp.A.to_scipy().T.tocsr()
-        pm = np.vectorize(_proj_multiplier, otypes=[float])
-        self.z = pm(c - At @ self.y, milp.lv, milp.uv)
+        # z and the dual objective (moi.jl:215-227) on the device
+        lps = native.LPStruct(milp.A.m, milp.A.n, milp.A.colptr, milp.A.rowval, milp.A.nzval,
+                              c, milp.lv, milp.uv, milp.lc, milp.uc)
+        self.z, raw_dual = native.reduced_costs(native.default_handle(device), lps, self.y)
         raw_obj = float(np.dot(c, self.x))
-        raw_dual = (np.sum(_safeprod_left(milp.lc, np.maximum(self.y, 0.0)))
-                    - np.sum(_safeprod_left(milp.uc, np.maximum(-self.y, 0.0)))
-                    + np.sum(_safeprod_left(milp.lv, np.maximum(self.z, 0.0)))
-                    - np.sum(_safeprod_left(milp.uv, np.maximum(-self.z, 0.0))))
         mx = model.sense == Sense.MAX
         self.obj_value = (-raw_obj if mx else raw_obj) + model.obj_constant
         self.dual_obj_value = (-float(raw_dual) if mx else float(raw_dual)) + model.obj_constant

@@ -263,6 +263,17 @@ def solve_history(handle: Handle):
     return [(int(passes[i]), errs[i]) for i in range(k)]
 
 
+def reduced_costs(handle: Handle, lp: LPStruct, y):
+    """cpdlp_reduced_costs: (z, dual objective) of the solution y of the LP, on
+    the device (moi.jl:215-227)."""
+    z = np.empty(lp.s.n)
+    obj = c_double()
+    yy = f64(y)
+    handle.check(handle.lib.cpdlp_reduced_costs(handle.h, byref(lp.s), _pd(yy), _pd(z),
+                                                byref(obj)), "cpdlp_reduced_costs")
+    return z, obj.value
+
+
 def batch_solve(handle: Handle, lps: list, params: A.ParamsC):
     """cpdlp_batch_solve over LPStructs; returns lists of x, y and StatsC."""
     k = len(lps)

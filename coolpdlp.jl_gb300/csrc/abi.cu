@@ -5,6 +5,7 @@
 #include <new>
 
 #include "batch.cuh"
+#include "duals.cuh"
 #include "tiles.cuh"
 #include "matrix.cuh"
 #include "noalloc.cuh"
@@ -341,6 +342,12 @@ int cpdlp_state_history(const cpdlp_state* s, int64_t* kkt_passes, cpdlp_kkt_err
     }
     if (count) *count = len;
     return CPDLP_OK;
+}
+
+int cpdlp_reduced_costs(cpdlp_handle* h, const cpdlp_lp* lp, const double* y, double* z_out,
+                        double* dual_objective) {
+    NEED(h);
+    return guarded(h, [&] { reduced_costs(*H(h), lp, y, z_out, dual_objective); });
 }
 
 int cpdlp_problem_layout(const cpdlp_problem* p, int32_t* format, int32_t* tile_nnz,

@@ -368,6 +368,15 @@ int cpdlp_solve_history(const cpdlp_handle* h, int64_t* kkt_passes, cpdlp_kkt_er
 int cpdlp_problem_layout(const cpdlp_problem* p, int32_t* format, int32_t* tile_nnz,
                          int64_t* width);
 
+/* The reduced costs z = proj_multiplier.(c .- A'y, lv, uv) (n) and the dual
+ * objective sum safeprod_left(lc, y+) - sum safeprod_left(uc, y-)
+ * + sum safeprod_left(lv, z+) - sum safeprod_left(uv, z-) of a solution y
+ * (m, original units), as MOI.optimize! computes them after solve
+ * (src/moi.jl:215-227), in FP64 on the device from the LP's original data;
+ * (A'y)_j runs over column j of A in row order.  z_out may be NULL. */
+int cpdlp_reduced_costs(cpdlp_handle* h, const cpdlp_lp* lp, const double* y, double* z_out,
+                        double* dual_objective);
+
 /* spectral_norm(A, A') (linalg.jl:86-96) of the problem's scaled matrix in its
  * float type, with the power-method settings of `params`. */
 int cpdlp_problem_spectral_norm(cpdlp_handle* h, cpdlp_problem* p, const cpdlp_params* params,

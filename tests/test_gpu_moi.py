@@ -88,3 +88,26 @@ def test_maximisation_and_limits_against_highs(cuda_lib):
     opt.optimize(m)
     assert opt.termination_status == moi.TerminationStatusCode.ITERATION_LIMIT
     assert opt.get_primal_status() == moi.ResultStatusCode.UNKNOWN_RESULT_STATUS
+
+
+def test_reduced_costs_on_device_match_host_formula(handle):
+    """cpdlp_reduced_costs (z and the dual objective of moi.jl:215-227, FP64
+    on the device) against the same formulas evaluated on the host, for a
+    random LP with infinite bounds of every kind and a random y."""
+    from coolpdlp import generators as G
+    from coolpdlp import native
+    from coolpdlp.moi import _proj_multiplier, _safeprod_left
+    lp, _, _ = G.random_milp_and_sol(300, 500, 0.05, seed=9)
+    y = np.random.default_rng(3).standard_normal(lp.m)
+    L = native.LPStruct(lp.m, lp.n, lp.colptr, lp.rowval, lp.nzval, lp.c, lp.lv, lp.uv, lp.lc,
+                        lp.uc)
+    z, dual = native.reduced_costs(handle, L, y)
+    At = lp.to_scipy().T.tocsr()
+    z_ref = np.array([_proj_multiplier(g, l, u) for g, l, u in zip(lp.c - At @ y, lp.lv, lp.uv)])
+    dual_ref = (np.sum(_safeprod_left(lp.lc, np.maximum(y, 0.0)))
+                - np.sum(_safeprod_left(lp.uc, np.maximum(-y, 0.0)))
+                + np.sum(_safeprod_left(lp.lv, np.maximum(z_ref, 0.0)))
+                - np.sum(_safeprod_left(lp.uv, np.maximum(-z_ref, 0.0))))
+    scale = 1.0 + np.abs(lp.c) + np.abs(At) @ np.abs(y)
+    assert np.max(np.abs(z - z_ref) / scale) <= 1e-13
+    assert abs(dual - dual_ref) <= 1e-10 * (1.0 + abs(dual_ref))
