@@ -380,7 +380,7 @@ def measure_flow(h, side: int, K: int, blocks: int = 10, solves: bool = True) ->
         prof = S.profile(20)
         kb = S.kernel_bytes()
         out[name] = {
-            "iters_per_s": blocks * CHECK_EVERY / (ms * 1e-3),
+            "iters_per_s": blocks * CHECK_EVERY / (ms * 1e-3), "layout": P.layout(),
             "kernels": {nm: {"ms": float(prof[i]), "bytes": float(kb[i]),
                              "gbs": float(kb[i] / (prof[i] * 1e-3) / 1e9),
                              "frac": float(kb[i] / (prof[i] * 1e-3) / 1e9 / peak)}
@@ -628,6 +628,7 @@ def run_ours(args):
     P = native.Problem(h, L, prm)
     S = native.State(P, prm)
     setup_s = time.perf_counter() - t0
+    layout = P.layout()   # the autotuner's product format per matrix
     ext = torch.cuda.ExternalStream(h.stream, device=torch.device("cuda", local))
 
     for _ in range(args.warmup):
@@ -738,7 +739,7 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": workload_config(lp, args.scale),
-            "hbm_gbs": hbm_gbs_whole,
+            "hbm_gbs": hbm_gbs_whole, "layout": layout,
             "roofline": roofline, "kernels": kernels,
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h,
