@@ -1910,9 +1910,9 @@ RefineResult refine_residual(Handle& h, ProblemT<float>& P32, ProblemT<double>& 
         kkt_base(&e);
         if (trace_on())
             fprintf(stderr,
-                    "[cpdlp refine] round %d: rel %.3e (p %.2e d %.2e g %.2e) dp %.3g dd %.3g "
+                    "[cpdlp refine] %.2fs round %d: rel %.3e (p %.2e d %.2e g %.2e) dp %.3g dd %.3g "
                     "-> %.3e after %lld passes (%s, %lld restarts)\n",
-                    R.rounds, r0, ep, ed, eg, dp, dd, rel_err(e), (long long)S.kkt_passes, why,
+                    now_seconds() - t0, R.rounds, r0, ep, ed, eg, dp, dd, rel_err(e), (long long)S.kkt_passes, why,
                     (long long)S.outer);
         if (!(rel_err(e) <= 0.5 * r0)) {
             R.err = e;
@@ -2038,8 +2038,9 @@ void solve_full(Handle& h, const cpdlp_lp* lp, const cpdlp_params* params, const
         S->solve();
     }
     if (mixed && trace_on())
-        fprintf(stderr, "[cpdlp refine] FP32 phase: rel %.3e (best %.3e) after %lld passes%s\n",
-                rel_err(S->err), fp32_best, (long long)S->kkt_passes, stalled ? " (stalled)" : "");
+        fprintf(stderr, "[cpdlp refine] %.2fs FP32 phase: rel %.3e (best %.3e) after %lld passes%s\n",
+                now_seconds() - t0, rel_err(S->err), fp32_best, (long long)S->kkt_passes,
+                stalled ? " (stalled)" : "");
     // refinement: the FP32 iterates stalled before the tolerance
     const bool refine = mixed && stalled;
     keep_history(*S, 0);
@@ -2111,8 +2112,8 @@ void solve_full(Handle& h, const cpdlp_lp* lp, const cpdlp_params* params, const
     }
     // a round made no progress: continue in FP64 from the refined point
     if (trace_on())
-        fprintf(stderr, "[cpdlp refine] no progress after %d rounds: FP64 continuation\n",
-                R.rounds);
+        fprintf(stderr, "[cpdlp refine] %.2fs no progress after %d rounds: FP64 continuation\n",
+                now_seconds() - t0, R.rounds);
     std::vector<double> xs(nz), ys(mz);
     if (n > 0) k_unscale<double><<<grid_for(n, 256), 256, 0, h.stream>>>(bx.p, Q64.D2.p, T64.xr.p, n);
     if (m > 0) k_unscale<double><<<grid_for(m, 256), 256, 0, h.stream>>>(by.p, Q64.D1.p, T64.yr.p, m);
@@ -2152,8 +2153,8 @@ void solve_full(Handle& h, const cpdlp_lp* lp, const cpdlp_params* params, const
         stats->history_length = (int64_t)h.solve_hist_passes.size();
     }
     if (trace_on())
-        fprintf(stderr, "[cpdlp refine] FP64 continuation: rel %.3e after %lld passes%s\n",
-                rel_err(C64->err), (long long)C64->kkt_passes,
+        fprintf(stderr, "[cpdlp refine] %.2fs FP64 continuation: rel %.3e after %lld passes%s\n",
+                now_seconds() - t0, rel_err(C64->err), (long long)C64->kkt_passes,
                 keep_base ? " (worse than the refined point, which is returned)" : "");
 }
 
