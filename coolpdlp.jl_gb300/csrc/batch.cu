@@ -1222,13 +1222,16 @@ struct Job {
             next.max_passes = std::max<int64_t>(prm.max_kkt_passes - R.kkt_passes, 1);
             next.stall_passes = 0;
             next.time_limit = prm.time_limit - R.time_elapsed;
-            next.x0 = x[id].data();
-            next.y0 = y[id].data();
             // continuation: the FP64 run keeps the FP32 run's |A|^2 estimate (an FP64
-            // power method over the same values up to FP32 rounding) and, after a
-            // converged FP32 run, its primal weight
+            // power method over the same values up to FP32 rounding).  After a
+            // converged FP32 run it starts from the FP32 solution with its primal
+            // weight; after a stalled one it starts cold (a stalled FP32 iterate
+            // can be a poor start: one LP of the 4,096-LP workload ran out of
+            // 93,400 FP64 passes from it and needs 3,400 from zero)
+            next.x0 = refine ? x[id].data() : nullptr;
+            next.y0 = refine ? y[id].data() : nullptr;
             next.theta0 = R.theta;
-            next.omega0 = refine ? R.omega : 0.0;  // a stalled run's weight is not kept
+            next.omega0 = refine ? R.omega : 0.0;
             return true;
         }
         final_[id] = 1;

@@ -1872,8 +1872,8 @@ RefineResult refine_residual(Handle& h, ProblemT<float>& P32, ProblemT<double>& 
                                    sizeof(float) * mz, cudaMemcpyDeviceToDevice, s));
             }
             if (trace_level() > 1)
-                fprintf(stderr, "[cpdlp refine]   %lld: rel %.3e (p %.2e d %.2e g %.2e) omega %.3g\n",
-                        (long long)S.kkt_passes, rc, e_cur.primal / e_cur.primal_scale,
+                fprintf(stderr, "[cpdlp refine]   %.3fs %lld: rel %.3e (p %.2e d %.2e g %.2e) omega %.3g\n",
+                        now_seconds() - t0, (long long)S.kkt_passes, rc, e_cur.primal / e_cur.primal_scale,
                         e_cur.dual / e_cur.dual_scale, e_cur.gap / e_cur.gap_scale, S.omega);
             if (rc <= target) { why = "target"; break; }
             // a later round (the error already small) that has not improved at
@@ -2026,8 +2026,8 @@ void solve_full(Handle& h, const cpdlp_lp* lp, const cpdlp_params* params, const
                                    sizeof(float) * mz1, cudaMemcpyDeviceToDevice, h.stream));
             }
             if (trace_level() > 1)
-                fprintf(stderr, "[cpdlp refine]   FP32 %lld: rel %.3e (p %.2e d %.2e g %.2e)\n",
-                        (long long)S->kkt_passes, rel, e.primal / e.primal_scale,
+                fprintf(stderr, "[cpdlp refine]   %.3fs FP32 %lld: rel %.3e (p %.2e d %.2e g %.2e)\n",
+                        now_seconds() - t0, (long long)S->kkt_passes, rel, e.primal / e.primal_scale,
                         e.dual / e.dual_scale, e.gap / e.gap_scale);
             if (watch.stalled(rel, S->kkt_passes, win, FP32_STALL_LONG * win, FP32_STALL_REL)) {
                 stalled = true;
