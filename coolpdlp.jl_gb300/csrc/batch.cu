@@ -75,7 +75,12 @@ constexpr int CLUSTER_CTAS = 8;
 constexpr int64_t CLUSTER_MIN_NNZ = CPDLP_CLUSTER_MIN_NNZ;
 // In the FP64 phase (few LPs, the tail of a job) the threshold is lower: a
 // single CTA takes seconds on the slowest stalled LPs while most SMs are idle
-constexpr int64_t PHASE_CLUSTER_MIN_NNZ = 4000;
+// (a 3,792-nonzero LP needing 30,000 FP64 passes set the 4,096-LP batch's
+// makespan at 4,000)
+#ifndef CPDLP_PHASE_CLUSTER_MIN_NNZ
+#define CPDLP_PHASE_CLUSTER_MIN_NNZ 1000
+#endif
+constexpr int64_t PHASE_CLUSTER_MIN_NNZ = CPDLP_PHASE_CLUSTER_MIN_NNZ;
 // an LP's FP32 run stalls when its relative KKT error has not halved over this
 // many checks; it then continues in FP64
 #ifndef CPDLP_BATCH_STALL_CHECKS
