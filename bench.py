@@ -67,8 +67,10 @@ def parse_args():
                     help="Poisson arrival rates per second, comma separated")
     ap.add_argument("--c1-solves", type=int, default=1,
                     help="1: solve the large LP to 1e-4 and (refined) to 1e-8 in the line")
-    ap.add_argument("--c1-time-limit", type=float, default=150.0,
-                    help="time limit in seconds of each large-LP solve")
+    ap.add_argument("--c1-time-limit", type=float, default=120.0,
+                    help="time limit in seconds of the large-LP solve to 1e-4")
+    ap.add_argument("--c1-refine-time-limit", type=float, default=90.0,
+                    help="time limit in seconds of the large-LP solve to 1e-8")
     ap.add_argument("--batch-m-hi", type=int, default=5000,
                     help="largest m of the batched LPs (5000 = the named workload)")
     ap.add_argument("--flow-side", type=int, default=256,
@@ -756,7 +758,7 @@ def run_ours(args):
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(lp, c0=c0)
         if args.c1_solves:
-            line["c1"] = measure_c1_solves(h, lp, args.c1_time_limit, args.c1_time_limit)
+            line["c1"] = measure_c1_solves(h, lp, args.c1_time_limit, args.c1_refine_time_limit)
         if args.flow_side > 0:
             line["flow"] = measure_flow(h, args.flow_side, args.flow_k,
                                         solves=not args.flow_no_solve)

@@ -8,6 +8,7 @@ arrays read back 1-based, exactly as the Julia struct fields."""
 from __future__ import annotations
 
 import ctypes
+import sys
 from ctypes import byref, c_int64, c_void_p
 
 import numpy as np
@@ -77,6 +78,10 @@ class _GPUSparseMatrix:
             self.ptr = None
 
     def __del__(self):
+        # at interpreter exit the CUDA runtime may already be torn down:
+        # the process releases the device memory itself
+        if sys.is_finalizing():
+            return
         try:
             self.close()
         except Exception:

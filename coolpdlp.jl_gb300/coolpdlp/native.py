@@ -2,6 +2,7 @@
 from __future__ import annotations
 
 import ctypes
+import sys
 import threading
 from ctypes import POINTER, byref, c_double, c_int32, c_int64, c_void_p
 
@@ -52,6 +53,10 @@ class Handle:
             self.h = None
 
     def __del__(self):
+        # at interpreter exit the CUDA runtime may already be torn down:
+        # the process releases the device memory itself
+        if sys.is_finalizing():
+            return
         try:
             self.close()
         except Exception:
@@ -145,6 +150,10 @@ class Problem:
             self.p = None
 
     def __del__(self):
+        # at interpreter exit the CUDA runtime may already be torn down:
+        # the process releases the device memory itself
+        if sys.is_finalizing():
+            return
         try:
             self.close()
         except Exception:
@@ -232,6 +241,10 @@ class State:
             self.s = None
 
     def __del__(self):
+        # at interpreter exit the CUDA runtime may already be torn down:
+        # the process releases the device memory itself
+        if sys.is_finalizing():
+            return
         try:
             self.close()
         except Exception:
@@ -364,6 +377,10 @@ class Job:
             self.j = None
 
     def __del__(self):
+        # at interpreter exit the CUDA runtime may already be torn down:
+        # the process releases the device memory itself
+        if sys.is_finalizing():
+            return
         try:
             self.close()
         except Exception:

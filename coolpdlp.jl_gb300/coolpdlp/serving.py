@@ -68,7 +68,7 @@ class Server:
     def __init__(self, device: int = 0, float_type: int = A.VAL_F32, params: A.ParamsC = None,
                  hbm_budget: float = 150e9, max_inflight_lps: int | None = None,
                  max_job_lps: int = 1024, big_nnz: int = 40_000, max_ctas: int | None = None,
-                 single_workers: int = 16, fp32_reltol: float = 1e-4):
+                 single_workers: int = 32, fp32_reltol: float = 1e-4):
         self.handle = native.Handle(device)
         self.params = params if params is not None else native.default_params()
         self.params.float_type = float_type
