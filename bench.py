@@ -80,6 +80,9 @@ def parse_args():
                     help="flow section without the solves to 1e-4 / 1e-8")
     ap.add_argument("--only-flow", action="store_true",
                     help="run only the flow measurement (profiling); no headline value")
+    ap.add_argument("--only-serving-stream", type=int, default=0,
+                    help="run only a long served stream of this many requests at the first "
+                         "rate of --serve-rates (FP32+FP64-refined); no headline value")
     ap.add_argument("--only-batch", action="store_true",
                     help="run only the batched measurement (profiling small cases)")
     return ap.parse_args()
@@ -557,6 +560,61 @@ def measure_serving(requests: int, rates, err_sample: int = 12) -> dict:
     return out
 
 
+def measure_serving_stream(requests: int, rate: float, err_sample: int = 24,
+                           seq_sample: int = 40) -> dict:
+    """One long served stream (the full request count of the served workload)
+    at one Poisson rate, FP32+FP64-refined iterates, each LP built on arrival.
+    The x and y of an evenly spaced sample of requests are kept and checked
+    against the plain FP64 path to 1e-8; the plain FP64 path's one-at-a-time
+    throughput is timed on another evenly spaced sample."""
+    import numpy as np
+    from coolpdlp import _abi as A
+    from coolpdlp import generators as G
+    from coolpdlp import native
+    from coolpdlp import serving
+    reqs = G.served_stream(requests, 1.0, seed=7)
+    arrivals = [q.arrival / rate for q in reqs]
+    tols = [q.reltol for q in reqs]
+    pick = list(range(0, requests, max(1, requests // err_sample)))[:err_sample]
+    srv = serving.Server(float_type=A.VAL_F32, hbm_budget=150e9, keep=set(pick))
+    out = {"requests": requests, "rate_per_s": rate,
+           "workload": (f"{requests} Poisson arrivals at {rate:g}/s: 80% random sparse LPs "
+                        "m log-U[100,20000] n=2m 5 nnz/col, 20% grid multicommodity flows "
+                        "side U{32..128} K U{2..8}; tolerance 1e-4 or 1e-8; "
+                        "150 GB admission budget; LPs built on arrival")}
+    out["fp32_refined"] = serving.replay(srv, arrivals, lambda i: G.request_lp(reqs[i]), tols,
+                                         timeout=4 * 3600.0)
+    results = srv.results
+    srv.close()
+    notopt = [i for i in range(requests) if int(results[i].stats.termination_status) != 0]
+    out["not_optimal"] = [[i, reqs[i].kind, tols[i], int(results[i].stats.termination_status),
+                           int(results[i].stats.kkt_passes)] for i in notopt[:50]]
+    h = native.Handle(0)
+    seq_idx = list(range(0, requests, max(1, requests // seq_sample)))[:seq_sample]
+    t0 = time.perf_counter()
+    for i in seq_idx:
+        lp = G.request_lp(reqs[i])
+        p = native.default_params()
+        p.termination_reltol = tols[i]
+        native.solve_lp(h, native.LPStruct(lp.m, lp.n, lp.colptr, lp.rowval, lp.nzval, lp.c,
+                                           lp.lv, lp.uv, lp.lc, lp.uc), p)
+    seq = len(seq_idx) / (time.perf_counter() - t0)
+    out["fp64_sequential"] = {"lps_per_s": seq, "sample": len(seq_idx),
+                              "what": "cpdlp_solve one request at a time, LP building excluded"}
+    out["fp32_refined"]["throughput_vs_sequential"] = \
+        out["fp32_refined"]["throughput_lps_per_s"] / seq
+    errs = {"1e-4": [], "1e-8": []}
+    for i in pick:
+        lp = G.request_lp(reqs[i])
+        ref, _ = fp64_reference(h, lp)
+        errs["1e-8" if tols[i] < 1e-6 else "1e-4"].append(obj_err(float(lp.c @ results[i].x), ref))
+    out["err_vs_fp64"] = {
+        "reference": ("plain FP64 path (cpdlp_solve) to 1e-8 relative KKT; relative objective "
+                      f"error of {len(pick)} evenly spaced served results, by requested tolerance"),
+        **{k: err_summary(v) for k, v in errs.items() if v}}
+    return out
+
+
 def run_reference(args):
     ws, rank, local = dist_info()
     if rank != 0:
@@ -607,6 +665,13 @@ def run_ours(args):
             print(json.dumps({"metric": METRIC, "impl": "ours", "value": None,
                               "flow": measure_flow(h, args.flow_side, args.flow_k,
                                                    solves=not args.flow_no_solve)}), flush=True)
+        return
+    if args.only_serving_stream > 0:
+        if rank == 0:
+            rate = [float(r) for r in args.serve_rates.split(",") if r][0]
+            print(json.dumps({"metric": METRIC, "impl": "ours", "value": None,
+                              "serving_stream": measure_serving_stream(
+                                  args.only_serving_stream, rate)}), flush=True)
         return
     if args.only_batch:
         # the batched workload alone (small cases for profilers); no headline value

@@ -68,7 +68,11 @@ class Server:
     def __init__(self, device: int = 0, float_type: int = A.VAL_F32, params: A.ParamsC = None,
                  hbm_budget: float = 150e9, max_inflight_lps: int | None = None,
                  max_job_lps: int = 1024, big_nnz: int = 40_000, max_ctas: int | None = None,
-                 single_workers: int = 32, fp32_reltol: float = 1e-4):
+                 single_workers: int = 32, fp32_reltol: float = 1e-4, keep=None):
+        """keep: None keeps every result's x and y; otherwise a container of
+        the request ids whose x and y are kept (the others keep their
+        statistics only, which bounds host memory on long streams)."""
+        self.keep = keep
         self.handle = native.Handle(device)
         self.params = params if params is not None else native.default_params()
         self.params.float_type = float_type
@@ -141,6 +145,8 @@ class Server:
             for k, w in enumerate(reqs):
                 if ready[k] and w.rid not in self.results:
                     x, y, st = job.collect_lp(k)
+                    if not self._kept(w.rid):
+                        x = y = None
                     self.results[w.rid] = Result(w.rid, x, y, st, w.arrival, t_adm, t, "batch")
                     self.inflight_bytes -= w.nbytes
                     self.inflight_lps -= 1
@@ -156,12 +162,17 @@ class Server:
                 still.append((fut, w, t_adm))
                 continue
             x, y, st = fut.result()
+            if not self._kept(w.rid):
+                x = y = None
             self.results[w.rid] = Result(w.rid, x, y, st, w.arrival, t_adm, self.now(), "single")
             self.inflight_bytes -= w.nbytes
             self.inflight_lps -= 1
             finished += 1
         self.singles = still
         return finished
+
+    def _kept(self, rid: int) -> bool:
+        return self.keep is None or rid in self.keep
 
     def _fits(self, w: _Waiting) -> bool:
         return (self.inflight_lps < self.max_inflight
@@ -212,7 +223,11 @@ def replay(server: Server, arrivals, lps, reltols, poll_sleep: float = 2e-4,
            timeout: float = 3600.0) -> dict:
     """Replays a request stream in real time: request i is offered once the
     server clock reaches arrivals[i] (seconds); returns latency and
-    throughput figures.  lps[i] is the LP of request i."""
+    throughput figures, overall and by requested tolerance.  lps[i] is the LP
+    of request i, or lps is a callable that builds it on arrival (long
+    streams: the LPs are not all held in host memory; see Server.keep for
+    the solutions)."""
+    get = lps if callable(lps) else (lambda i: lps[i])
     order = np.argsort(np.asarray(arrivals), kind="stable")
     server.t0 = time.perf_counter()
     nxt = 0
@@ -221,7 +236,7 @@ def replay(server: Server, arrivals, lps, reltols, poll_sleep: float = 2e-4,
         now = server.now()
         while nxt < n and arrivals[order[nxt]] <= now:
             i = int(order[nxt])
-            server.offer(i, lps[i], reltols[i], arrival=float(arrivals[i]))
+            server.offer(i, get(i), reltols[i], arrival=float(arrivals[i]))
             nxt += 1
         server.pump()
         if nxt == n and server.idle():
@@ -233,6 +248,13 @@ def replay(server: Server, arrivals, lps, reltols, poll_sleep: float = 2e-4,
     finish = max(r.finished for r in server.results.values())
     status = np.bincount([int(server.results[i].stats.termination_status) for i in range(n)],
                          minlength=4)
+    tol = np.asarray(reltols, dtype=np.float64)[:n]
+    by_tol = {}
+    for t in sorted(set(tol.tolist())):
+        sel = tol == t
+        by_tol[f"{t:g}"] = {"requests": int(sel.sum()),
+                            "p50_ms": float(np.percentile(lat[sel], 50) * 1e3),
+                            "p99_ms": float(np.percentile(lat[sel], 99) * 1e3)}
     return {
         "requests": n,
         "p50_ms": float(np.percentile(lat, 50) * 1e3),
@@ -244,4 +266,5 @@ def replay(server: Server, arrivals, lps, reltols, poll_sleep: float = 2e-4,
         "jobs": server.jobs_submitted,
         "single_route": int(sum(1 for r in server.results.values() if r.route == "single")),
         "peak_admitted_bytes": int(server.peak_bytes),
+        "by_tolerance": by_tol,
     }
