@@ -587,9 +587,24 @@ def measure_serving_stream(requests: int, rate: float, err_sample: int = 24,
     results = srv.results
     srv.close()
     notopt = [i for i in range(requests) if int(results[i].stats.termination_status) != 0]
-    out["not_optimal"] = [[i, reqs[i].kind, tols[i], int(results[i].stats.termination_status),
-                           int(results[i].stats.kkt_passes)] for i in notopt[:50]]
+    out["not_optimal"] = {
+        "count": len(notopt),
+        "by_route": {rt: sum(1 for i in notopt if results[i].route == rt)
+                     for rt in ("batch", "single")},
+        "first": [[i, reqs[i].kind, reqs[i].m, tols[i], results[i].route,
+                   int(results[i].stats.termination_status), int(results[i].stats.kkt_passes)]
+                  for i in notopt[:20]]}
     h = native.Handle(0)
+    # the plain FP64 path (same pass limit) on the first few of them
+    same = []
+    for i in notopt[:6]:
+        lp = G.request_lp(reqs[i])
+        p = native.default_params()
+        p.termination_reltol = tols[i]
+        _, _, st = native.solve_lp(h, native.LPStruct(lp.m, lp.n, lp.colptr, lp.rowval, lp.nzval,
+                                                      lp.c, lp.lv, lp.uv, lp.lc, lp.uc), p)
+        same.append([i, int(st.termination_status), int(st.kkt_passes)])
+    out["not_optimal"]["plain_fp64_path"] = same
     seq_idx = list(range(0, requests, max(1, requests // seq_sample)))[:seq_sample]
     t0 = time.perf_counter()
     for i in seq_idx:

@@ -259,7 +259,7 @@ __device__ __forceinline__ void lp_tiles(const CsrView<V, T>& A, int t0, int t1,
     for (int t = t0 + gw; t < t1; t += BW * CS) {
         const int4 tk = A.tasks[t];
         short_tile<ITEMS, 1, V, T, Epi, true, BATCH_RPL, true>(A, xs, epi, acc, tk.x, tk.y, tk.z, tk.w,
-                                                       lane, prod + w * 32 * ITEMS);
+                                                       lane, prod + w * tile_buf<ITEMS>());
     }
 }
 
@@ -617,7 +617,7 @@ __device__ __forceinline__ void skip_one(const BatchArgs<T>& g, const BatchCtl& 
 // (BatchLP.power_rtol > 0).
 template <int ITEMS, class V, int CS>
 __global__ void __launch_bounds__(BT) k_batch_power(PowerArgs<V> g) {
-    __shared__ double prod[BW * 32 * ITEMS];
+    __shared__ __align__(16) double prod[BW * tile_buf<ITEMS>()];
     __shared__ double sh[BW * 8 + 8];
     __shared__ BatchLP L;
     __shared__ int s_lp;
@@ -700,7 +700,7 @@ __global__ void __launch_bounds__(BT) k_batch_power(PowerArgs<V> g) {
 // same LP.
 template <int ITEMS, class T, int CS>
 __global__ void __launch_bounds__(BT, batch_min_blocks<T>()) k_batch_pdlp(BatchArgs<T> g) {
-    __shared__ T prod[BW * 32 * ITEMS];
+    __shared__ __align__(16) T prod[BW * tile_buf<ITEMS>()];
     __shared__ double sh[BW * 8 + 8];
     __shared__ BatchCtl C;
     const int rank = Grp<CS>::rank();

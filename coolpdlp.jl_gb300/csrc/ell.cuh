@@ -75,10 +75,11 @@ __global__ void __launch_bounds__(WARPS * 32)
 template <int WARPS, class V, class T, class Epi>
 __global__ void __launch_bounds__(WARPS * 32)
     k_ell4(EllView<V, T> A, const T* __restrict__ x4, Epi epi) {
-    const int64_t r = (int64_t)blockIdx.x * (WARPS * 32) + threadIdx.x;
     typename Epi::Acc acc;
     epi.init(acc);
-    if (r < A.rows) {
+    // a capped grid (ell4_grid) strides over the rows
+    for (int64_t r = (int64_t)blockIdx.x * (WARPS * 32) + threadIdx.x; r < A.rows;
+         r += (int64_t)gridDim.x * (WARPS * 32)) {
         const int a = ld_keep(A.ptr + r);
         const int len = ld_keep(A.ptr + r + 1) - a;
         T s0 = T(0), s1 = T(0), s2 = T(0), s3 = T(0);
@@ -140,6 +141,11 @@ inline unsigned ell_grid(int64_t rows, int warps) {
     const int64_t g = (rows + warps * 32 - 1) / (warps * 32);
     return (unsigned)(g > 0 ? g : 1);
 }
+// the same for the four-iterate pass, at most max_blocks (0: no cap)
+inline unsigned ell4_grid(int64_t rows, int warps, int64_t max_blocks) {
+    const unsigned g = ell_grid(rows, warps);
+    return (max_blocks > 0 && g > max_blocks) ? (unsigned)max_blocks : g;
+}
 
 template <int WARPS, int NVEC, class V, class T, class Epi>
 void launch_ell(const EllView<V, T>& A, const VecSet<T, NVEC>& xs, const Epi& epi, cudaStream_t s) {
@@ -148,9 +154,10 @@ void launch_ell(const EllView<V, T>& A, const VecSet<T, NVEC>& xs, const Epi& ep
     CK_LAUNCH();
 }
 template <int WARPS, class V, class T, class Epi>
-void launch_ell4(const EllView<V, T>& A, const T* x4, const Epi& epi, cudaStream_t s) {
+void launch_ell4(const EllView<V, T>& A, const T* x4, const Epi& epi, int64_t max_blocks,
+                 cudaStream_t s) {
     if (A.rows == 0) return;
-    k_ell4<WARPS, V, T, Epi><<<ell_grid(A.rows, WARPS), WARPS * 32, 0, s>>>(A, x4, epi);
+    k_ell4<WARPS, V, T, Epi><<<ell4_grid(A.rows, WARPS, max_blocks), WARPS * 32, 0, s>>>(A, x4, epi);
     CK_LAUNCH();
 }
 

@@ -391,6 +391,19 @@ int64_t side_partials(const ProblemT<T>& P, int side, int warps) {
     const int64_t longs = P.fmt[side] == CPDLP_FMT_ELL ? 0 : (side == 0 ? P.planA : P.planAt).nlong;
     return side_blocks(P, side, warps) + longs;
 }
+// the same for the four-iterate pass (its grid capped at P.kkt4_cap blocks)
+template <class T>
+int64_t side_blocks4(const ProblemT<T>& P, int side, int warps) {
+    if (P.fmt[side] == CPDLP_FMT_ELL)
+        return side_rows(P, side) > 0 ? ell4_grid(side_rows(P, side), warps, P.kkt4_cap) : 0;
+    const TilePlan& pl = side == 0 ? P.planA : P.planAt;
+    return (pl.ntasks + pl.nltasks) > 0 ? tiles4_grid(pl, warps, P.kkt4_cap) : 0;
+}
+template <class T>
+int64_t side_partials4(const ProblemT<T>& P, int side, int warps) {
+    const int64_t longs = P.fmt[side] == CPDLP_FMT_ELL ? 0 : (side == 0 ? P.planA : P.planAt).nlong;
+    return side_blocks4(P, side, warps) + longs;
+}
 
 template <class V, class VT, class T>
 EllView<V, VT> ell_view(const ProblemT<T>& P, int side, const int32_t* ptr) {
@@ -415,9 +428,9 @@ template <int W, class V, class VT, class Epi, class T>
 void launch_side4(const ProblemT<T>& P, int side, const CsrView<V, VT>& view, const VT* x4,
                   const Epi& epi, cudaStream_t s) {
     if (P.fmt[side] == CPDLP_FMT_ELL)
-        launch_ell4<W>(ell_view<V, VT>(P, side, view.ptr), x4, epi, s);
+        launch_ell4<W>(ell_view<V, VT>(P, side, view.ptr), x4, epi, P.kkt4_cap, s);
     else
-        launch_tiles4<W>(side == 0 ? P.planA : P.planAt, view, x4, epi, s);
+        launch_tiles4<W>(side == 0 ? P.planA : P.planAt, view, x4, epi, P.kkt4_cap, s);
 }
 
 // the ELL slabs of a CSR (0-based; narrow storage keeps the signed index):
@@ -786,9 +799,13 @@ ProblemBase* make_problem(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm
     P->rows_At_partials = side_partials(*P, 1, TILE_WARPS);
     P->rows_A_kkt = side_partials(*P, 0, kkt_warps<T>());
     P->rows_At_kkt = side_partials(*P, 1, kkt_warps<T>());
+    P->kkt4_cap = (int64_t)h.num_sms * kkt_blocks_per_sm<T>();
+    P->rows_A_kkt4 = side_partials4(*P, 0, kkt_warps<T>());
+    P->rows_At_kkt4 = side_partials4(*P, 1, kkt_warps<T>());
     int64_t rows_max = std::max<int64_t>(std::max(P->rows_A_partials, P->rows_At_partials),
                                          (int64_t)h.num_sms * 4 + 8);
     rows_max = std::max<int64_t>(rows_max, std::max(P->rows_A_kkt, P->rows_At_kkt));
+    rows_max = std::max<int64_t>(rows_max, std::max(P->rows_A_kkt4, P->rows_At_kkt4));
     P->red_rows.alloc((size_t)rows_max * 12);
     P->red_cols.alloc((size_t)rows_max * 12);
     P->red_out.alloc(64);
@@ -1159,7 +1176,8 @@ struct StateT : StateBase {
         ProblemT<T>& P = *PT;
         cudaStream_t s = h->stream;
         constexpr int W = kkt_warps<T>();
-        const int64_t gA = side_blocks(P, 0, W), gAt = side_blocks(P, 1, W);
+        const int64_t gA = NV == 4 ? side_blocks4(P, 0, W) : side_blocks(P, 0, W);
+        const int64_t gAt = NV == 4 ? side_blocks4(P, 1, W) : side_blocks(P, 1, W);
         KktRowEpi<T, NV, SC, W> re;
         re.lc = P.lc.p; re.uc = P.uc.p; re.invD1 = P.invD1_T();
         for (int p = 0; p < NV; p++) re.y[p] = ys[p];
@@ -1190,8 +1208,10 @@ struct StateT : StateBase {
         ProblemT<T>& P = *PT;
         cudaStream_t s = h->stream;
         enqueue_kkt<NV>(xs, ys);
-        reduce_partials(P.red_rows.p, P.rows_A_kkt, 2 * NV, P.red_out.p, s);
-        reduce_partials(P.red_cols.p, P.rows_At_kkt, 3 * NV, P.red_out.p + 2 * NV, s);
+        reduce_partials(P.red_rows.p, NV == 4 ? P.rows_A_kkt4 : P.rows_A_kkt, 2 * NV,
+                        P.red_out.p, s);
+        reduce_partials(P.red_cols.p, NV == 4 ? P.rows_At_kkt4 : P.rows_At_kkt, 3 * NV,
+                        P.red_out.p + 2 * NV, s);
         launches += tiles_launches(P.planA) + tiles_launches(P.planAt) + 2;
         double* pin = h->pinned_area(sizeof(double) * 64);
         CK(cudaMemcpyAsync(pin, P.red_out.p, sizeof(double) * 5 * NV, cudaMemcpyDeviceToHost, s));

@@ -56,8 +56,10 @@ struct ProblemBase {
     // reduction scratch (FP64 block partials) sized for NVEC = 4
     DBuf<double> red_rows, red_cols, red_out;
     int64_t rows_A_partials = 0, rows_At_partials = 0;
-    // block-partial rows of the KKT pass (kkt_warps<T>() per block)
+    // block-partial rows of the KKT pass (kkt_warps<T>() per block): one
+    // iterate, and four packed iterates (grid capped at kkt4_cap blocks)
     int64_t rows_A_kkt = 0, rows_At_kkt = 0;
+    int64_t kkt4_cap = 0, rows_A_kkt4 = 0, rows_At_kkt4 = 0;
 };
 
 template <class T>

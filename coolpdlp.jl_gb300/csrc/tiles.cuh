@@ -177,6 +177,15 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
 __device__ __forceinline__ void cp_async_wait_all() {
     asm volatile("cp.async.wait_all;" ::: "memory");
 }
+// four values to 16-byte-aligned shared memory (one vector store for FP32,
+// two for FP64)
+__device__ __forceinline__ void store4_shared(float* p, const float (&v)[4]) {
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void store4_shared(double* p, const double (&v)[4]) {
+    reinterpret_cast<double2*>(p)[0] = make_double2(v[0], v[1]);
+    reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
+}
 template <class V, class T>
 __device__ __forceinline__ T load1v(const V* p) {
     return (T)__ldcs(p);
@@ -197,11 +206,21 @@ __device__ __forceinline__ uint64_t global_ns() {
 }
 
 constexpr int TILE_WARPS = 8;
+// elements of a warp's short-tile product buffer (16-byte aligned): the tile's
+// nonzeros from the 4-element-aligned window start, plus the window's slack
+template <int ITEMS>
+constexpr int tile_buf() { return 32 * ITEMS + 4; }
 // Warps per block of the KKT pass: the four iterates' gathered values of a
 // whole tile live in shared memory, within the static 48 KB (4 warps for FP32
 // iterates, 2 for FP64).
 template <class T>
 constexpr int kkt_warps() { return sizeof(T) == 4 ? 4 : 2; }
+// Resident blocks per SM of the four-iterate KKT pass, which caps its grid at
+// SMs x this (the kernel loops over its tasks): 4 x 4 warps for FP32 (up to
+// 109 registers a thread), 6 x 2 warps for FP64 (33 KB of shared memory a
+// block).
+template <class T>
+constexpr int kkt_blocks_per_sm() { return sizeof(T) == 4 ? 4 : 6; }
 
 // One warp, one short tile.  All loads of a phase are volatile PTX issued back
 // to back, so they are in flight together: (1) the tile's indices and values
@@ -258,16 +277,37 @@ __device__ __forceinline__ void short_tile(const CsrView<V, T>& A, const VecSet<
                                ? gather<COH>(xv + (is_pm1<V>::value ? pm1_col(cc[j][q]) : cc[j][q]))
                                : T(0);
         }
+        // products to shared memory, indexed from the aligned window start.
+        // FP32 tiles with medium rows store a chunk's four products with one
+        // 16-byte store (fewer shared-store wavefronts; the entries outside
+        // the tile are never read); the other kernels store the tile's
+        // entries one by one, which keeps them at fewer registers (measured
+        // on C1: the vector store took the primal step from 64 to 72
+        // registers and 0.124 to 0.130 ms, and the dual step from 0.120 to
+        // 0.111 ms)
+        constexpr bool VEC_STORE = MED && sizeof(T) == 4;
 #pragma unroll
         for (int j = 0; j < NV4; j++) {
             const int e = base + 4 * (lane + 32 * j);
+            if constexpr (VEC_STORE) {
+                if (e < nz1) {
+                    T pr[4];
 #pragma unroll
-            for (int q = 0; q < 4; q++)
-                if (e + q >= nz0 && e + q < nz1)
-                    prod[e + q - nz0] = is_pm1<V>::value ? pm1_apply(cc[j][q], xg[j][q])
-                                                         : mul_rn(vv[j][q], xg[j][q]);
+                    for (int q = 0; q < 4; q++)
+                        pr[q] = is_pm1<V>::value ? pm1_apply(cc[j][q], xg[j][q])
+                                                 : mul_rn(vv[j][q], xg[j][q]);
+                    store4_shared(prod + (e - base), pr);
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    if (e + q >= nz0 && e + q < nz1)
+                        prod[e + q - base] = is_pm1<V>::value ? pm1_apply(cc[j][q], xg[j][q])
+                                                              : mul_rn(vv[j][q], xg[j][q]);
+            }
         }
         __syncwarp();
+        const T* prow = prod + (nz0 - base);  // prow[i - nz0]: nonzero i of the tile
 #pragma unroll
         for (int k = 0; k < RPL; k++) {
             const int r = r0 + lane + 32 * k;
@@ -283,14 +323,14 @@ __device__ __forceinline__ void short_tile(const CsrView<V, T>& A, const VecSet<
                     const int a = __shfl_sync(FULL_MASK, ra[k], l) - nz0;
                     const int b = __shfl_sync(FULL_MASK, rb[k], l) - nz0;
                     T part = T(0);
-                    for (int i = a + lane; i < b; i += 32) part = add_rn(part, prod[i]);
+                    for (int i = a + lane; i < b; i += 32) part = add_rn(part, prow[i]);
                     part = warp_sum_tree(part);
                     if (lane == l) sum = part;
                 }
             }
             if (r < r1) {
                 if (len <= LONG_ROW)
-                    for (int i = ra[k] - nz0; i < rb[k] - nz0; i++) sum = add_rn(sum, prod[i]);
+                    for (int i = ra[k] - nz0; i < rb[k] - nz0; i++) sum = add_rn(sum, prow[i]);
                 epi.row(p, r, sum, pre[k], acc);
             }
         }
@@ -371,7 +411,7 @@ __device__ __forceinline__ void long_piece(const CsrView<V, T>& A, const VecSet<
 template <int ITEMS, int WARPS, int NVEC, class V, class T, class Epi, int RPL, bool MED>
 __global__ void __launch_bounds__(WARPS * 32, sizeof(T) == 8 ? CPDLP_F64_MIN_BLOCKS : 1)
     k_tiles(CsrView<V, T> A, VecSet<T, NVEC> xs, Epi epi) {
-    __shared__ T prod[WARPS][32 * ITEMS];
+    __shared__ __align__(16) T prod[WARPS][tile_buf<ITEMS>()];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int task = blockIdx.x * WARPS + w;
     typename Epi::Acc acc;
@@ -639,24 +679,40 @@ __global__ void __launch_bounds__(WARPS * 32)
     k_tiles4(CsrView<V, T> A, const T* __restrict__ x4, Epi epi) {
     __shared__ __align__(16) T prod[WARPS][4 * 32 * ITEMS];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int task = blockIdx.x * WARPS + w;
     typename Epi::Acc acc;
     epi.init(acc);
-    if (task < A.nltasks) {
-        long_piece4<ITEMS>(A, x4, epi, acc, A.ltasks[task], lane, prod[w]);
-    } else if (task - A.nltasks < A.ntasks) {
-        const int4 t = A.tasks[task - A.nltasks];
-        short_tile4<ITEMS, V, T, Epi, RPL, MED>(A, x4, epi, acc, t.x, t.y, t.z, t.w, lane, prod[w]);
+    // the grid may be capped (tiles4_grid): each warp then takes every
+    // (gridDim.x * WARPS)-th task, in a fixed order, and a block's FP64 sums
+    // are reduced once for all its tasks (the block reduction's FP64 shuffles
+    // cost as much as the per-row terms when every block has one task each)
+    const int total = A.nltasks + A.ntasks;
+    for (int task = blockIdx.x * WARPS + w; task < total; task += gridDim.x * WARPS) {
+        if (task < A.nltasks) {
+            long_piece4<ITEMS>(A, x4, epi, acc, A.ltasks[task], lane, prod[w]);
+        } else {
+            const int4 t = A.tasks[task - A.nltasks];
+            short_tile4<ITEMS, V, T, Epi, RPL, MED>(A, x4, epi, acc, t.x, t.y, t.z, t.w, lane,
+                                                    prod[w]);
+        }
+        __syncwarp();
     }
     epi.finish(acc);
 }
 
+// blocks of a four-iterate pass: one task per warp, at most max_blocks (0: no
+// cap); the block-partial rows of its reducing epilogue
+inline unsigned tiles4_grid(const TilePlan& plan, int warps, int64_t max_blocks) {
+    int64_t g = ((int64_t)plan.ntasks + plan.nltasks + warps - 1) / warps;
+    if (max_blocks > 0 && g > max_blocks) g = max_blocks;
+    return (unsigned)g;
+}
+
 template <int WARPS, class V, class T, class Epi>
 void launch_tiles4(const TilePlan& plan, const CsrView<V, T>& view, const T* x4, const Epi& epi,
-                   cudaStream_t s) {
+                   int64_t max_blocks, cudaStream_t s) {
     const int64_t tasks = (int64_t)plan.ntasks + plan.nltasks;
     if (tasks == 0) return;
-    const unsigned grid = (unsigned)((tasks + WARPS - 1) / WARPS);
+    const unsigned grid = tiles4_grid(plan, WARPS, max_blocks);
 #define CPDLP_TILES4(IT, R, M) k_tiles4<IT, WARPS, V, T, Epi, R, M><<<grid, WARPS * 32, 0, s>>>(view, x4, epi)
     if (plan.medium) {
         if (plan.rpl != 2) fail(CPDLP_ERR_ARGUMENT, "tile plan with long rows needs 64-row tiles");
