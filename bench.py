@@ -80,6 +80,10 @@ def parse_args():
                     help="flow section without the solves to 1e-4 / 1e-8")
     ap.add_argument("--only-flow", action="store_true",
                     help="run only the flow measurement (profiling); no headline value")
+    ap.add_argument("--matrix-type", choices=["auto", "csr", "ell"], default="auto",
+                    help="product format of the large LP (profiling; auto = the autotuner)")
+    ap.add_argument("--tile-nnz", type=int, default=0,
+                    help="CSR tile size of the large LP (profiling; 0 = autotuned)")
     ap.add_argument("--only-serving-stream", type=int, default=0,
                     help="run only a long served stream of this many requests at the first "
                          "rate of --serve-rates (FP32+FP64-refined); no headline value")
@@ -704,6 +708,8 @@ def run_ours(args):
     prm.termination_reltol = 0.0
     prm.max_kkt_passes = 1 << 60
     prm.time_limit = 1e30
+    prm.matrix_type = {"auto": A.FMT_AUTO, "csr": A.FMT_CSR, "ell": A.FMT_ELL}[args.matrix_type]
+    prm.tile_nnz = args.tile_nnz
     L = native.LPStruct(lp.m, lp.n, lp.colptr, lp.rowval, lp.nzval, lp.c, lp.lv, lp.uv, lp.lc,
                         lp.uc)
     t0 = time.perf_counter()
@@ -711,6 +717,7 @@ def run_ours(args):
     S = native.State(P, prm)
     setup_s = time.perf_counter() - t0
     layout = P.layout()   # the autotuner's product format per matrix
+    layout["density_order"] = P.order() is not None
     ext = torch.cuda.ExternalStream(h.stream, device=torch.device("cuda", local))
 
     for _ in range(args.warmup):

@@ -32,8 +32,11 @@ OPTIMAL, TIME_LIMIT, ITERATION_LIMIT, STILL_RUNNING = 0, 1, 2, 3
 PRIMAL_INFEASIBLE, DUAL_INFEASIBLE = 4, 5
 ALGO_PDLP, ALGO_PDHG = 0, 1
 VAL_F64, VAL_F32, VAL_PM1 = 0, 1, 2
-# tile_flags bits: CPDLP_TILE_NO_NARROW keeps scaled values for a +-1 matrix
+# tile_flags bits: CPDLP_TILE_NO_NARROW keeps scaled values for a +-1 matrix;
+# CPDLP_TILE_DENSITY_ORDER / _NO_DENSITY_ORDER force the density order on / off
 TILE_NO_NARROW = 1
+TILE_DENSITY_ORDER = 2
+TILE_NO_DENSITY_ORDER = 4
 FMT_AUTO, FMT_CSR, FMT_ELL, FMT_COO = -1, 0, 1, 2
 VEC_SOL, VEC_SOL_LAST, VEC_SOL_AVG, VEC_SOL_AVG_LAST, VEC_SOL_RESTART = 0, 1, 2, 3, 4
 
@@ -167,7 +170,7 @@ EXPORTED_SYMBOLS = (
     "cpdlp_state_create", "cpdlp_state_destroy", "cpdlp_state_solve", "cpdlp_state_step",
     "cpdlp_state_kkt", "cpdlp_state_vectors", "cpdlp_state_solution", "cpdlp_state_stats",
     "cpdlp_state_history", "cpdlp_solve", "cpdlp_solve_history", "cpdlp_problem_spectral_norm",
-    "cpdlp_problem_layout", "cpdlp_reduced_costs",
+    "cpdlp_problem_layout", "cpdlp_problem_order", "cpdlp_reduced_costs",
     "cpdlp_batch_solve", "cpdlp_state_solve_blocks", "cpdlp_state_profile",
     "cpdlp_state_kernel_bytes", "cpdlp_spmv_csr_noalloc",
     "cpdlp_submit", "cpdlp_poll", "cpdlp_wait", "cpdlp_cancel", "cpdlp_collect",
@@ -212,6 +215,7 @@ def _declare(lib):
                                   POINTER(StatsC)]),
         "cpdlp_solve_history": (c_int32, [H, P64, POINTER(KKTErrorsC), c_int64, P64]),
         "cpdlp_problem_layout": (c_int32, [H, POINTER(c_int32), POINTER(c_int32), P64]),
+        "cpdlp_problem_order": (c_int32, [H, H, POINTER(c_int32), P64, P64]),
         "cpdlp_reduced_costs": (c_int32, [H, POINTER(LPC), PD, PD, PD]),
         "cpdlp_problem_spectral_norm": (c_int32, [H, H, POINTER(ParamsC), PD, P64]),
         "cpdlp_batch_solve": (c_int32, [H, c_int64, POINTER(LPC), POINTER(ParamsC),

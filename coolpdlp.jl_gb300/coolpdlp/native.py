@@ -130,6 +130,20 @@ class Problem:
         return {side: {"format": names.get(fmt[k], str(fmt[k])), "tile_nnz": int(tile[k]),
                        "ell_width": int(width[k])} for k, side in enumerate(("A", "At"))}
 
+    def order(self):
+        """cpdlp_problem_order: None when the solve runs in the caller's order,
+        else the 0-based (order_row, order_col) of the density order
+        (internal row i is the caller's row order_row[i])."""
+        flag = c_int32(0)
+        orow = np.empty(max(self.m, 1), dtype=np.int64)
+        ocol = np.empty(max(self.n, 1), dtype=np.int64)
+        self.handle.check(self.handle.lib.cpdlp_problem_order(self.handle.h, self.p, byref(flag),
+                                                              _p64(orow), _p64(ocol)),
+                          "cpdlp_problem_order")
+        if not flag.value:
+            return None
+        return orow[:self.m] - 1, ocol[:self.n] - 1
+
     def scaling(self):
         d1 = np.empty(self.m)
         d2 = np.empty(self.n)

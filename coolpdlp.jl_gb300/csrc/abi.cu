@@ -3,6 +3,7 @@
 // the message in the handle.
 #include <memory>
 #include <new>
+#include <vector>
 
 #include "batch.cuh"
 #include "duals.cuh"
@@ -361,6 +362,27 @@ int cpdlp_problem_layout(const cpdlp_problem* p, int32_t* format, int32_t* tile_
         if (width) width[sd] = ell ? P->ell_width[sd] : 0;
     }
     return CPDLP_OK;
+}
+
+int cpdlp_problem_order(cpdlp_handle* h, const cpdlp_problem* p, int32_t* ordered,
+                        int64_t* order_row, int64_t* order_col) {
+    NEED(h);
+    if (!p) return CPDLP_ERR_ARGUMENT;
+    const ProblemBase* P = reinterpret_cast<const ProblemBase*>(p);
+    if (ordered) *ordered = P->ordered ? 1 : 0;
+    if (!P->ordered) return CPDLP_OK;
+    return guarded(h, [&] {
+        for (int sd = 0; sd < 2; sd++) {
+            int64_t* out = sd == 0 ? order_row : order_col;
+            const int64_t len = sd == 0 ? P->m : P->n;
+            if (!out || len <= 0) continue;
+            std::vector<int32_t> o((size_t)len);
+            CK(cudaMemcpyAsync(o.data(), (sd == 0 ? P->order_row : P->order_col).p,
+                               sizeof(int32_t) * len, cudaMemcpyDeviceToHost, H(h)->stream));
+            CK(cudaStreamSynchronize(H(h)->stream));
+            for (int64_t k = 0; k < len; k++) out[k] = (int64_t)o[(size_t)k] + 1;
+        }
+    });
 }
 
 int cpdlp_solve_history(const cpdlp_handle* h, int64_t* kkt_passes, cpdlp_kkt_errors* errs,

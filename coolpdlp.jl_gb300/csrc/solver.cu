@@ -569,6 +569,144 @@ void fetch_reduced(Handle& h, const double* part, int64_t rows, int q, double* d
 }
 
 // ---------------------------------------------------------------------------
+// density order: the order of the reference's sort_rows_columns
+// (permutation.jl:1-46) -- rows and columns by increasing length, ties in
+// index order (Julia's stable sortperm) -- applied inside the solver
+// ---------------------------------------------------------------------------
+// the rows of a CSR (row pointer hp) by increasing length: a counting sort
+std::vector<int32_t> order_by_length(const std::vector<int32_t>& hp, int64_t rows) {
+    int32_t maxlen = 0;
+    for (int64_t r = 0; r < rows; r++) maxlen = std::max(maxlen, hp[r + 1] - hp[r]);
+    std::vector<int64_t> next((size_t)maxlen + 2, 0);
+    for (int64_t r = 0; r < rows; r++) next[(size_t)(hp[r + 1] - hp[r]) + 1]++;
+    for (size_t l = 1; l < next.size(); l++) next[l] += next[l - 1];
+    std::vector<int32_t> order((size_t)rows);
+    for (int64_t r = 0; r < rows; r++) order[(size_t)next[(size_t)(hp[r + 1] - hp[r])]++] = (int32_t)r;
+    return order;
+}
+
+// A problem's matrices in density order (internal row i = row orow[i] of A,
+// internal column j = column ocol[j]), built next to the problem's own
+template <class T>
+struct DensityOrder {
+    std::vector<int32_t> hp2, hp1;   // row pointers of A and A' in the new order
+    DBuf<int32_t> orow, ocol;        // new -> old
+    DBuf<int32_t> a_ptr, a_idx, at_ptr, at_idx;
+    DBuf<T> a_val, at_val;
+};
+
+template <class T>
+void build_density_order(Handle& h, const ProblemT<T>& P, const std::vector<int32_t>& hp2,
+                         const std::vector<int32_t>& hp1, DensityOrder<T>& o) {
+    cudaStream_t s = h.stream;
+    const int64_t m = P.m, n = P.n, nnz = P.nnz;
+    const size_t mz = (size_t)std::max<int64_t>(m, 1), nz = (size_t)std::max<int64_t>(n, 1),
+                 zn = (size_t)std::max<int64_t>(nnz, 1);
+    const std::vector<int32_t> orow = order_by_length(hp2, m), ocol = order_by_length(hp1, n);
+    std::vector<int32_t> irow((size_t)m), icol((size_t)n);
+    for (int64_t k = 0; k < m; k++) irow[(size_t)orow[(size_t)k]] = (int32_t)k;
+    for (int64_t k = 0; k < n; k++) icol[(size_t)ocol[(size_t)k]] = (int32_t)k;
+    DBuf<int32_t> dirow(mz), dicol(nz);
+    o.orow.alloc(mz);
+    o.ocol.alloc(nz);
+    if (m > 0) {
+        CK(cudaMemcpyAsync(o.orow.p, orow.data(), sizeof(int32_t) * m, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dirow.p, irow.data(), sizeof(int32_t) * m, cudaMemcpyHostToDevice, s));
+    }
+    if (n > 0) {
+        CK(cudaMemcpyAsync(o.ocol.p, ocol.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dicol.p, icol.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, s));
+    }
+    o.a_ptr.alloc((size_t)m + 1);
+    o.at_ptr.alloc((size_t)n + 1);
+    // index arrays carry the tile engine's 16 padding elements, value arrays PAD_ELEMS
+    o.a_idx.alloc(zn + 16);
+    o.at_idx.alloc(zn + 16);
+    CK(cudaMemsetAsync(o.a_idx.p, 0, sizeof(int32_t) * (zn + 16), s));
+    CK(cudaMemsetAsync(o.at_idx.p, 0, sizeof(int32_t) * (zn + 16), s));
+    if (!P.pm1) {
+        o.a_val.alloc(zn + PAD_ELEMS);
+        o.at_val.alloc(zn + PAD_ELEMS);
+        CK(cudaMemsetAsync(o.a_val.p, 0, sizeof(T) * (zn + PAD_ELEMS), s));
+        CK(cudaMemsetAsync(o.at_val.p, 0, sizeof(T) * (zn + PAD_ELEMS), s));
+    }
+    reorder_csr<T>(P.a_ptr.p, P.a_idx.p, P.pm1 ? nullptr : P.a_val.p, m, nnz, o.orow.p, dicol.p,
+                   o.a_ptr.p, o.a_idx.p, P.pm1 ? nullptr : o.a_val.p, s);
+    reorder_csr<T>(P.at_ptr.p, P.at_idx.p, P.pm1 ? nullptr : P.at_val.p, n, nnz, o.ocol.p, dirow.p,
+                   o.at_ptr.p, o.at_idx.p, P.pm1 ? nullptr : o.at_val.p, s);
+    o.hp2.assign((size_t)m + 1, 0);
+    o.hp1.assign((size_t)n + 1, 0);
+    CK(cudaMemcpyAsync(o.hp2.data(), o.a_ptr.p, sizeof(int32_t) * (m + 1), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(o.hp1.data(), o.at_ptr.p, sizeof(int32_t) * (n + 1), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+}
+
+// exchanges the problem's matrices with the reordered ones
+template <class T>
+void swap_matrices(ProblemT<T>& P, DensityOrder<T>& o) {
+    std::swap(P.a_ptr, o.a_ptr);
+    std::swap(P.a_idx, o.a_idx);
+    std::swap(P.at_ptr, o.at_ptr);
+    std::swap(P.at_idx, o.at_idx);
+    std::swap(P.a_val, o.a_val);
+    std::swap(P.at_val, o.at_val);
+}
+
+// makes the reordered matrices (already swapped in) the problem's: its
+// vectors follow the new order and it keeps the orders for the ABI boundary
+template <class T>
+void adopt_density_order(Handle& h, ProblemT<T>& P, DensityOrder<T>& o) {
+    cudaStream_t s = h.stream;
+    auto reorder = [&](auto& v, const int32_t* ord, int64_t len) {
+        using E = typename std::remove_reference<decltype(*v.p)>::type;
+        if (!v.p || len <= 0) return;
+        std::remove_reference_t<decltype(v)> t(v.n);
+        gather_values<E, E>(v.p, ord, t.p, len, s);
+        std::swap(v, t);
+        CK(cudaStreamSynchronize(s));
+    };
+    for (DBuf<T>* v : {&P.c, &P.lv, &P.uv, &P.d2t, &P.invD2t}) reorder(*v, o.ocol.p, P.n);
+    for (DBuf<T>* v : {&P.lc, &P.uc, &P.d1t, &P.invD1t}) reorder(*v, o.orow.p, P.m);
+    for (DBuf<double>* v : {&P.D2, &P.invD2}) reorder(*v, o.ocol.p, P.n);
+    for (DBuf<double>* v : {&P.D1, &P.invD1}) reorder(*v, o.orow.p, P.m);
+    P.order_row = std::move(o.orow);
+    P.order_col = std::move(o.ocol);
+    P.ordered = true;
+}
+
+__global__ void k_scatter_order(const double* __restrict__ in, const int32_t* __restrict__ order,
+                                double* __restrict__ out, int64_t n) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) out[order[k]] = in[k];
+}
+
+}  // namespace
+
+// a device vector over P's rows (side 0) or columns (side 1), from the
+// caller's order into the solver's, in place
+void order_to_internal(const ProblemBase& P, int side, double* v, cudaStream_t s) {
+    const int64_t len = side == 0 ? P.m : P.n;
+    if (!P.ordered || len <= 0) return;
+    DBuf<double> t((size_t)len);
+    CK(cudaMemcpyAsync(t.p, v, sizeof(double) * len, cudaMemcpyDeviceToDevice, s));
+    gather_values<double, double>(t.p, (side == 0 ? P.order_row : P.order_col).p, v, len, s);
+    CK(cudaStreamSynchronize(s));
+}
+// ... and back into the caller's order
+void order_to_user(const ProblemBase& P, int side, double* v, cudaStream_t s) {
+    const int64_t len = side == 0 ? P.m : P.n;
+    if (!P.ordered || len <= 0) return;
+    DBuf<double> t((size_t)len);
+    CK(cudaMemcpyAsync(t.p, v, sizeof(double) * len, cudaMemcpyDeviceToDevice, s));
+    k_scatter_order<<<grid_for(len, 256), 256, 0, s>>>(t.p, (side == 0 ? P.order_row : P.order_col).p,
+                                                       v, len);
+    CK_LAUNCH();
+    CK(cudaStreamSynchronize(s));
+}
+
+namespace {
+
+// ---------------------------------------------------------------------------
 // problem creation: preprocess (common.jl:154-169) on the device
 // ---------------------------------------------------------------------------
 template <class T>
@@ -729,6 +867,18 @@ ProblemBase* make_problem(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm
     const int32_t mt = prm->matrix_type;
     if (mt != CPDLP_FMT_AUTO && mt != CPDLP_FMT_CSR && mt != CPDLP_FMT_ELL && mt != CPDLP_FMT_COO)
         fail(CPDLP_ERR_ARGUMENT, "matrix_type must be CPDLP_FMT_AUTO, _CSR, _ELL or _COO");
+    const bool order_on = (prm->tile_flags & CPDLP_TILE_DENSITY_ORDER) != 0;
+    const bool order_off = (prm->tile_flags & CPDLP_TILE_NO_DENSITY_ORDER) != 0;
+    if (order_on && order_off)
+        fail(CPDLP_ERR_ARGUMENT, "CPDLP_TILE_DENSITY_ORDER and CPDLP_TILE_NO_DENSITY_ORDER both set");
+    if (order_on && nnz > 0) {
+        DensityOrder<T> o;
+        build_density_order(h, *P, hp2, hp1, o);
+        swap_matrices(*P, o);
+        adopt_density_order(h, *P, o);
+        hp2 = std::move(o.hp2);
+        hp1 = std::move(o.hp1);
+    }
     auto ell_fits = [&](const std::vector<int32_t>& hp, int64_t rows) {
         int64_t w = 0;
         for (int64_t r = 0; r < rows; r++) w = std::max<int64_t>(w, hp[r + 1] - hp[r]);
@@ -753,8 +903,9 @@ ProblemBase* make_problem(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm
         DBuf<StepCoef<T>> cf(1);
         CK(cudaMemsetAsync(cf.p, 0, sizeof(StepCoef<T>), s));
         ProblemT<T>* Q = P;
-        const SideChoice cAt = tune_side<T>(h, *P, 1, hp1, items_At, try_csr, ell_At, pm1 ? 3 : 1,
-                                            [&](int fmt, TilePlan& pl, T* part) {
+        // the primal step over A' and the dual step over A, with the
+        // problem's current matrices
+        auto launch_At = [&](int fmt, TilePlan& pl, T* part) {
             if (pm1) {
                 const CsrView<Pm1, T> V{Q->at_ptr.p, Q->at_idx.p, nullptr, pl.tasks.p, pl.ntasks,
                                         pl.ltasks.p, pl.nltasks, pl.counters.p, part};
@@ -769,9 +920,8 @@ ProblemBase* make_problem(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm
                 if (fmt == CPDLP_FMT_ELL) launch_ell<TILE_WARPS>(ell_view<T, T>(*Q, 1, Q->at_ptr.p), VecSet<T, 1>{{vy.p}}, pe, s);
                 else launch_tiles<1>(pl, V, VecSet<T, 1>{{vy.p}}, pe, s);
             }
-        });
-        const SideChoice cA = tune_side<T>(h, *P, 0, hp2, items_A, try_csr, ell_A, pm1 ? 2 : 0,
-                                           [&](int fmt, TilePlan& pl, T* part) {
+        };
+        auto launch_A = [&](int fmt, TilePlan& pl, T* part) {
             if (pm1) {
                 const CsrView<Pm1, T> V{Q->a_ptr.p, Q->a_idx.p, nullptr, pl.tasks.p, pl.ntasks,
                                         pl.ltasks.p, pl.nltasks, pl.counters.p, part};
@@ -786,9 +936,77 @@ ProblemBase* make_problem(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm
                 if (fmt == CPDLP_FMT_ELL) launch_ell<TILE_WARPS>(ell_view<T, T>(*Q, 0, Q->a_ptr.p), VecSet<T, 1>{{vxb.p}}, de, s);
                 else launch_tiles<1>(pl, V, VecSet<T, 1>{{vxb.p}}, de, s);
             }
-        });
+        };
+        const SideChoice cAt = tune_side<T>(h, *P, 1, hp1, items_At, try_csr, ell_At, pm1 ? 3 : 1,
+                                            launch_At);
+        const SideChoice cA = tune_side<T>(h, *P, 0, hp2, items_A, try_csr, ell_A, pm1 ? 2 : 0,
+                                           launch_A);
         items_A = cA.items;
         items_At = cAt.items;
+        // density order as a candidate (CSR on both matrices): both step
+        // kernels timed in each order, the density order kept when it is at
+        // least 3% faster; decided once per matrix shape for the process
+        if (mt == CPDLP_FMT_AUTO && !order_on && !order_off && P->fmt[0] == CPDLP_FMT_CSR &&
+            P->fmt[1] == CPDLP_FMT_CSR) {
+            static std::mutex mu;
+            static std::map<std::tuple<int64_t, int64_t, int64_t, int, int, int>, bool> cache;
+            const auto key = std::make_tuple(m, n, nnz, (int)sizeof(T), h.device, (int)pm1);
+            int decided = -1;
+            {
+                std::lock_guard<std::mutex> lock(mu);
+                auto it = cache.find(key);
+                if (it != cache.end()) decided = it->second ? 1 : 0;
+            }
+            cudaEvent_t e0, e1;
+            CK(cudaEventCreate(&e0));
+            CK(cudaEventCreate(&e1));
+            auto time_steps = [&](const std::vector<int32_t>& pa, const std::vector<int32_t>& pat) {
+                TilePlan plA, plAt;
+                build_tile_plan(pa, (int32_t)m, items_A, plA, s);
+                build_tile_plan(pat, (int32_t)n, items_At, plAt, s);
+                DBuf<T> partA((size_t)std::max(plA.npieces, 1)), partAt((size_t)std::max(plAt.npieces, 1));
+                launch_At(CPDLP_FMT_CSR, plAt, partAt.p);
+                launch_A(CPDLP_FMT_CSR, plA, partA.p);
+                CK(cudaEventRecord(e0, s));
+                for (int r = 0; r < 4; r++) {
+                    launch_At(CPDLP_FMT_CSR, plAt, partAt.p);
+                    launch_A(CPDLP_FMT_CSR, plA, partA.p);
+                }
+                CK(cudaEventRecord(e1, s));
+                CK(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                CK(cudaEventElapsedTime(&ms, e0, e1));
+                return ms;
+            };
+            try {
+                if (decided != 0) {
+                    DensityOrder<T> o;
+                    build_density_order(h, *P, hp2, hp1, o);
+                    bool keep = decided == 1;
+                    if (decided < 0) {
+                        const float t_plain = time_steps(hp2, hp1);
+                        swap_matrices(*P, o);
+                        const float t_order = time_steps(o.hp2, o.hp1);
+                        swap_matrices(*P, o);
+                        keep = t_order < 0.97f * t_plain;
+                        std::lock_guard<std::mutex> lock(mu);
+                        cache[key] = keep;
+                    }
+                    if (keep) {
+                        swap_matrices(*P, o);
+                        adopt_density_order(h, *P, o);
+                        hp2 = std::move(o.hp2);
+                        hp1 = std::move(o.hp1);
+                    }
+                }
+            } catch (...) {
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                throw;
+            }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+        }
     }
     // the CSR plans (also kept for an ELL side: the tuner and the exports use them)
     build_tile_plan(hp2, (int32_t)m, items_A, P->planA, s);
@@ -882,6 +1100,7 @@ double spectral_norm_T(Handle& h, ProblemT<V>& P, const cpdlp_params* prm, int64
     DBuf<double> scal(4);
     DBuf<int> d_it(1);
     if (n > 0) CK(cudaMemcpyAsync(x.p, x0.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    order_to_internal(P, 1, x.p, s);  // the start vector of the caller's column order
     CK(cudaMemsetAsync(d_it.p, 0, sizeof(int), s));
     const CsrView<V, double> A{P.a_ptr.p, P.a_idx.p, P.a_val.p, P.planA.tasks.p, P.planA.ntasks,
                                P.planA.ltasks.p, P.planA.nltasks, P.planA.counters.p, pA.p};
@@ -1547,12 +1766,14 @@ struct StateT : StateBase {
         if (hx && P.n > 0) {
             k_widen<T><<<grid_for(P.n, 256), 256, 0, s>>>(vx, tmp.p, P.n);
             CK_LAUNCH();
+            order_to_user(P, 1, tmp.p, s);
             CK(cudaMemcpyAsync(hx, tmp.p, sizeof(double) * P.n, cudaMemcpyDeviceToHost, s));
             CK(cudaStreamSynchronize(s));
         }
         if (hy && P.m > 0) {
             k_widen<T><<<grid_for(P.m, 256), 256, 0, s>>>(vy, tmp.p, P.m);
             CK_LAUNCH();
+            order_to_user(P, 0, tmp.p, s);
             CK(cudaMemcpyAsync(hy, tmp.p, sizeof(double) * P.m, cudaMemcpyDeviceToHost, s));
             CK(cudaStreamSynchronize(s));
         }
@@ -1566,6 +1787,8 @@ struct StateT : StateBase {
         if (P.n > 0) k_unscale<T><<<grid_for(P.n, 256), 256, 0, s>>>(x[cur].p, P.D2.p, tx.p, P.n);
         if (P.m > 0) k_unscale<T><<<grid_for(P.m, 256), 256, 0, s>>>(y[cur].p, P.D1.p, ty.p, P.m);
         CK_LAUNCH();
+        order_to_user(P, 1, tx.p, s);
+        order_to_user(P, 0, ty.p, s);
         if (hx && P.n > 0) CK(cudaMemcpyAsync(hx, tx.p, sizeof(double) * P.n, cudaMemcpyDeviceToHost, s));
         if (hy && P.m > 0) CK(cudaMemcpyAsync(hy, ty.p, sizeof(double) * P.m, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
@@ -1596,6 +1819,8 @@ StateBase* make_state(Handle& h, ProblemT<T>* P, const cpdlp_params* prm, const 
     else CK(cudaMemsetAsync(tx.p, 0, sizeof(double) * nz, s));
     if (y0 && m > 0) CK(cudaMemcpyAsync(ty.p, y0, sizeof(double) * m, cudaMemcpyHostToDevice, s));
     else CK(cudaMemsetAsync(ty.p, 0, sizeof(double) * mz, s));
+    if (x0) order_to_internal(*P, 1, tx.p, s);
+    if (y0) order_to_internal(*P, 0, ty.p, s);
     if (n > 0) k_prescale<T><<<grid_for(n, 256), 256, 0, s>>>(tx.p, P->D2.p, S->x[0].p, n);
     if (m > 0) k_prescale<T><<<grid_for(m, 256), 256, 0, s>>>(ty.p, P->D1.p, S->y[0].p, m);
     CK_LAUNCH();
@@ -2096,6 +2321,10 @@ void solve_full(Handle& h, const cpdlp_lp* lp, const cpdlp_params* params, const
     cpdlp_params p64 = *params;
     p64.float_type = CPDLP_VAL_F64;
     p64.termination_reltol = params->refine_reltol;
+    // the FP64 copy takes the FP32 problem's order (the rounds combine their
+    // vectors elementwise)
+    p64.tile_flags = (p64.tile_flags & ~(CPDLP_TILE_DENSITY_ORDER | CPDLP_TILE_NO_DENSITY_ORDER)) |
+                     (P->ordered ? CPDLP_TILE_DENSITY_ORDER : CPDLP_TILE_NO_DENSITY_ORDER);
     std::unique_ptr<ProblemBase> P64(problem_create(h, lp, &p64));
     auto& Q64 = static_cast<ProblemT<double>&>(*P64);
     std::unique_ptr<StateBase> S64(state_create(h, P64.get(), &p64, nullptr, nullptr, eta32, omega32));
@@ -2112,6 +2341,8 @@ void solve_full(Handle& h, const cpdlp_lp* lp, const cpdlp_params* params, const
         if (n > 0) k_unscale<double><<<grid_for(n, 256), 256, 0, h.stream>>>(bx.p, Q64.D2.p, T64.xr.p, n);
         if (m > 0) k_unscale<double><<<grid_for(m, 256), 256, 0, h.stream>>>(by.p, Q64.D1.p, T64.yr.p, m);
         CK_LAUNCH();
+        order_to_user(Q64, 1, T64.xr.p, h.stream);
+        order_to_user(Q64, 0, T64.yr.p, h.stream);
         if (x_out && n > 0)
             CK(cudaMemcpyAsync(x_out, T64.xr.p, sizeof(double) * n, cudaMemcpyDeviceToHost, h.stream));
         if (y_out && m > 0)
@@ -2138,6 +2369,9 @@ void solve_full(Handle& h, const cpdlp_lp* lp, const cpdlp_params* params, const
     if (n > 0) k_unscale<double><<<grid_for(n, 256), 256, 0, h.stream>>>(bx.p, Q64.D2.p, T64.xr.p, n);
     if (m > 0) k_unscale<double><<<grid_for(m, 256), 256, 0, h.stream>>>(by.p, Q64.D1.p, T64.yr.p, m);
     CK_LAUNCH();
+    // in the caller's order: the continuation's state takes them as a start
+    order_to_user(Q64, 1, T64.xr.p, h.stream);
+    order_to_user(Q64, 0, T64.yr.p, h.stream);
     if (n > 0) CK(cudaMemcpyAsync(xs.data(), T64.xr.p, sizeof(double) * n, cudaMemcpyDeviceToHost, h.stream));
     if (m > 0) CK(cudaMemcpyAsync(ys.data(), T64.yr.p, sizeof(double) * m, cudaMemcpyDeviceToHost, h.stream));
     CK(cudaStreamSynchronize(h.stream));
@@ -2179,11 +2413,17 @@ void solve_full(Handle& h, const cpdlp_lp* lp, const cpdlp_params* params, const
 }
 
 void problem_scaling(Handle& h, ProblemBase* P, double* d1, double* d2) {
-    if (d1 && P->m > 0)
-        CK(cudaMemcpyAsync(d1, P->D1.p, sizeof(double) * P->m, cudaMemcpyDeviceToHost, h.stream));
-    if (d2 && P->n > 0)
-        CK(cudaMemcpyAsync(d2, P->D2.p, sizeof(double) * P->n, cudaMemcpyDeviceToHost, h.stream));
-    CK(cudaStreamSynchronize(h.stream));
+    for (int sd = 0; sd < 2; sd++) {
+        double* out = sd == 0 ? d1 : d2;
+        const int64_t len = sd == 0 ? P->m : P->n;
+        if (!out || len <= 0) continue;
+        DBuf<double> t((size_t)len);
+        CK(cudaMemcpyAsync(t.p, (sd == 0 ? P->D1 : P->D2).p, sizeof(double) * len,
+                           cudaMemcpyDeviceToDevice, h.stream));
+        order_to_user(*P, sd, t.p, h.stream);
+        CK(cudaMemcpyAsync(out, t.p, sizeof(double) * len, cudaMemcpyDeviceToHost, h.stream));
+        CK(cudaStreamSynchronize(h.stream));
+    }
 }
 
 }  // namespace cpdlp

@@ -60,7 +60,16 @@ struct ProblemBase {
     // iterate, and four packed iterates (grid capped at kkt4_cap blocks)
     int64_t rows_A_kkt = 0, rows_At_kkt = 0;
     int64_t kkt4_cap = 0, rows_A_kkt4 = 0, rows_At_kkt4 = 0;
+    // density order (CPDLP_TILE_DENSITY_ORDER or the autotuner's choice):
+    // internal row i is the caller's row order_row[i], internal column j the
+    // caller's column order_col[j]; vectors cross the C ABI in the caller's
+    // order (order_to_internal / order_to_user)
+    bool ordered = false;
+    DBuf<int32_t> order_row, order_col;
 };
+
+void order_to_internal(const ProblemBase& P, int side, double* v, cudaStream_t s);
+void order_to_user(const ProblemBase& P, int side, double* v, cudaStream_t s);
 
 template <class T>
 struct ProblemT : ProblemBase {

@@ -221,6 +221,31 @@ __global__ void k_gather_values(const TI* __restrict__ in, const int32_t* __rest
     if (k < nnz) out[k] = (TO)in[perm[k]];
 }
 
+// lengths of the reordered rows: len[i] = length of row order[i]
+__global__ void k_ordered_lengths(const int32_t* __restrict__ ptr, const int32_t* __restrict__ order,
+                                  int64_t rows, int32_t* __restrict__ len) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < rows) len[i] = ptr[order[i] + 1] - ptr[order[i]];
+}
+
+// entry k of the reordered CSR: the same place in row order[i] of the input,
+// its column renamed (a narrow +-1 index ~c of a -1 entry stays encoded)
+template <class T>
+__global__ void k_reorder_entries(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+                                  const T* __restrict__ val, const int32_t* __restrict__ ptr_out,
+                                  const int32_t* __restrict__ row_of,
+                                  const int32_t* __restrict__ order,
+                                  const int32_t* __restrict__ col_inv, int64_t nnz,
+                                  int32_t* __restrict__ idx_out, T* __restrict__ val_out) {
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nnz) return;
+    const int32_t i = row_of[k];
+    const int64_t src = (int64_t)ptr[order[i]] + (k - ptr_out[i]);
+    const int32_t c = idx[src];
+    idx_out[k] = c >= 0 ? col_inv[c] : ~col_inv[~c];
+    if (val) val_out[k] = val[src];
+}
+
 }  // namespace
 
 void exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, cudaStream_t s) {
@@ -271,6 +296,34 @@ void gather_values(const TI* in, const int32_t* perm, TO* out, int64_t nnz, cuda
 }
 template void gather_values<double, double>(const double*, const int32_t*, double*, int64_t, cudaStream_t);
 template void gather_values<float, double>(const double*, const int32_t*, float*, int64_t, cudaStream_t);
+template void gather_values<float, float>(const float*, const int32_t*, float*, int64_t, cudaStream_t);
+
+template <class T>
+void reorder_csr(const int32_t* ptr, const int32_t* idx, const T* val, int64_t rows, int64_t nnz,
+                 const int32_t* order, const int32_t* col_inv, int32_t* ptr_out, int32_t* idx_out,
+                 T* val_out, cudaStream_t s) {
+    DBuf<int32_t> len((size_t)(rows > 0 ? rows : 1));
+    if (rows > 0) {
+        k_ordered_lengths<<<grid_for(rows, 256), 256, 0, s>>>(ptr, order, rows, len.p);
+        CK_LAUNCH();
+    }
+    exclusive_scan_i32(len.p, ptr_out, rows, s);
+    if (nnz > 0) {
+        DBuf<int32_t> row_of((size_t)nnz);
+        expand_rows(ptr_out, rows, row_of.p, nnz, s);
+        k_reorder_entries<T><<<grid_for(nnz, 256), 256, 0, s>>>(ptr, idx, val, ptr_out, row_of.p,
+                                                               order, col_inv, nnz, idx_out,
+                                                               val_out);
+        CK_LAUNCH();
+    }
+    CK(cudaStreamSynchronize(s));
+}
+template void reorder_csr<float>(const int32_t*, const int32_t*, const float*, int64_t, int64_t,
+                                 const int32_t*, const int32_t*, int32_t*, int32_t*, float*,
+                                 cudaStream_t);
+template void reorder_csr<double>(const int32_t*, const int32_t*, const double*, int64_t, int64_t,
+                                  const int32_t*, const int32_t*, int32_t*, int32_t*, double*,
+                                  cudaStream_t);
 
 static int bit_width(uint64_t v) {
     int b = 0;

@@ -39,4 +39,14 @@ void expand_rows(const int32_t* ptr, int64_t rows, int32_t* row_of, int64_t nnz,
 template <class TO, class TI>
 void gather_values(const TI* in, const int32_t* perm, TO* out, int64_t nnz, cudaStream_t s);
 
+// A CSR with its rows reordered -- row i of the output is row order[i] of the
+// input -- and its column indices renamed by col_inv (input column -> output
+// column).  Every row keeps its entries in their input order, so a row's sum
+// runs in the same order as before.  val may be null (narrow +-1 storage,
+// whose -1 entries keep the ~col encoding).  ptr_out: rows + 1 entries.
+template <class T>
+void reorder_csr(const int32_t* ptr, const int32_t* idx, const T* val, int64_t rows, int64_t nnz,
+                 const int32_t* order, const int32_t* col_inv, int32_t* ptr_out, int32_t* idx_out,
+                 T* val_out, cudaStream_t s);
+
 }  // namespace cpdlp

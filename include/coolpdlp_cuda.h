@@ -167,8 +167,25 @@ typedef struct cpdlp_params {
  * matrix values are all exactly +-1 stores the matrix narrow: the signs ride
  * in the column indices (4 bytes per nonzero, no value array) and the kernels
  * apply the diagonal scalings D1, D2 themselves.  CPDLP_TILE_NO_NARROW keeps
- * the scaled values instead. */
-enum { CPDLP_TILE_NO_NARROW = 1 };
+ * the scaled values instead.
+ * Density order (EXT): CPDLP_TILE_DENSITY_ORDER renumbers the rows and the
+ * columns of a single-LP solve's matrices by increasing length, ties in index
+ * order -- the order of the reference's sort_rows_columns
+ * (src/components/permutation.jl:1-46) -- while every row keeps its entries in
+ * their input order, so each row's products and sum are the ones of the
+ * unordered problem.  The gathers of the many-times-referenced long rows'
+ * entries then share cache lines.  CPDLP_TILE_NO_DENSITY_ORDER never
+ * reorders.  With neither, the autotuner (matrix_type CPDLP_FMT_AUTO, at
+ * least 2^21 nonzeros, CSR chosen for both matrices) times both fused step
+ * kernels in each order and keeps the density order when it is at least 3%
+ * faster.  Every vector crossing the ABI (starting points, iterates,
+ * solutions, scalings) is in the caller's order either way;
+ * cpdlp_problem_order reports the choice. */
+enum {
+    CPDLP_TILE_NO_NARROW = 1,
+    CPDLP_TILE_DENSITY_ORDER = 2,
+    CPDLP_TILE_NO_DENSITY_ORDER = 4
+};
 
 /* An LP in the reference's "cuPDLPx form" (src/problems/milp.jl:1-20):
  *   min c'x  s.t.  lv <= x <= uv,  lc <= A x <= uc
@@ -367,6 +384,14 @@ int cpdlp_solve_history(const cpdlp_handle* h, int64_t* kkt_passes, cpdlp_kkt_er
  * and ELL width (0 for CSR).  Any pointer may be NULL.  EXT (measurement). */
 int cpdlp_problem_layout(const cpdlp_problem* p, int32_t* format, int32_t* tile_nnz,
                          int64_t* width);
+
+/* Whether the solve of this problem runs in density order
+ * (CPDLP_TILE_DENSITY_ORDER); *ordered = 1 or 0.  With order_row (m) and
+ * order_col (n) non-NULL and the order applied, they receive the 1-based
+ * orders: internal row i is the caller's row order_row[i], as the perm_cons
+ * and perm_var of cpdlp_sort_rows_columns.  EXT (measurement). */
+int cpdlp_problem_order(cpdlp_handle* h, const cpdlp_problem* p, int32_t* ordered,
+                        int64_t* order_row, int64_t* order_col);
 
 /* The reduced costs z = proj_multiplier.(c .- A'y, lv, uv) (n) and the dual
  * objective sum safeprod_left(lc, y+) - sum safeprod_left(uc, y-)
