@@ -1280,7 +1280,9 @@ Job* job_submit(Handle& h, int64_t count, const cpdlp_lp* lps, const cpdlp_param
     if (params->check_every <= 0) fail(CPDLP_ERR_ARGUMENT, "check_every must be positive");
     if (params->float_type != CPDLP_VAL_F64 && params->float_type != CPDLP_VAL_F32)
         fail(CPDLP_ERR_ARGUMENT, "float_type must be CPDLP_VAL_F64 or CPDLP_VAL_F32");
-    if (params->tile_flags & ~CPDLP_TILE_NO_NARROW) fail(CPDLP_ERR_ARGUMENT, "unknown tile_flags bits");
+    // the density-order bits concern single-LP solves (batched LPs run in their own order)
+    if (params->tile_flags & ~(CPDLP_TILE_NO_NARROW | CPDLP_TILE_DENSITY_ORDER | CPDLP_TILE_NO_DENSITY_ORDER))
+        fail(CPDLP_ERR_ARGUMENT, "unknown tile_flags bits");
     if (count > INT32_MAX) fail(CPDLP_ERR_UNSUPPORTED, "batch too large");
     if (max_ctas < 0) fail(CPDLP_ERR_ARGUMENT, "max_ctas must be >= 0");
     for (int64_t k = 0; k < count; k++) check_lp(lps[k]);

@@ -2198,7 +2198,8 @@ void StateBase::stats(cpdlp_stats* st) const {
 ProblemBase* problem_create(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm, bool plans) {
     if (!lp || !prm) fail(CPDLP_ERR_ARGUMENT, "null lp or params");
     if (lp->m < 0 || lp->n < 0) fail(CPDLP_ERR_DIMENSION, "negative problem size");
-    if (prm->tile_flags & ~CPDLP_TILE_NO_NARROW) fail(CPDLP_ERR_ARGUMENT, "unknown tile_flags bits");
+    if (prm->tile_flags & ~(CPDLP_TILE_NO_NARROW | CPDLP_TILE_DENSITY_ORDER | CPDLP_TILE_NO_DENSITY_ORDER))
+        fail(CPDLP_ERR_ARGUMENT, "unknown tile_flags bits");
     if (prm->float_type == CPDLP_VAL_F32) return make_problem<float>(h, lp, prm, plans);
     if (prm->float_type == CPDLP_VAL_F64) return make_problem<double>(h, lp, prm, plans);
     fail(CPDLP_ERR_ARGUMENT, "float_type must be CPDLP_VAL_F64 or CPDLP_VAL_F32");

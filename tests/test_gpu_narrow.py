@@ -165,6 +165,10 @@ def test_unknown_tile_flags_rejected(handle):
     L = native.LPStruct(lp.m, lp.n, lp.colptr, lp.rowval, lp.nzval, lp.c, lp.lv, lp.uv, lp.lc,
                         lp.uc)
     p = _params(True)
-    p.tile_flags = 2
+    p.tile_flags = 8
+    with pytest.raises(A.ArgumentError):
+        native.solve_lp(handle, L, p)
+    # the density order forced both on and off
+    p.tile_flags = A.TILE_DENSITY_ORDER | A.TILE_NO_DENSITY_ORDER
     with pytest.raises(A.ArgumentError):
         native.solve_lp(handle, L, p)
