@@ -84,6 +84,8 @@ def parse_args():
                     help="product format of the large LP (profiling; auto = the autotuner)")
     ap.add_argument("--tile-nnz", type=int, default=0,
                     help="CSR tile size of the large LP (profiling; 0 = autotuned)")
+    ap.add_argument("--density-order", choices=["auto", "on", "off"], default="auto",
+                    help="density order of the large LP (profiling; auto = the autotuner)")
     ap.add_argument("--only-serving-stream", type=int, default=0,
                     help="run only a long served stream of this many requests at the first "
                          "rate of --serve-rates (FP32+FP64-refined); no headline value")
@@ -710,6 +712,8 @@ def run_ours(args):
     prm.time_limit = 1e30
     prm.matrix_type = {"auto": A.FMT_AUTO, "csr": A.FMT_CSR, "ell": A.FMT_ELL}[args.matrix_type]
     prm.tile_nnz = args.tile_nnz
+    prm.tile_flags = {"auto": 0, "on": A.TILE_DENSITY_ORDER,
+                      "off": A.TILE_NO_DENSITY_ORDER}[args.density_order]
     L = native.LPStruct(lp.m, lp.n, lp.colptr, lp.rowval, lp.nzval, lp.c, lp.lv, lp.uv, lp.lc,
                         lp.uc)
     t0 = time.perf_counter()

@@ -40,6 +40,7 @@ double now_seconds() {
 namespace {
 
 constexpr int RED_THREADS = TILE_WARPS * 32;
+int trace_level();  // CPDLP_TRACE (defined with the refinement's traces)
 
 // ---------------------------------------------------------------------------
 // preconditioning kernels (FP64, preconditioning.jl:37-155)
@@ -713,6 +714,15 @@ template <class T>
 ProblemBase* make_problem(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm, bool plans) {
     double t0 = now_seconds();
     cudaStream_t s = h.stream;
+    // CPDLP_TRACE=1: the time of each setup phase (synchronised only when tracing)
+    double t_mark = t0;
+    auto mark = [&](const char* what) {
+        if (trace_level() <= 0) return;
+        CK(cudaStreamSynchronize(s));
+        const double t = now_seconds();
+        fprintf(stderr, "[cpdlp setup] %-28s %8.2f ms\n", what, 1e3 * (t - t_mark));
+        t_mark = t;
+    };
     auto* P = new ProblemT<T>();
     std::unique_ptr<ProblemT<T>> guard(P);
     P->h = &h;
@@ -725,6 +735,7 @@ ProblemBase* make_problem(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm
         if (m > 0 && !v) fail(CPDLP_ERR_ARGUMENT, "null constraint vector (lc or uc)");
     CscPair S;
     build_csc_pair(h, m, n, lp->nnz, lp->colptr, lp->rowval, lp->nzval, S);
+    mark("upload, check, transpose");
     const int64_t nnz = S.nnz;
     P->m = m; P->n = n; P->nnz = nnz;
     const size_t zn = (size_t)(nnz > 0 ? nnz : 1), mz = (size_t)(m > 0 ? m : 1),
@@ -755,6 +766,7 @@ ProblemBase* make_problem(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm
         k_mul_into<<<gn, 256, 0, s>>>(r2.p, d2.p, n);
         CK_LAUNCH();
     }
+    mark("Ruiz");
     // Pock-Chambolle on the Ruiz-scaled ORIGINAL matrix (preconditioning.jl:146-155)
     if (nnz > 0) {
         k_scale_S1<<<gz, 256, 0, s>>>(S.idx1.p, S.col1.p, vA.p, r1.p, r2.p, tA.p, nnz);
@@ -849,6 +861,7 @@ ProblemBase* make_problem(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm
     }
     P->D1 = std::move(D1);
     P->D2 = std::move(D2);
+    mark("Pock-Chambolle, values, vectors");
     if (!plans) {  // the batched solver partitions the matrices itself
         P->zero_cost = false;
         CK(cudaStreamSynchronize(s));
@@ -871,6 +884,7 @@ ProblemBase* make_problem(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm
     const bool order_off = (prm->tile_flags & CPDLP_TILE_NO_DENSITY_ORDER) != 0;
     if (order_on && order_off)
         fail(CPDLP_ERR_ARGUMENT, "CPDLP_TILE_DENSITY_ORDER and CPDLP_TILE_NO_DENSITY_ORDER both set");
+    mark("row pointers to the host");
     if (order_on && nnz > 0) {
         DensityOrder<T> o;
         build_density_order(h, *P, hp2, hp1, o);
@@ -1008,6 +1022,7 @@ ProblemBase* make_problem(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm
             cudaEventDestroy(e1);
         }
     }
+    mark("formats, autotuner, density order");
     // the CSR plans (also kept for an ELL side: the tuner and the exports use them)
     build_tile_plan(hp2, (int32_t)m, items_A, P->planA, s);
     build_tile_plan(hp1, (int32_t)n, items_At, P->planAt, s);
@@ -1042,6 +1057,7 @@ ProblemBase* make_problem(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm
     for (int64_t j = 0; j < n; j++)
         if (lp->c[j] != 0.0) { zc = false; break; }
     P->zero_cost = zc;
+    mark("tile plans, scales");
     CK(cudaStreamSynchronize(s));
     P->setup_seconds = now_seconds() - t0;
     guard.release();
@@ -1869,6 +1885,9 @@ StateBase* make_state(Handle& h, ProblemT<T>* P, const cpdlp_params* prm, const 
     for (auto* e : {&S->err, &S->err_cand, &S->err_cand_last, &S->err_restart})
         e->primal = e->primal_scale = e->dual = e->dual_scale = e->gap = e->gap_scale = NAN;
     CK(cudaStreamSynchronize(s));
+    if (trace_level() > 0)
+        fprintf(stderr, "[cpdlp setup] %-28s %8.2f ms (%lld power iterations)\n",
+                "state, power method", 1e3 * (now_seconds() - t0), (long long)S->power_iterations);
     S->setup_seconds = P->setup_seconds + (now_seconds() - t0);
     guard.release();
     return S;
@@ -1891,8 +1910,8 @@ constexpr int REFINE_MAX_ROUNDS = 8;
 constexpr double REFINE_ROUND_DECAY = 1e-4;
 constexpr double REFINE_MAX_SCALE = 1099511627776.0;  // 2^40
 
-// CPDLP_TRACE=1 in the environment prints one line per refinement round to
-// stderr, CPDLP_TRACE=2 also one line per check
+// CPDLP_TRACE=1 in the environment prints one line per setup phase and per
+// refinement round to stderr, CPDLP_TRACE=2 also one line per check
 int trace_level() {
     static const int lvl = [] {
         const char* v = std::getenv("CPDLP_TRACE");
@@ -2281,7 +2300,11 @@ void solve_full(Handle& h, const cpdlp_lp* lp, const cpdlp_params* params, const
             }
         }
     } else {
+        const double ts = now_seconds();
         S->solve();
+        if (trace_on())
+            fprintf(stderr, "[cpdlp setup] %-28s %8.2f ms (%lld passes)\n", "solve", 1e3 * (now_seconds() - ts),
+                    (long long)S->kkt_passes);
     }
     if (mixed && trace_on())
         fprintf(stderr, "[cpdlp refine] %.2fs FP32 phase: rel %.3e (best %.3e) after %lld passes%s\n",
@@ -2291,7 +2314,10 @@ void solve_full(Handle& h, const cpdlp_lp* lp, const cpdlp_params* params, const
     const bool refine = mixed && stalled;
     keep_history(*S, 0);
     if (!refine) {
+        const double ts = now_seconds();
         S->solution(x_out, y_out);
+        if (trace_on())
+            fprintf(stderr, "[cpdlp setup] %-28s %8.2f ms\n", "solution to the host", 1e3 * (now_seconds() - ts));
         if (stats) {
             S->stats(stats);
             stats->history_length = (int64_t)h.solve_hist_passes.size();
