@@ -38,25 +38,6 @@
 namespace cpdlp {
 
 namespace {
-// f(k) for k in [0, count) on up to 16 host threads (contiguous blocks of k)
-template <class F>
-void parallel_for(int64_t count, F&& f) {
-    const int64_t hw = std::max<int64_t>(1, std::min<int64_t>(16, std::thread::hardware_concurrency()));
-    const int64_t nt = std::min<int64_t>(hw, std::max<int64_t>(1, count / 64));
-    if (nt <= 1) {
-        for (int64_t k = 0; k < count; k++) f(k);
-        return;
-    }
-    std::vector<std::thread> th;
-    for (int64_t t = 0; t < nt; t++)
-        th.emplace_back([&, t] {
-            for (int64_t k = count * t / nt; k < count * (t + 1) / nt; k++) f(k);
-        });
-    for (auto& x : th) x.join();
-}
-}  // namespace
-
-namespace {
 
 namespace cg = cooperative_groups;
 

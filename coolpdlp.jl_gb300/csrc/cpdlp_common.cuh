@@ -11,7 +11,9 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <utility>
+#include <vector>
 #include <vector>
 
 #include "../../include/coolpdlp_cuda.h"
@@ -238,5 +240,23 @@ inline unsigned grid_for(int64_t items, int threads, int64_t cap = 1 << 30) {
 
 // wall clock (seconds)
 double now_seconds();
+
+// f(k) for k in [0, count) on up to 16 host threads, each a contiguous block
+// of k (f must not depend on which thread runs it)
+template <class F>
+void parallel_for(int64_t count, F&& f) {
+    const int64_t hw = std::max<int64_t>(1, std::min<int64_t>(16, std::thread::hardware_concurrency()));
+    const int64_t nt = std::min<int64_t>(hw, std::max<int64_t>(1, count / 64));
+    if (nt <= 1) {
+        for (int64_t k = 0; k < count; k++) f(k);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (int64_t t = 0; t < nt; t++)
+        th.emplace_back([&, t] {
+            for (int64_t k = count * t / nt; k < count * (t + 1) / nt; k++) f(k);
+        });
+    for (auto& x : th) x.join();
+}
 
 }  // namespace cpdlp

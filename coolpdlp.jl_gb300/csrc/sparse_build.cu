@@ -5,6 +5,8 @@
 // row.  SparseArrays produces it with a sequential counting sort; here it is a
 // stable LSD radix sort of the CSC entries by row, which yields the same
 // (unique) order, so the index arrays match the reference bit for bit.
+#include <cstdlib>
+
 #include "sparse_build.cuh"
 
 namespace cpdlp {
@@ -333,6 +335,19 @@ static int bit_width(uint64_t v) {
 
 void build_csc_pair(Handle& h, int64_t m, int64_t n, int64_t nnz, const int64_t* colptr1,
                     const int64_t* rowval1, const double* nzval, CscPair& out) {
+    // CPDLP_TRACE=1: the time of each phase
+    static const bool trace = [] {
+        const char* v = std::getenv("CPDLP_TRACE");
+        return v && std::atoi(v) > 0;
+    }();
+    double t_mark = now_seconds();
+    auto mark = [&](const char* what) {
+        if (!trace) return;
+        CK(cudaStreamSynchronize(h.stream));
+        const double t = now_seconds();
+        fprintf(stderr, "[cpdlp setup]   %-26s %8.2f ms\n", what, 1e3 * (t - t_mark));
+        t_mark = t;
+    };
     if (m < 0 || n < 0 || nnz < 0) fail(CPDLP_ERR_DIMENSION, "negative matrix size");
     if (!colptr1 || (nnz > 0 && (!rowval1 || !nzval)))
         fail(CPDLP_ERR_ARGUMENT, "null CSC array pointer");
@@ -350,6 +365,7 @@ void build_csc_pair(Handle& h, int64_t m, int64_t n, int64_t nnz, const int64_t*
     DBuf<int> flags(1);
     CK(cudaMemsetAsync(flags.p, 0, sizeof(int), s));
     out.ptr1.alloc((size_t)n + 1);
+    mark("upload");
     k_check_colptr<<<grid_for(n + 1, 256), 256, 0, s>>>(cp.p, n, nnz, out.ptr1.p, flags.p);
     CK_LAUNCH();
     int hflags = 0;
@@ -373,6 +389,7 @@ void build_csc_pair(Handle& h, int64_t m, int64_t n, int64_t nnz, const int64_t*
         if (hflags & BAD_ORDER)
             fail(CPDLP_ERR_ARGUMENT, "invalid CSC: rows not strictly ascending inside a column");
     }
+    mark("checks");
     // transpose: stable sort of the entries by row
     out.ptr2.alloc((size_t)m + 1);
     out.idx2.alloc(zn + 16);
@@ -399,6 +416,7 @@ void build_csc_pair(Handle& h, int64_t m, int64_t n, int64_t nnz, const int64_t*
         CK_LAUNCH();
     }
     CK(cudaStreamSynchronize(s));
+    mark("transpose");
 }
 
 }  // namespace cpdlp
