@@ -574,18 +574,6 @@ void fetch_reduced(Handle& h, const double* part, int64_t rows, int q, double* d
 // (permutation.jl:1-46) -- rows and columns by increasing length, ties in
 // index order (Julia's stable sortperm) -- applied inside the solver
 // ---------------------------------------------------------------------------
-// the rows of a CSR (row pointer hp) by increasing length: a counting sort
-std::vector<int32_t> order_by_length(const std::vector<int32_t>& hp, int64_t rows) {
-    int32_t maxlen = 0;
-    for (int64_t r = 0; r < rows; r++) maxlen = std::max(maxlen, hp[r + 1] - hp[r]);
-    std::vector<int64_t> next((size_t)maxlen + 2, 0);
-    for (int64_t r = 0; r < rows; r++) next[(size_t)(hp[r + 1] - hp[r]) + 1]++;
-    for (size_t l = 1; l < next.size(); l++) next[l] += next[l - 1];
-    std::vector<int32_t> order((size_t)rows);
-    for (int64_t r = 0; r < rows; r++) order[(size_t)next[(size_t)(hp[r + 1] - hp[r])]++] = (int32_t)r;
-    return order;
-}
-
 // A problem's matrices in density order (internal row i = row orow[i] of A,
 // internal column j = column ocol[j]), built next to the problem's own
 template <class T>
@@ -597,27 +585,18 @@ struct DensityOrder {
 };
 
 template <class T>
-void build_density_order(Handle& h, const ProblemT<T>& P, const std::vector<int32_t>& hp2,
-                         const std::vector<int32_t>& hp1, DensityOrder<T>& o) {
+void build_density_order(Handle& h, const ProblemT<T>& P, DensityOrder<T>& o) {
     cudaStream_t s = h.stream;
     const int64_t m = P.m, n = P.n, nnz = P.nnz;
     const size_t mz = (size_t)std::max<int64_t>(m, 1), nz = (size_t)std::max<int64_t>(n, 1),
                  zn = (size_t)std::max<int64_t>(nnz, 1);
-    const std::vector<int32_t> orow = order_by_length(hp2, m), ocol = order_by_length(hp1, n);
-    std::vector<int32_t> irow((size_t)m), icol((size_t)n);
-    for (int64_t k = 0; k < m; k++) irow[(size_t)orow[(size_t)k]] = (int32_t)k;
-    for (int64_t k = 0; k < n; k++) icol[(size_t)ocol[(size_t)k]] = (int32_t)k;
+    // stable sorts of the row lengths on the device (rows of A: the constraints,
+    // rows of A': the variables)
     DBuf<int32_t> dirow(mz), dicol(nz);
     o.orow.alloc(mz);
     o.ocol.alloc(nz);
-    if (m > 0) {
-        CK(cudaMemcpyAsync(o.orow.p, orow.data(), sizeof(int32_t) * m, cudaMemcpyHostToDevice, s));
-        CK(cudaMemcpyAsync(dirow.p, irow.data(), sizeof(int32_t) * m, cudaMemcpyHostToDevice, s));
-    }
-    if (n > 0) {
-        CK(cudaMemcpyAsync(o.ocol.p, ocol.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, s));
-        CK(cudaMemcpyAsync(dicol.p, icol.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, s));
-    }
+    order_by_length(P.a_ptr.p, m, nnz, o.orow.p, dirow.p, s);
+    order_by_length(P.at_ptr.p, n, nnz, o.ocol.p, dicol.p, s);
     o.a_ptr.alloc((size_t)m + 1);
     o.at_ptr.alloc((size_t)n + 1);
     // index arrays carry the tile engine's 16 padding elements, value arrays PAD_ELEMS
@@ -887,7 +866,7 @@ ProblemBase* make_problem(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm
     mark("row pointers to the host");
     if (order_on && nnz > 0) {
         DensityOrder<T> o;
-        build_density_order(h, *P, hp2, hp1, o);
+        build_density_order(h, *P, o);
         swap_matrices(*P, o);
         adopt_density_order(h, *P, o);
         hp2 = std::move(o.hp2);
@@ -995,7 +974,7 @@ ProblemBase* make_problem(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm
             try {
                 if (decided != 0) {
                     DensityOrder<T> o;
-                    build_density_order(h, *P, hp2, hp1, o);
+                    build_density_order(h, *P, o);
                     bool keep = decided == 1;
                     if (decided < 0) {
                         const float t_plain = time_steps(hp2, hp1);

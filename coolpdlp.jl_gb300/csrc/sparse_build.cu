@@ -230,6 +230,19 @@ __global__ void k_ordered_lengths(const int32_t* __restrict__ ptr, const int32_t
     if (i < rows) len[i] = ptr[order[i] + 1] - ptr[order[i]];
 }
 
+__global__ void k_lengths_u32(const int32_t* __restrict__ ptr, int64_t rows, uint32_t* __restrict__ len) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < rows) len[i] = (uint32_t)(ptr[i + 1] - ptr[i]);
+}
+__global__ void k_order_out(const uint32_t* __restrict__ sorted, int64_t n, int32_t* __restrict__ order,
+                            int32_t* __restrict__ inv) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) {
+        order[k] = (int32_t)sorted[k];
+        inv[sorted[k]] = (int32_t)k;
+    }
+}
+
 // entry k of the reordered CSR: the same place in row order[i] of the input,
 // its column renamed (a narrow +-1 index ~c of a -1 entry stays encoded)
 template <class T>
@@ -300,6 +313,26 @@ template void gather_values<double, double>(const double*, const int32_t*, doubl
 template void gather_values<float, double>(const double*, const int32_t*, float*, int64_t, cudaStream_t);
 template void gather_values<float, float>(const float*, const int32_t*, float*, int64_t, cudaStream_t);
 
+static int bit_width(uint64_t v) {
+    int b = 0;
+    while (v) { b++; v >>= 1; }
+    return b;
+}
+
+void order_by_length(const int32_t* ptr, int64_t rows, int64_t max_len, int32_t* order, int32_t* inv,
+                     cudaStream_t s) {
+    if (rows <= 0) return;
+    DBuf<uint32_t> k0((size_t)rows), v0((size_t)rows), k1((size_t)rows), v1((size_t)rows);
+    k_lengths_u32<<<grid_for(rows, 256), 256, 0, s>>>(ptr, rows, k0.p);
+    k_iota<<<grid_for(rows, 256), 256, 0, s>>>(v0.p, rows);
+    CK_LAUNCH();
+    uint32_t *kp = k0.p, *vp = v0.p, *kt = k1.p, *vt = v1.p;
+    radix_sort_pairs(kp, vp, kt, vt, rows, bit_width((uint64_t)(max_len > 0 ? max_len : 0)), s);
+    k_order_out<<<grid_for(rows, 256), 256, 0, s>>>(vp, rows, order, inv);
+    CK_LAUNCH();
+    CK(cudaStreamSynchronize(s));
+}
+
 template <class T>
 void reorder_csr(const int32_t* ptr, const int32_t* idx, const T* val, int64_t rows, int64_t nnz,
                  const int32_t* order, const int32_t* col_inv, int32_t* ptr_out, int32_t* idx_out,
@@ -327,11 +360,6 @@ template void reorder_csr<double>(const int32_t*, const int32_t*, const double*,
                                   const int32_t*, const int32_t*, int32_t*, int32_t*, double*,
                                   cudaStream_t);
 
-static int bit_width(uint64_t v) {
-    int b = 0;
-    while (v) { b++; v >>= 1; }
-    return b;
-}
 
 void build_csc_pair(Handle& h, int64_t m, int64_t n, int64_t nnz, const int64_t* colptr1,
                     const int64_t* rowval1, const double* nzval, CscPair& out) {
@@ -357,6 +385,7 @@ void build_csc_pair(Handle& h, int64_t m, int64_t n, int64_t nnz, const int64_t*
     out.m = m; out.n = n; out.nnz = nnz;
     DBuf<int64_t> cp((size_t)n + 1), rv((size_t)(nnz > 0 ? nnz : 1));
     out.val1.alloc((size_t)(nnz > 0 ? nnz : 1));
+    mark("allocate");
     CK(cudaMemcpyAsync(cp.p, colptr1, sizeof(int64_t) * (size_t)(n + 1), cudaMemcpyHostToDevice, s));
     if (nnz > 0) {
         CK(cudaMemcpyAsync(rv.p, rowval1, sizeof(int64_t) * (size_t)nnz, cudaMemcpyHostToDevice, s));

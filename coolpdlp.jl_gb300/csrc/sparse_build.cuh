@@ -39,6 +39,12 @@ void expand_rows(const int32_t* ptr, int64_t rows, int32_t* row_of, int64_t nnz,
 template <class TO, class TI>
 void gather_values(const TI* in, const int32_t* perm, TO* out, int64_t nnz, cudaStream_t s);
 
+// The rows of a CSR by increasing length, ties in index order (a stable sort,
+// like Julia's sortperm): order[i] = the i-th row, inv[order[i]] = i.
+// max_len bounds the row lengths.
+void order_by_length(const int32_t* ptr, int64_t rows, int64_t max_len, int32_t* order, int32_t* inv,
+                     cudaStream_t s);
+
 // A CSR with its rows reordered -- row i of the output is row order[i] of the
 // input -- and its column indices renamed by col_inv (input column -> output
 // column).  Every row keeps its entries in their input order, so a row's sum
