@@ -81,11 +81,11 @@ def parse_args():
     ap.add_argument("--only-flow", action="store_true",
                     help="run only the flow measurement (profiling); no headline value")
     ap.add_argument("--matrix-type", choices=["auto", "csr", "ell"], default="auto",
-                    help="product format of the large LP (profiling; auto = the autotuner)")
+                    help="product format of the large LP and the flow LP (profiling; auto = the autotuner)")
     ap.add_argument("--tile-nnz", type=int, default=0,
-                    help="CSR tile size of the large LP (profiling; 0 = autotuned)")
+                    help="CSR tile size of the large LP and the flow LP (profiling; 0 = autotuned)")
     ap.add_argument("--density-order", choices=["auto", "on", "off"], default="auto",
-                    help="density order of the large LP (profiling; auto = the autotuner)")
+                    help="density order of the large LP and the flow LP (profiling; auto = the autotuner)")
     ap.add_argument("--only-serving-stream", type=int, default=0,
                     help="run only a long served stream of this many requests at the first "
                          "rate of --serve-rates (FP32+FP64-refined); no headline value")
@@ -347,7 +347,20 @@ def measure_batch(h, count: int, sample: int, m_hi: int = 5000, rank: int = 0, w
     return out
 
 
-def measure_flow(h, side: int, K: int, blocks: int = 10, solves: bool = True) -> dict:
+def layout_params(prm, args):
+    """--matrix-type, --tile-nnz and --density-order (profiling: a pinned
+    layout, no autotuner launches) on a problem's parameters."""
+    from coolpdlp import _abi as A
+    if args is None:
+        return
+    prm.matrix_type = {"auto": A.FMT_AUTO, "csr": A.FMT_CSR, "ell": A.FMT_ELL}[args.matrix_type]
+    prm.tile_nnz = args.tile_nnz
+    prm.tile_flags |= {"auto": 0, "on": A.TILE_DENSITY_ORDER,
+                       "off": A.TILE_NO_DENSITY_ORDER}[args.density_order]
+
+
+def measure_flow(h, side: int, K: int, blocks: int = 10, solves: bool = True,
+                 args=None) -> dict:
     """The structured multicommodity min-cost flow LP (side x side grid, K
     commodities, matrix values exactly +-1): FP32 PDLP iterations per second
     with the narrow +-1 storage (the default) and with the scaled values
@@ -374,6 +387,7 @@ def measure_flow(h, side: int, K: int, blocks: int = 10, solves: bool = True) ->
         prm.termination_reltol = 0.0
         prm.max_kkt_passes = 1 << 60
         prm.time_limit = 1e30
+        layout_params(prm, args)
         P = native.Problem(h, L, prm)
         S = native.State(P, prm)
         for _ in range(3):
@@ -690,7 +704,8 @@ def run_ours(args):
             h = native.Handle(local)
             print(json.dumps({"metric": METRIC, "impl": "ours", "value": None,
                               "flow": measure_flow(h, args.flow_side, args.flow_k,
-                                                   solves=not args.flow_no_solve)}), flush=True)
+                                                   solves=not args.flow_no_solve, args=args)}),
+                  flush=True)
         return
     if args.only_serving_stream > 0:
         if rank == 0:
@@ -715,10 +730,7 @@ def run_ours(args):
     prm.termination_reltol = 0.0
     prm.max_kkt_passes = 1 << 60
     prm.time_limit = 1e30
-    prm.matrix_type = {"auto": A.FMT_AUTO, "csr": A.FMT_CSR, "ell": A.FMT_ELL}[args.matrix_type]
-    prm.tile_nnz = args.tile_nnz
-    prm.tile_flags = {"auto": 0, "on": A.TILE_DENSITY_ORDER,
-                      "off": A.TILE_NO_DENSITY_ORDER}[args.density_order]
+    layout_params(prm, args)
     L = native.LPStruct(lp.m, lp.n, lp.colptr, lp.rowval, lp.nzval, lp.c, lp.lv, lp.uv, lp.lc,
                         lp.uc)
     t0 = time.perf_counter()
@@ -857,7 +869,7 @@ def run_ours(args):
             line["c1"] = measure_c1_solves(h, lp, args.c1_time_limit, args.c1_refine_time_limit)
         if args.flow_side > 0:
             line["flow"] = measure_flow(h, args.flow_side, args.flow_k,
-                                        solves=not args.flow_no_solve)
+                                        solves=not args.flow_no_solve, args=args)
         if batch is not None:
             line["batch"] = batch
         if args.serve_requests > 0:
