@@ -18,10 +18,12 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cstdio>
+#include <exception>
 #include <chrono>
 #include <functional>
 #include <map>
 #include <mutex>
+#include <thread>
 #include <tuple>
 #include <memory>
 #include <type_traits>
@@ -1002,9 +1004,28 @@ ProblemBase* make_problem(Handle& h, const cpdlp_lp* lp, const cpdlp_params* prm
         }
     }
     mark("formats, autotuner, density order");
-    // the CSR plans (also kept for an ELL side: the tuner and the exports use them)
-    build_tile_plan(hp2, (int32_t)m, items_A, P->planA, s);
-    build_tile_plan(hp1, (int32_t)n, items_At, P->planAt, s);
+    // the CSR plans (also kept for an ELL side: the tuner and the exports use them),
+    // the two on two host threads (each a sequential pass over its rows)
+    {
+        std::exception_ptr err;
+        std::thread t([&] {
+            try {
+                CK(cudaSetDevice(h.device));
+                AllocScope scope(s);
+                build_tile_plan(hp1, (int32_t)n, items_At, P->planAt, s);
+            } catch (...) {
+                err = std::current_exception();
+            }
+        });
+        try {
+            build_tile_plan(hp2, (int32_t)m, items_A, P->planA, s);
+        } catch (...) {
+            t.join();
+            throw;
+        }
+        t.join();
+        if (err) std::rethrow_exception(err);
+    }
     P->partA.alloc((size_t)(P->planA.npieces > 0 ? P->planA.npieces : 1) * 4);
     P->partAt.alloc((size_t)(P->planAt.npieces > 0 ? P->planAt.npieces : 1) * 4);
     P->rows_A_partials = side_partials(*P, 0, TILE_WARPS);
