@@ -84,3 +84,36 @@ def test_admission_respects_hbm_budget():
     assert 0 < out["peak_admitted_bytes"] <= budget
     assert out["jobs"] >= 3
     server.close()
+
+
+def test_lazy_stream_keeps_only_sampled_solutions():
+    """LPs built on arrival (replay with a callable) and Server(keep=...): the
+    kept requests' x and y equal those of the same stream replayed with every
+    LP built up front; the others keep their statistics only; the per-tolerance
+    latency figures cover every request."""
+    from coolpdlp import generators as G
+    from coolpdlp import serving, _abi as A
+    reqs, lps = _stream(count=16, rate=800.0, seed=3)
+    keep = {0, 5, 11}
+    built = []
+
+    def make(i):
+        built.append(i)
+        return G.request_lp(reqs[i])
+
+    lazy = serving.Server(float_type=A.VAL_F32, big_nnz=4000, max_ctas=16, keep=keep)
+    out = serving.replay(lazy, [r.arrival for r in reqs], make, [r.reltol for r in reqs])
+    full = serving.Server(float_type=A.VAL_F32, big_nnz=4000, max_ctas=16)
+    serving.replay(full, [r.arrival for r in reqs], lps, [r.reltol for r in reqs])
+    assert sorted(built) == list(range(len(reqs)))
+    assert out["status_counts"][0] == len(reqs)
+    assert sum(v["requests"] for v in out["by_tolerance"].values()) == len(reqs)
+    for i in range(len(reqs)):
+        got, ref = lazy.results[i], full.results[i]
+        assert got.stats.kkt_passes == ref.stats.kkt_passes
+        if i in keep:
+            assert np.array_equal(got.x, ref.x) and np.array_equal(got.y, ref.y)
+        else:
+            assert got.x is None and got.y is None
+    lazy.close()
+    full.close()
