@@ -24,9 +24,9 @@
 // rejected with CPDLP_ERR_UNSUPPORTED.  Host code cannot use the array's name
 // as a device address, so the address is looked up with cudaGetSymbolAddress
 // once per device (thread-safe), on that device's first call, with the device
-// current.  That first call should therefore come before any stream capture;
-// with CUDA's lazy module loading it is also the call that makes the array
-// resident, so make it before the device-memory budget is fixed.  Every call
+// current.  With CUDA's lazy module loading that first call is also the one
+// that makes the array resident, so make it before the device-memory budget
+// is fixed.  Every call
 // shares the array and it keeps the last call's contents; no part needs
 // clearing, because every slot a call reads is written earlier in the same
 // call.

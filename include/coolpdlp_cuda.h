@@ -417,11 +417,11 @@ int cpdlp_problem_spectral_norm(cpdlp_handle* h, cpdlp_problem* p, const cpdlp_p
  * cpdlp_matrix).  Its scratch is a fixed 1 MiB device array of this library,
  * shared by all calls and kept until process exit: at most 33,554,432
  * nonzeros (larger inputs return CPDLP_ERR_UNSUPPORTED).  The first call on a
- * device looks up the addresses of that array and of a validation flag (make
- * it before any stream capture; under CUDA's lazy module loading it is also
- * where the array becomes resident, so make it before fixing a memory
- * budget).  Each call blocks until its product is done: it reads the
- * validation flag back on the handle's stream.  Invalid indices return
+ * device looks up the addresses of that array and of a validation flag (under
+ * CUDA's lazy module loading it is also where the array becomes resident, so
+ * make it before fixing a memory budget).  Each call blocks until its
+ * product is done: it reads the validation flag back on the handle's
+ * stream.  Invalid indices return
  * CPDLP_ERR_ARGUMENT after the call (offending entries are skipped).  Calls
  * that overlap on the GPU race on the scratch array and on the validation
  * flag: their results can be wrong, and one call's invalid-input error can be
