@@ -1190,11 +1190,14 @@ double spectral_norm_T(Handle& h, ProblemT<V>& P, const cpdlp_params* prm, int64
         cudaGraphDestroy(g);
         CK(inst);
     }
-    // powm!: iterate while !(it > maxiter || residual <= tol); it counts iterations run
+    // powm!: iterate while !(it > maxiter || residual <= tol); it counts iterations run.
+    // Iterations are queued ahead of the host's check, 2 at first and twice as
+    // many each time a result is read, up to DEPTH: an LP that stops after 2
+    // iterations (C1 with FP32 iterates) runs no 6 extra ones.
     double theta_d = 0.0;
-    int64_t launched = 0, it = 0;
+    int64_t launched = 0, it = 0, ahead = 2;
     for (;;) {
-        while (launched - it < DEPTH && launched <= maxiter) {
+        while (launched - it < ahead && launched <= maxiter) {
             CK(cudaGraphLaunch(cleanup.exec, s));
             CK(cudaEventRecord(cleanup.ev[launched % DEPTH], s));
             launched++;
@@ -1202,6 +1205,7 @@ double spectral_norm_T(Handle& h, ProblemT<V>& P, const cpdlp_params* prm, int64
         CK(cudaEventSynchronize(cleanup.ev[it % DEPTH]));
         const PowerSlot slot = ring[it % DEPTH];
         it++;
+        ahead = std::min<int64_t>(2 * ahead, DEPTH);
         theta_d = slot.theta;
         if (it > maxiter || slot.residual <= tol || slot.residual <= rtol * slot.theta) break;
         if (now_seconds() >= deadline) break;
