@@ -70,7 +70,7 @@ class Server:
                  hbm_budget: float = 150e9, max_inflight_lps: int | None = None,
                  max_job_lps: int = 1024, big_nnz: int = 40_000, max_ctas: int | None = None,
                  single_workers: int = 32, fp32_reltol: float = 1e-4, keep=None,
-                 big_nnz_refined: int = 20_000):
+                 big_nnz_refined: int = 20_000, fp64_refined_below: int = 60_000):
         """keep: None keeps every result's x and y; otherwise a container of
         the request ids whose x and y are kept (the others keep their
         statistics only, which bounds host memory on long streams).
@@ -78,9 +78,17 @@ class Server:
         fp32_reltol take the single-LP path above this many nonzeros (instead
         of big_nnz): it has the refinement rounds, a job's FP64 phase has not
         (saturated 160-request stream: 41.7 LPs/s against 36.8-40.3 with
-        40,000 for every request)."""
+        40,000 for every request).
+        fp64_refined_below: such requests on the single-LP path with fewer
+        nonzeros run FP64 iterates from the start: their kernels are
+        latency-bound, so FP32 gains little, and the FP32 phase's stall rule
+        and the rounds can cost passes (one 22,760-nonzero 1e-8 request ran
+        into the 100,000-pass limit that plain FP64 stays under; the
+        saturated stream went from 42.4 to 43.0 LPs/s with 60,000, and to
+        35.6 with 150,000)."""
         self.keep = keep
         self.big_nnz_refined = int(big_nnz_refined)
+        self.fp64_refined_below = int(fp64_refined_below)
         self.handle = native.Handle(device)
         self.params = params if params is not None else native.default_params()
         self.params.float_type = float_type
@@ -216,11 +224,13 @@ class Server:
         if h is None:
             h = self._tls.handle = native.Handle(self.device)
         p = native.copy_params(self.params)
-        if self.float_type == A.VAL_F32:
+        if self.float_type == A.VAL_F32 and not (w.reltol < self.fp32_reltol
+                                                 and w.nnz < self.fp64_refined_below):
             # FP32 to the FP32 tolerance; FP64 for tighter targets and stalls
             p.termination_reltol = max(self.fp32_reltol, w.reltol)
             p.refine_reltol = w.reltol
         else:
+            p.float_type = A.VAL_F64
             p.termination_reltol = w.reltol
         return native.solve_lp(h, w.lp, p)
 
