@@ -24,6 +24,8 @@
 // the aligned 128-bit window may read up to 3 elements past the last row.
 #pragma once
 
+#include <atomic>
+#include <cmath>
 #include <type_traits>
 
 #include "cpdlp_common.cuh"
@@ -428,13 +430,44 @@ __global__ void __launch_bounds__(WARPS * 32, sizeof(T) == 8 ? CPDLP_F64_MIN_BLO
 
 // Launches the tile kernel on `s` with WARPS warps per block.  Reducing
 // epilogues write one row of block partials per block.
+// The unified L1 / shared memory of an SM is split by a carveout; the driver
+// picks one that fits many blocks of a kernel, which leaves the gathers'
+// L1 data cache smaller than these kernels need.  Once per kernel, outside a
+// stream capture, this asks for just the shared memory of the kernel's
+// resident blocks (by registers) and leaves the rest to L1 (C1's primal step:
+// 0.1185 -> 0.1156 ms, dual step 0.1096 -> 0.1084 ms).
+template <auto Kernel>
+void prefer_l1(int threads, cudaStream_t s) {
+    static std::atomic<int> state{0};  // 0: not yet, 1: in progress, 2: done
+    if (state.load(std::memory_order_acquire) == 2) return;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return;
+    int expected = 0;
+    if (!state.compare_exchange_strong(expected, 1)) return;
+    cudaFuncAttributes fa{};
+    int blocks = 0, dev = 0, smem_sm = 0;
+    if (cudaFuncGetAttributes(&fa, Kernel) == cudaSuccess &&
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, Kernel, threads, 0) == cudaSuccess &&
+        cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) == cudaSuccess &&
+        blocks > 0 && smem_sm > 0) {
+        const double need = (double)blocks * (double)(fa.sharedSizeBytes + 1024);
+        const int pct = std::min(100, (int)std::ceil(100.0 * need / smem_sm) + 1);
+        cudaFuncSetAttribute(Kernel, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+    }
+    cudaGetLastError();  // a refused hint leaves the driver's choice
+    state.store(2, std::memory_order_release);
+}
+
 template <int WARPS, int NVEC, class V, class T, class Epi>
 void launch_tiles_w(const TilePlan& plan, const CsrView<V, T>& view, const VecSet<T, NVEC>& xs,
                     const Epi& epi, cudaStream_t s) {
     const int64_t tasks = (int64_t)plan.ntasks + plan.nltasks;
     if (tasks == 0) return;
     const unsigned grid = (unsigned)((tasks + WARPS - 1) / WARPS);
-#define CPDLP_TILES(IT, R, M) k_tiles<IT, WARPS, NVEC, V, T, Epi, R, M><<<grid, WARPS * 32, 0, s>>>(view, xs, epi)
+#define CPDLP_TILES(IT, R, M)                                                 \
+    prefer_l1<k_tiles<IT, WARPS, NVEC, V, T, Epi, R, M>>(WARPS * 32, s);      \
+    k_tiles<IT, WARPS, NVEC, V, T, Epi, R, M><<<grid, WARPS * 32, 0, s>>>(view, xs, epi)
     if (plan.medium) {
         if (plan.rpl != 2) fail(CPDLP_ERR_ARGUMENT, "tile plan with long rows needs 64-row tiles");
         switch (plan.items) {
@@ -713,7 +746,9 @@ void launch_tiles4(const TilePlan& plan, const CsrView<V, T>& view, const T* x4,
     const int64_t tasks = (int64_t)plan.ntasks + plan.nltasks;
     if (tasks == 0) return;
     const unsigned grid = tiles4_grid(plan, WARPS, max_blocks);
-#define CPDLP_TILES4(IT, R, M) k_tiles4<IT, WARPS, V, T, Epi, R, M><<<grid, WARPS * 32, 0, s>>>(view, x4, epi)
+#define CPDLP_TILES4(IT, R, M)                                                \
+    prefer_l1<k_tiles4<IT, WARPS, V, T, Epi, R, M>>(WARPS * 32, s);           \
+    k_tiles4<IT, WARPS, V, T, Epi, R, M><<<grid, WARPS * 32, 0, s>>>(view, x4, epi)
     if (plan.medium) {
         if (plan.rpl != 2) fail(CPDLP_ERR_ARGUMENT, "tile plan with long rows needs 64-row tiles");
         switch (plan.items) {
