@@ -149,14 +149,14 @@ inline unsigned ell4_grid(int64_t rows, int warps, int64_t max_blocks) {
 
 template <int WARPS, int NVEC, class V, class T, class Epi>
 void launch_ell(const EllView<V, T>& A, const VecSet<T, NVEC>& xs, const Epi& epi, cudaStream_t s) {
-    if (A.rows == 0) return;
+    if (A.rows == 0 || tiles_dry_run()) return;
     k_ell<WARPS, NVEC, V, T, Epi><<<ell_grid(A.rows, WARPS), WARPS * 32, 0, s>>>(A, xs, epi);
     CK_LAUNCH();
 }
 template <int WARPS, class V, class T, class Epi>
 void launch_ell4(const EllView<V, T>& A, const T* x4, const Epi& epi, int64_t max_blocks,
                  cudaStream_t s) {
-    if (A.rows == 0) return;
+    if (A.rows == 0 || tiles_dry_run()) return;
     k_ell4<WARPS, V, T, Epi><<<ell4_grid(A.rows, WARPS, max_blocks), WARPS * 32, 0, s>>>(A, x4, epi);
     CK_LAUNCH();
 }

@@ -1318,6 +1318,16 @@ struct StateT : StateBase {
     void build_graph(int parity, int len) {
         cudaStream_t s = h->stream;
         cudaGraph_t g;
+        // the step kernels' L1 carveout hint (prefer_l1) is set outside a
+        // capture: walk one step's launches without launching them
+        tiles_dry_run() = true;
+        try {
+            enqueue_step(parity, coef.p, s);
+        } catch (...) {
+            tiles_dry_run() = false;
+            throw;
+        }
+        tiles_dry_run() = false;
         CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         int par = parity;
         for (int k = 0; k < len; k++) {

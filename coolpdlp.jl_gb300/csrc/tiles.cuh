@@ -436,6 +436,14 @@ __global__ void __launch_bounds__(WARPS * 32, sizeof(T) == 8 ? CPDLP_F64_MIN_BLO
 // stream capture, this asks for just the shared memory of the kernel's
 // resident blocks (by registers) and leaves the rest to L1 (C1's primal step:
 // 0.1185 -> 0.1156 ms, dual step 0.1096 -> 0.1084 ms).
+// Set while a caller walks its launch sequence only to apply prefer_l1 (the
+// step kernels, before their CUDA-graph capture): the tile launchers then
+// skip the launches themselves.
+inline bool& tiles_dry_run() {
+    static thread_local bool dry = false;
+    return dry;
+}
+
 template <auto Kernel>
 void prefer_l1(int threads, cudaStream_t s) {
     static std::atomic<int> state{0};  // 0: not yet, 1: in progress, 2: done
@@ -467,7 +475,8 @@ void launch_tiles_w(const TilePlan& plan, const CsrView<V, T>& view, const VecSe
     const unsigned grid = (unsigned)((tasks + WARPS - 1) / WARPS);
 #define CPDLP_TILES(IT, R, M)                                                 \
     prefer_l1<k_tiles<IT, WARPS, NVEC, V, T, Epi, R, M>>(WARPS * 32, s);      \
-    k_tiles<IT, WARPS, NVEC, V, T, Epi, R, M><<<grid, WARPS * 32, 0, s>>>(view, xs, epi)
+    if (!tiles_dry_run())                                                     \
+        k_tiles<IT, WARPS, NVEC, V, T, Epi, R, M><<<grid, WARPS * 32, 0, s>>>(view, xs, epi)
     if (plan.medium) {
         if (plan.rpl != 2) fail(CPDLP_ERR_ARGUMENT, "tile plan with long rows needs 64-row tiles");
         switch (plan.items) {
@@ -748,7 +757,8 @@ void launch_tiles4(const TilePlan& plan, const CsrView<V, T>& view, const T* x4,
     const unsigned grid = tiles4_grid(plan, WARPS, max_blocks);
 #define CPDLP_TILES4(IT, R, M)                                                \
     prefer_l1<k_tiles4<IT, WARPS, V, T, Epi, R, M>>(WARPS * 32, s);           \
-    k_tiles4<IT, WARPS, V, T, Epi, R, M><<<grid, WARPS * 32, 0, s>>>(view, x4, epi)
+    if (!tiles_dry_run())                                                     \
+        k_tiles4<IT, WARPS, V, T, Epi, R, M><<<grid, WARPS * 32, 0, s>>>(view, x4, epi)
     if (plan.medium) {
         if (plan.rpl != 2) fail(CPDLP_ERR_ARGUMENT, "tile plan with long rows needs 64-row tiles");
         switch (plan.items) {
