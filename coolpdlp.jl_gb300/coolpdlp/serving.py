@@ -20,9 +20,11 @@ server keeps a FIFO of arrived requests and, on every ``pump()``:
 
 Latency is measured from a request's arrival to the pump that sees it done.
 With FP32 iterates the batched path stops each LP at the FP32 tolerance and
-finishes LPs with tighter targets (and LPs whose FP32 iterates stall) in an
-FP64 phase warm-started from the FP32 solution; the single-LP path does the
-same through refine_reltol.  There is no counterpart in the reference, which
+finishes LPs with tighter targets in an FP64 phase warm-started from the FP32
+solution (LPs whose FP32 iterates stall restart cold in FP64); the single-LP
+path refines tighter targets through refine_reltol (FP32 rounds on the FP64
+residual), except that such requests under ``fp64_refined_below`` nonzeros run
+FP64 iterates from the start.  There is no counterpart in the reference, which
 solves one LP per call.
 """
 from __future__ import annotations
