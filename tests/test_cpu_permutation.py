@@ -59,3 +59,29 @@ def test_sort_rows_columns_is_stable_and_rejects_bad_csc():
     bad.A.colptr = np.array([1, 3, 3], dtype=np.int64)  # ...but not inside one column
     with pytest.raises(A.ArgumentError):
         cp.sort_rows_columns(bad)
+
+
+def test_density_order_preserves_the_solution(oracle):
+    """The property the solver's density order rests on: the LP in the order of
+    sort_rows_columns is the same LP, so the Float64 oracle solves it to the
+    same status and objective (within 1e-6 relative; the reductions run in
+    another order), and its solution mapped back through the permutations is a
+    solution of the original LP."""
+    from coolpdlp import generators as G
+    for lp in (G.random_sparse_lp(300, 600, 5, seed=8), G.powerlaw_lp(400, 800, 4800, seed=2,
+                                                                     cap=400)):
+        pv, pc, colptr, rowval, nzval = oracle.sort_rows_columns(lp)
+        sl = G.LPData(lp.m, lp.n, colptr, rowval, nzval, lp.c[pv], lp.lv[pv], lp.uv[pv],
+                      lp.lc[pc], lp.uc[pc])
+        prm = oracle.params(termination_reltol=1e-8, max_kkt_passes=1 << 40)
+        x0, _, s0 = oracle.solve(lp, prm)
+        x1, _, s1 = oracle.solve(sl, prm)
+        assert s0["termination_status"] == s1["termination_status"] == 0
+        o0, o1 = float(lp.c @ x0), float(sl.c @ x1)
+        assert abs(o0 - o1) <= 1e-6 * max(1.0, abs(o0)), (o0, o1)
+        x = np.empty(lp.n)
+        x[pv] = x1
+        ax = lp.to_scipy() @ x
+        viol = np.maximum(lp.lc - ax, 0.0) + np.maximum(ax - lp.uc, 0.0)
+        assert np.max(viol) <= 1e-5 * (1.0 + np.max(np.abs(np.where(np.isfinite(lp.uc), lp.uc,
+                                                                        0.0))))
